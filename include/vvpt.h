@@ -1,0 +1,314 @@
+/*
+ * vvpt.h — C ABI of the GB300-native offline path tracer.
+ *
+ * This is the drop-in boundary for vengine's path-traced offline renderer
+ * (kwstanths/vviewer). Everything below is plain C: pointers, sizes and POD
+ * structs, no C++ or torch types. Every entry point returns a vvpt_status and
+ * never throws; device-side failures surface through status words that the
+ * library reads back on the host.
+ *
+ * Reference interfaces replaced (paths relative to the vviewer project):
+ *   - RendererPathTracing (src/lib/vengine/core/Renderer.hpp:11-39):
+ *       renderInfo()/render()/renderProgress()/isRayTracingEnabled()
+ *       -> vvpt_render / vvpt_progress / vvpt_create
+ *   - VulkanRendererPathTracing::render() and its batch loop
+ *       (src/lib/vengine/vulkan/renderers/VulkanRendererPathTracing.cpp:121-226, 791-901)
+ *       -> vvpt_render
+ *   - The GPU-side scene buffers the shaders read (InstanceData, MaterialData,
+ *       LightData, LightInstance, SceneData, PathTracingData;
+ *       src/lib/vengine/shaders/include/structs.glsl:4-69,
+ *       src/lib/vengine/core/Scene.hpp:27-35,
+ *       src/lib/vengine/vulkan/renderers/VulkanRendererPathTracing.hpp:57-61)
+ *       -> vvpt_scene_desc / vvpt_scene_data, uploaded by vvpt_scene_upload
+ *   - TLAS/BLAS creation (src/lib/vengine/vulkan/resources/VulkanAccelerationStructure.cpp:14-279,
+ *       src/lib/vengine/vulkan/VulkanScene.cpp:306-381) -> vvpt_scene_upload
+ *   - traceRayEXT closest hit (shaders/pt/raygen.rgen.glsl:110 with the empty
+ *       any-hit of shaders/pt/rayPrimary.rahit.glsl:32-71) -> vvpt_trace_closest
+ */
+#ifndef VVPT_H
+#define VVPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VVPT_API __declspec(dllexport)
+#else
+#define VVPT_API __attribute__((visibility("default")))
+#endif
+
+/* Error model: the reference logs and breaks out of its batch loop on a
+ * fence timeout or device loss (VulkanRendererPathTracing.cpp:869-882) and
+ * returns early on an empty scene (:132-136). Here every call reports. */
+typedef enum vvpt_status {
+    VVPT_OK = 0,
+    VVPT_ERR_INVALID_ARG = 1,     /* null pointer, bad size, index out of range */
+    VVPT_ERR_OOM = 2,             /* device or host allocation failed */
+    VVPT_ERR_BUDGET_EXCEEDED = 3, /* a job does not fit the device-memory budget */
+    VVPT_ERR_TIMEOUT = 4,         /* deadline passed before the work finished */
+    VVPT_ERR_DEVICE = 5,          /* CUDA error or a device status word was set */
+    VVPT_ERR_NOT_READY = 6,       /* job still running (vvpt_poll) */
+    VVPT_ERR_EMPTY_SCENE = 7,     /* nothing to render (reference: warning + return) */
+    VVPT_ERR_UNSUPPORTED = 8
+} vvpt_status;
+
+typedef struct vvpt_ctx vvpt_ctx;
+typedef struct vvpt_scene vvpt_scene;
+
+/* ---- Scene buffers (mirrors of the reference GPU structs) ---------------- */
+
+/* Vertex, shaders/include/structs.glsl:4-12 (scalar layout, 68 bytes). */
+typedef struct vvpt_vertex {
+    float position[3];
+    float uv[2];
+    float normal[3];
+    float color[3];
+    float tangent[3];
+    float bitangent[3];
+} vvpt_vertex;
+
+/* One mesh = one BLAS (VulkanMesh.cpp:15-26). indices: 3 per triangle. */
+typedef struct vvpt_mesh_desc {
+    const vvpt_vertex *vertices;
+    uint32_t num_vertices;
+    const uint32_t *indices;
+    uint32_t num_triangles;
+} vvpt_mesh_desc;
+
+/* MaterialData, shaders/include/structs.glsl:41-52 (128 bytes).
+ * albedo: RGB albedo, A alpha. metallic_roughness_ao: R metallic, G roughness,
+ * B AO, A transparent flag. emissive: RGB colour, A intensity.
+ * textures1: albedo, metallic, roughness, AO texture indices.
+ * textures2: emissive, normal, BRDF-LUT, alpha texture indices.
+ * uv_tiling: R u tiling, G v tiling, B material type (0 PBR, 2 Lambert, 3 volume).
+ * Volumes pack sigma_a in albedo, sigma_s in metallic_roughness_ao and g in
+ * emissive[0] (src/lib/vengine/vulkan/resources/VulkanMaterial.cpp:438-483). */
+typedef struct vvpt_material {
+    float albedo[4];
+    float metallic_roughness_ao[4];
+    float emissive[4];
+    uint32_t textures1[4];
+    uint32_t textures2[4];
+    float uv_tiling[4];
+    uint32_t padding[8];
+} vvpt_material;
+
+enum {
+    VVPT_MATERIAL_PBR_STANDARD = 0,
+    VVPT_MATERIAL_LAMBERT = 2,
+    VVPT_MATERIAL_VOLUME = 3
+};
+
+/* InstanceData, src/lib/vengine/core/Instances.hpp:17-35, with the buffer
+ * device addresses replaced by a mesh index. model: column-major 4x4
+ * object-to-world. id: R object id, G front-facing volume material index,
+ * B back-facing volume material index (-1 = none). flags bit 0: the instance
+ * is in the TLAS (opaque groups and transparent objects are, light-only
+ * objects are not; VulkanScene.cpp:306-357). */
+typedef struct vvpt_instance {
+    float model[16];
+    float id[4];
+    uint32_t material_index;
+    uint32_t mesh_index;
+    uint32_t num_triangles;
+    uint32_t flags;
+} vvpt_instance;
+
+enum { VVPT_INSTANCE_IN_TLAS = 1u };
+
+/* LightData, shaders/include/structs.glsl:55-61: RGB colour, A intensity;
+ * type[0] = LightType (0 point, 1 directional). */
+typedef struct vvpt_light_data {
+    float color[4];
+    uint32_t type[4];
+    uint32_t padding[8];
+} vvpt_light_data;
+
+/* LightInstance, src/lib/vengine/core/Instances.hpp:39-44, filled as in
+ * src/lib/vengine/vulkan/VulkanInstances.cpp:66-109. info: R LightData index,
+ * G InstanceData index, A light type (0 point, 1 directional, 2 mesh).
+ * position: world position (point) or -direction source (directional: the
+ * model matrix applied to +Z) or row 0 of the model matrix (mesh);
+ * position1/position2: rows 1/2 of the model matrix (mesh). */
+typedef struct vvpt_light_instance {
+    uint32_t info[4];
+    float position[4];
+    float position1[4];
+    float position2[4];
+} vvpt_light_instance;
+
+enum {
+    VVPT_TEXTURE_RGBA8_LINEAR = 0,
+    VVPT_TEXTURE_RGBA8_SRGB = 1,
+    VVPT_TEXTURE_RGBA32F = 2
+};
+
+/* A 2D texture sampled bilinearly at LOD 0 with repeat addressing
+ * (VulkanTexture.cpp:219-230). The environment map is an equirectangular
+ * RGBA32F image looked up with the mapping of
+ * shaders/include/environmentMap.glsl:3-10. */
+typedef struct vvpt_texture_desc {
+    uint32_t width;
+    uint32_t height;
+    uint32_t format;
+    uint32_t reserved;
+    const void *data;
+} vvpt_texture_desc;
+
+typedef struct vvpt_scene_desc {
+    const vvpt_mesh_desc *meshes;
+    uint32_t num_meshes;
+    const vvpt_instance *instances;
+    uint32_t num_instances;
+    const vvpt_material *materials;
+    uint32_t num_materials;
+    const vvpt_light_data *light_data;
+    uint32_t num_light_data;
+    const vvpt_light_instance *lights; /* point/directional first, then mesh lights */
+    uint32_t num_lights;
+    const vvpt_texture_desc *textures;
+    uint32_t num_textures;
+    const vvpt_texture_desc *environment; /* may be NULL */
+} vvpt_scene_desc;
+
+/* SceneData, src/lib/vengine/core/Scene.hpp:27-35, column-major matrices,
+ * projection already flipped ([1][1] *= -1) for the render resolution
+ * (VulkanRendererPathTracing.cpp:143-170). exposure: R exposure, G environment
+ * intensity, B lens radius, A focal distance. background: RGB colour, A
+ * environment type (0 solid, 1 HDRI, 2 solid + HDRI lighting). volumes: R
+ * camera volume material index (-1 none), G znear, B zfar. */
+typedef struct vvpt_scene_data {
+    float view[16];
+    float view_inverse[16];
+    float projection[16];
+    float projection_inverse[16];
+    float exposure[4];
+    float background[4];
+    float volumes[4];
+} vvpt_scene_data;
+
+/* RendererPathTracing::RenderInfo (src/lib/vengine/core/Renderer.hpp:14-28),
+ * compute fields only; file naming and writing stay in the host adapter. */
+typedef struct vvpt_render_info {
+    uint32_t samples;    /* total samples per pixel; batches = samples / batch_size */
+    uint32_t depth;      /* max traced segments per sample */
+    uint32_t batch_size; /* samples per batch (one RNG seed per batch) */
+    uint32_t width;
+    uint32_t height;
+    uint32_t flags;      /* VVPT_RENDER_* */
+} vvpt_render_info;
+
+enum {
+    /* also return per-pixel sum over batches of the squared batch sums
+     * (radiance only), for Monte Carlo error estimates */
+    VVPT_RENDER_WANT_BATCH_M2 = 1u
+};
+
+/* Output images, RGBA32F row-major W*H*4 floats each, A = 1 (the three
+ * storage images of raygen.rgen.glsl:131-144). Any pointer may be NULL.
+ * on_device != 0: pointers are device pointers (stay valid, written in
+ * place); else host pointers (copied back before the call returns). */
+typedef struct vvpt_outputs {
+    float *radiance;
+    float *albedo;
+    float *normal;
+    float *radiance_m2;
+    int32_t on_device;
+} vvpt_outputs;
+
+/* Closest-hit ray record for vvpt_trace_closest: origin, tmin, direction, tmax. */
+typedef struct vvpt_ray {
+    float origin[3];
+    float tmin;
+    float direction[3];
+    float tmax;
+} vvpt_ray;
+
+/* Hit record: instance = InstanceData slot (gl_InstanceCustomIndexEXT),
+ * primitive = triangle index in the mesh (gl_PrimitiveID), u/v = barycentric
+ * weights of vertices 1 and 2 (hitAttributeEXT attribs). instance = 0xFFFFFFFF
+ * on a miss. */
+typedef struct vvpt_hit {
+    float t;
+    float u;
+    float v;
+    uint32_t instance;
+    uint32_t primitive;
+} vvpt_hit;
+
+/* ---- Context ------------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device` (one stream set per context).
+ * Fails with VVPT_ERR_DEVICE when no usable GPU is present (the reference
+ * throws at init without ray-tracing support, VulkanRendererPathTracing.cpp:48-51). */
+VVPT_API vvpt_status vvpt_create(int device, vvpt_ctx **out_ctx);
+VVPT_API vvpt_status vvpt_destroy(vvpt_ctx *ctx);
+/* Last error message of this context (thread-local copy owned by ctx). */
+VVPT_API const char *vvpt_last_error(vvpt_ctx *ctx);
+/* Library version string, no context needed. */
+VVPT_API const char *vvpt_version(void);
+
+/* ---- Scene --------------------------------------------------------------- */
+
+/* Uploads meshes, instances, materials, lights and textures, and builds the
+ * BLAS per mesh and the instance TLAS on the device. The scene stays resident
+ * until vvpt_scene_release. */
+VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *desc, vvpt_scene **out_scene);
+VVPT_API vvpt_status vvpt_scene_release(vvpt_ctx *ctx, vvpt_scene *scene);
+/* Bytes of device memory held by the scene (geometry, BVH, textures). */
+VVPT_API vvpt_status vvpt_scene_device_bytes(vvpt_ctx *ctx, const vvpt_scene *scene, uint64_t *out_bytes);
+
+/* ---- Render -------------------------------------------------------------- */
+
+/* One synchronous render (RendererPathTracing::render). */
+VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx,
+                                 vvpt_scene *scene,
+                                 const vvpt_scene_data *scene_data,
+                                 const vvpt_render_info *info,
+                                 vvpt_outputs *outputs);
+/* Fraction of the current/last render done, readable from any thread
+ * (RendererPathTracing::renderProgress). */
+VVPT_API vvpt_status vvpt_progress(vvpt_ctx *ctx, float *out_progress);
+
+/* Closest hit for a batch of rays against the scene (no shading). rays/hits
+ * are host pointers unless on_device != 0. */
+VVPT_API vvpt_status vvpt_trace_closest(vvpt_ctx *ctx,
+                                        vvpt_scene *scene,
+                                        const vvpt_ray *rays,
+                                        uint32_t num_rays,
+                                        vvpt_hit *hits,
+                                        int32_t on_device);
+
+/* Launch statistics of the last vvpt_render: kernels launched, wavefront
+ * iterations, segments traced, shadow and emitter rays traced. */
+typedef struct vvpt_render_stats {
+    uint64_t kernel_launches;
+    uint64_t iterations;
+    uint64_t segments;
+    uint64_t shadow_rays;
+    uint64_t emitter_rays;
+    uint64_t paths;
+    double device_ms;
+} vvpt_render_stats;
+VVPT_API vvpt_status vvpt_last_render_stats(vvpt_ctx *ctx, vvpt_render_stats *out_stats);
+
+/* Tuning knobs (path-slot pool size and blocks per SM for the wavefront
+ * kernels); 0 = automatic. */
+typedef struct vvpt_tuning {
+    uint32_t slots;
+    uint32_t blocks_per_sm;
+    uint32_t threads_per_block;
+    uint32_t iterations_per_graph;
+} vvpt_tuning;
+VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *tuning);
+VVPT_API vvpt_status vvpt_get_tuning(vvpt_ctx *ctx, vvpt_tuning *out_tuning);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VVPT_H */

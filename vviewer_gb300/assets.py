@@ -1,0 +1,311 @@
+"""Mesh and image I/O for the path tracer's host side.
+
+OBJ: the reference imports models with assimp 5.2.5 using
+aiProcess_Triangulate | aiProcess_FlipUVs | aiProcess_CalcTangentSpace and then
+flips v once more (src/lib/vengine/core/io/AssimpLoadModel.cpp:55-130, 543).
+assimp's OBJ importer emits one vertex per face corner; the two v flips cancel.
+Tangents follow assimp's published CalcTangentSpace method: a per-face tangent
+from the UV gradients, projected per corner onto the plane of that corner's
+normal, then averaged over corners that share a position when both their
+normals and tangents are within the 45 degree smoothing angle. Only the
+tangent reaches the shading frame (fixFrame overwrites the bitangent), and it
+is invariant under the v flip.
+
+RGBE: Greg Ward's shared-exponent format as written by stb_image_write
+(header "#?RADIANCE", FORMAT=32-bit_rle_rgbe, "-Y H +X W", new-style RLE
+scanlines) and decoded as stb_image does (c * 2^(e - 136)).
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+
+import numpy as np
+
+from .scene import VERTEX_DTYPE, Mesh
+
+f32 = np.float32
+
+
+# ---------------------------------------------------------------- OBJ
+
+def _parse_obj(text: str):
+    v, vt, vn = [], [], []
+    faces = []  # list of corner lists (vi, ti, ni)
+    name = "defaultobject"
+    for line in text.splitlines():
+        if not line or line[0] == "#":
+            continue
+        parts = line.split()
+        tag = parts[0]
+        if tag == "v":
+            v.append([float(x) for x in parts[1:4]])
+        elif tag == "vt":
+            vt.append([float(x) for x in parts[1:3]])
+        elif tag == "vn":
+            vn.append([float(x) for x in parts[1:4]])
+        elif tag == "o":
+            name = parts[1] if len(parts) > 1 else name
+        elif tag == "f":
+            corners = []
+            for c in parts[1:]:
+                idx = c.split("/")
+                vi = int(idx[0])
+                ti = int(idx[1]) if len(idx) > 1 and idx[1] else 0
+                ni = int(idx[2]) if len(idx) > 2 and idx[2] else 0
+                corners.append((vi, ti, ni))
+            faces.append(corners)
+    return name, np.array(v, dtype=f32).reshape(-1, 3), np.array(vt, dtype=f32).reshape(-1, 2), \
+        np.array(vn, dtype=f32).reshape(-1, 3), faces
+
+
+def _fix(i: int, n: int) -> int:
+    return i - 1 if i > 0 else n + i
+
+
+def obj_arrays(path: str | Path) -> dict:
+    """Parsed OBJ as arrays: v, vt, vn and triangulated corner indices
+    (T x 3 x 3, 1-based position/uv/normal indices, 0 = absent)."""
+    name, V, VT, VN, faces = _parse_obj(Path(path).read_text())
+    tris = []
+    for f in faces:
+        # fan triangulation (aiProcess_Triangulate on convex polygons)
+        for k in range(1, len(f) - 1):
+            tris.append((f[0], f[k], f[k + 1]))
+    corners = np.zeros((len(tris), 3, 3), dtype=np.int64)
+    for t, tri in enumerate(tris):
+        for c in range(3):
+            vi, ti, ni = tri[c]
+            corners[t, c] = (_fix(vi, len(V)) + 1, (_fix(ti, len(VT)) + 1) if ti else 0,
+                             (_fix(ni, len(VN)) + 1) if ni else 0)
+    return {"name": name, "v": V, "vt": VT, "vn": VN, "f": corners.astype(np.int32)}
+
+
+def mesh_from_obj_arrays(name: str, V: np.ndarray, VT: np.ndarray, VN: np.ndarray, F: np.ndarray) -> Mesh:
+    """Builds a Mesh with one vertex per face corner, in face order (assimp's OBJ importer)."""
+    F = np.asarray(F, dtype=np.int64).reshape(-1, 3)
+    n = F.shape[0]
+    pos = np.asarray(V, dtype=f32)[F[:, 0] - 1]
+    uv = np.zeros((n, 2), dtype=f32)
+    if len(VT):
+        ok = F[:, 1] > 0
+        uv[ok] = np.asarray(VT, dtype=f32)[F[ok, 1] - 1]
+    nrm = np.zeros((n, 3), dtype=f32)
+    if len(VN) and (F[:, 2] > 0).all():
+        nrm = np.asarray(VN, dtype=f32)[F[:, 2] - 1]
+    else:
+        p = pos.reshape(-1, 3, 3).astype(np.float64)
+        fn = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+        fn /= np.maximum(np.linalg.norm(fn, axis=1, keepdims=True), 1e-30)
+        nrm = np.repeat(fn, 3, axis=0).astype(f32)
+    # AssimpLoadModel.cpp:72: normals normalised
+    lens = np.sqrt((nrm.astype(np.float64) ** 2).sum(axis=1))
+    nrm = (nrm / np.where(lens > 0, lens, 1.0)[:, None]).astype(f32)
+    tangent, bitangent = calc_tangent_space(pos, uv, nrm)
+    verts = np.zeros(n, dtype=VERTEX_DTYPE)
+    verts["position"] = pos
+    verts["uv"] = uv  # FlipUVs then 1 - v again: net original v
+    verts["normal"] = nrm
+    verts["color"] = 1.0
+    verts["tangent"] = tangent
+    verts["bitangent"] = bitangent
+    return Mesh(name=name, vertices=verts, indices=np.arange(n, dtype=np.uint32).reshape(-1, 3))
+
+
+def load_obj(path: str | Path) -> Mesh:
+    """Loads a single-object OBJ as one Mesh in assimp's vertex order."""
+    a = obj_arrays(path)
+    return mesh_from_obj_arrays(a["name"], a["v"], a["vt"], a["vn"], a["f"].reshape(-1, 3))
+
+
+def calc_tangent_space(pos: np.ndarray, uv: np.ndarray, nrm: np.ndarray, max_angle_deg: float = 45.0):
+    """Per-corner tangents/bitangents (corners grouped in threes)."""
+    n = pos.shape[0]
+    p = pos.astype(np.float64).reshape(-1, 3, 3)
+    t = uv.astype(np.float64).reshape(-1, 3, 2)
+    v = p[:, 1] - p[:, 0]
+    w = p[:, 2] - p[:, 0]
+    sx = t[:, 1, 0] - t[:, 0, 0]
+    sy = t[:, 1, 1] - t[:, 0, 1]
+    tx = t[:, 2, 0] - t[:, 0, 0]
+    ty = t[:, 2, 1] - t[:, 0, 1]
+    dir_corr = np.where(tx * sy - ty * sx < 0.0, -1.0, 1.0)
+    degen = sx * ty == sy * tx
+    sx = np.where(degen, 0.0, sx)
+    sy = np.where(degen, 1.0, sy)
+    tx = np.where(degen, 1.0, tx)
+    ty = np.where(degen, 0.0, ty)
+    tan_f = (w * sy[:, None] - v * ty[:, None]) * dir_corr[:, None]
+    bit_f = (w * sx[:, None] - v * tx[:, None]) * dir_corr[:, None]
+    tan_c = np.repeat(tan_f, 3, axis=0)
+    bit_c = np.repeat(bit_f, 3, axis=0)
+    nn = nrm.astype(np.float64)
+    lt = tan_c - nn * (tan_c * nn).sum(1, keepdims=True)
+    lb = bit_c - nn * (bit_c * nn).sum(1, keepdims=True)
+
+    def _norm(a):
+        ln = np.sqrt((a * a).sum(1, keepdims=True))
+        ok = (ln[:, 0] > 0) & np.isfinite(ln[:, 0])
+        out = np.where(ok[:, None], a / np.where(ln > 0, ln, 1.0), np.nan)
+        return out, ok
+
+    lt, okt = _norm(lt)
+    lb, okb = _norm(lb)
+    # invalid tangents: any vector orthogonal to the normal
+    bad = ~(okt & okb)
+    if bad.any():
+        for i in np.nonzero(bad)[0]:
+            a = np.array([1.0, 0.0, 0.0]) if abs(nn[i, 0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+            tt = np.cross(nn[i], a)
+            tt /= np.linalg.norm(tt)
+            lt[i] = tt
+            lb[i] = np.cross(nn[i], tt)
+    # smoothing over corners sharing a position
+    cos_max = math.cos(math.radians(max_angle_deg))
+    keys = np.round(pos.astype(np.float64) * 1e5).astype(np.int64)
+    order = np.lexsort((keys[:, 2], keys[:, 1], keys[:, 0]))
+    ks = keys[order]
+    brk = np.nonzero(np.any(ks[1:] != ks[:-1], axis=1))[0] + 1
+    groups = np.split(order, brk)
+    out_t = lt.copy()
+    out_b = lb.copy()
+    done = np.zeros(n, dtype=bool)
+    for g in groups:
+        if len(g) == 1:
+            continue
+        for i in g:
+            if done[i]:
+                continue
+            close = [j for j in g if (nn[i] @ nn[j]) >= cos_max and (lt[i] @ lt[j]) >= cos_max]
+            st = lt[close].sum(0)
+            sb = lb[close].sum(0)
+            st /= max(np.linalg.norm(st), 1e-30)
+            sb /= max(np.linalg.norm(sb), 1e-30)
+            for j in close:
+                out_t[j] = st
+                out_b[j] = sb
+                done[j] = True
+    return out_t.astype(f32), out_b.astype(f32)
+
+
+# ---------------------------------------------------------------- RGBE (Radiance .hdr)
+
+def rgbe_encode(rgb: np.ndarray) -> np.ndarray:
+    """float RGB (H x W x 3) -> RGBE bytes (H x W x 4), stb_image_write's rule."""
+    rgb = np.asarray(rgb, dtype=np.float32)
+    m = rgb.max(axis=-1)
+    out = np.zeros(rgb.shape[:-1] + (4,), dtype=np.uint8)
+    ok = m >= 1e-32
+    mant, ex = np.frexp(m[ok].astype(np.float32))
+    scale = (mant.astype(np.float32) * np.float32(256.0) / m[ok]).astype(np.float32)
+    vals = (rgb[ok] * scale[:, None]).astype(np.float32)
+    out[ok, :3] = vals.astype(np.uint8)
+    out[ok, 3] = (ex + 128).astype(np.uint8)
+    return out
+
+
+def rgbe_decode(rgbe: np.ndarray) -> np.ndarray:
+    """RGBE bytes -> float32 RGB, stb_image's rule (no half-step offset)."""
+    rgbe = np.asarray(rgbe, dtype=np.uint8)
+    e = rgbe[..., 3].astype(np.int32)
+    f = np.where(e != 0, np.ldexp(np.float32(1.0), e - 136), 0.0).astype(np.float32)
+    return (rgbe[..., :3].astype(np.float32) * f[..., None]).astype(np.float32)
+
+
+def read_hdr_rgbe(path: str | Path) -> np.ndarray:
+    """Reads a Radiance file written with new-style RLE; returns H x W x 4 RGBE bytes."""
+    data = Path(path).read_bytes()
+    pos = 0
+    lines = []
+    while True:
+        end = data.index(b"\n", pos)
+        line = data[pos:end].decode("latin-1")
+        pos = end + 1
+        if line.startswith("-Y") or line.startswith("+Y"):
+            lines.append(line)
+            break
+        lines.append(line)
+    if not lines[0].startswith("#?RADIANCE") and not lines[0].startswith("#?RGBE"):
+        raise ValueError("not a Radiance file")
+    parts = lines[-1].split()
+    H, W = int(parts[1]), int(parts[3])
+    out = np.zeros((H, W, 4), dtype=np.uint8)
+    buf = np.frombuffer(data, dtype=np.uint8)
+    for y in range(H):
+        if (W >= 8 and W < 32768 and int(buf[pos]) == 2 and int(buf[pos + 1]) == 2
+                and (int(buf[pos + 2]) << 8 | int(buf[pos + 3])) == W):
+            pos += 4
+            for c in range(4):
+                x = 0
+                while x < W:
+                    count = int(buf[pos])
+                    pos += 1
+                    if count > 128:
+                        count -= 128
+                        out[y, x:x + count, c] = buf[pos]
+                        pos += 1
+                    else:
+                        out[y, x:x + count, c] = buf[pos:pos + count]
+                        pos += count
+                    x += count
+        else:
+            out[y] = buf[pos:pos + 4 * W].reshape(W, 4)
+            pos += 4 * W
+    return out
+
+
+def read_hdr(path: str | Path) -> np.ndarray:
+    return rgbe_decode(read_hdr_rgbe(path))
+
+
+def _rle_channel(row: np.ndarray) -> bytes:
+    """stb_image_write's run-length encoding of one scanline channel."""
+    out = bytearray()
+    n = len(row)
+    x = 0
+    while x < n:
+        r = x
+        while r + 2 < n:
+            if row[r] == row[r + 1] and row[r] == row[r + 2]:
+                break
+            r += 1
+        if r + 2 >= n:
+            r = n
+        # literals x..r
+        while x < r:
+            len_ = min(r - x, 128)
+            out.append(len_)
+            out.extend(bytes(row[x:x + len_]))
+            x += len_
+        if r + 2 < n:
+            run_end = r
+            while run_end < n and row[run_end] == row[r]:
+                run_end += 1
+            while x < run_end:
+                len_ = min(run_end - x, 127)
+                out.append(len_ + 128)
+                out.append(int(row[r]))
+                x += len_
+    return bytes(out)
+
+
+def write_hdr(path: str | Path, image: np.ndarray) -> None:
+    """Writes RGB(A) float data as an RLE Radiance file (alpha ignored)."""
+    img = np.asarray(image, dtype=np.float32)
+    H, W = img.shape[:2]
+    rgbe = rgbe_encode(img[..., :3])
+    head = f"#?RADIANCE\n# Written by stb_image_write\nFORMAT=32-bit_rle_rgbe\n\n-Y {H} +X {W}\n".encode()
+    body = bytearray()
+    for y in range(H):
+        if 8 <= W < 32768:
+            body.extend(bytes([2, 2, (W >> 8) & 0xFF, W & 0xFF]))
+            for c in range(4):
+                body.extend(_rle_channel(rgbe[y, :, c]))
+        else:
+            body.extend(rgbe[y].tobytes())
+    Path(path).write_bytes(head + bytes(body))
+
+
+def srgb_encode(linear: np.ndarray) -> np.ndarray:
+    x = np.clip(linear, 0.0, 1.0)
+    return np.where(x <= 0.0031308, x * 12.92, 1.055 * np.power(x, 1.0 / 2.4) - 0.055)

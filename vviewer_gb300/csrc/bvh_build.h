@@ -1,0 +1,39 @@
+// Host-side binned-SAH BVH builder (binary nodes). Used for every BLAS (over
+// triangles) and for the TLAS (over instance world boxes).
+//
+// Replaces the driver-built acceleration structures of the reference
+// (src/lib/vengine/vulkan/resources/VulkanAccelerationStructure.cpp:14-279,
+// built with VK_BUILD_ACCELERATION_STRUCTURE_PREFER_FAST_TRACE_BIT_KHR).
+#pragma once
+#include <stdint.h>
+#include <vector>
+
+#include "scene_gpu.h"
+
+namespace vvpt {
+
+struct Box3 {
+    float lo[3];
+    float hi[3];
+};
+
+struct BVHBuildOptions {
+    int bins = 32;          // SAH bins per axis
+    int max_leaf = 4;       // preferred leaf size
+    int max_depth = 56;     // force leaves below this depth (traversal stack bound)
+    double cost_traversal = 1.0;
+    double cost_intersect = 1.0;
+    int threads = 0;        // 0 = hardware concurrency (large builds only)
+};
+
+struct BVHBuildResult {
+    std::vector<BVHNode> nodes; // node 0 is the root
+    std::vector<uint32_t> order; // leaf order -> primitive index
+    int depth = 0;
+};
+
+// Builds a BVH over `boxes`. Always emits at least a root node (an empty
+// input gives a root with two empty children).
+BVHBuildResult build_bvh2(const std::vector<Box3> &boxes, const BVHBuildOptions &opt = BVHBuildOptions());
+
+}  // namespace vvpt

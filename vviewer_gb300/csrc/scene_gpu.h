@@ -1,0 +1,136 @@
+// Device-resident scene layout. Shared by the host-side builder (bvh_build.cpp,
+// api.cu) and the kernels. Plain structs, 16-byte aligned where the kernels do
+// 128-bit loads.
+#pragma once
+#include <stdint.h>
+
+#ifndef __CUDACC__
+struct alignas(16) float4 { float x, y, z, w; };
+struct alignas(16) int4 { int x, y, z, w; };
+#else
+#include <cuda_runtime.h>
+#endif
+
+namespace vvpt {
+
+// Binary BVH node, 64 bytes: both children's boxes plus child links, so one
+// node visit is four 128-bit loads. lxy = (l.lo.x, l.hi.x, l.lo.y, l.hi.y),
+// rxy likewise, lrz = (l.lo.z, l.hi.z, r.lo.z, r.hi.z).
+// c = (left, right, left_count, right_count): count > 0 -> leaf covering
+// primitives [index, index + count) of the leaf-ordered primitive array;
+// count == 0 -> internal node `index` (relative to the BVH's first node);
+// index == -1 -> empty child.
+struct alignas(16) BVHNode {
+    float4 lxy;
+    float4 rxy;
+    float4 lrz;
+    int4 c;
+};
+static_assert(sizeof(BVHNode) == 64, "BVHNode must be 64 bytes");
+
+// Compressed 8-wide node (80 bytes). Child boxes are quantised to 8 bits per
+// plane relative to the node origin p with per-axis power-of-two scales e.
+// imask bit i: child slot i is an internal node. Internal children are stored
+// contiguously from child_base; leaf children's triangles contiguously from
+// tri_base. meta[i]: 0 = empty slot; internal: 0b001xxxxx with xxxxx = 24 + slot
+// rank; leaf: (tri count as unary in the top 3 bits) | tri offset (5 bits).
+struct alignas(16) WideNode {
+    float px, py, pz;
+    uint8_t ex, ey, ez, imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlox[8], qloy[8], qloz[8];
+    uint8_t qhix[8], qhiy[8], qhiz[8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
+
+// Triangle in leaf order for intersection: v0.w carries the original
+// primitive index (gl_PrimitiveID) as raw bits.
+struct alignas(16) TriVerts {
+    float4 v0, v1, v2;
+};
+
+// Shading vertex: position + u, normal + v, tangent (+pad). Bitangents are not
+// kept: fixFrame (shaders/include/frame.glsl:7-36) overwrites the bitangent in
+// both of its branches, so the input value never reaches the result.
+struct alignas(16) ShadeVertex {
+    float4 pos_u;
+    float4 nrm_v;
+    float4 tan_;
+};
+
+struct MeshInfo {
+    uint32_t node_offset;   // first BVHNode of the BLAS
+    uint32_t tri_offset;    // first TriVerts (leaf order)
+    uint32_t vertex_offset; // first ShadeVertex
+    uint32_t index_offset;  // first index triple (in uint32 units / 3)
+    uint32_t num_triangles;
+    uint32_t num_nodes;
+    uint32_t pad0, pad1;
+};
+
+// Per-instance data the kernels read (128 bytes).
+struct alignas(16) DevInstance {
+    float4 w2o[3];  // world-to-object rows
+    float4 o2w[3];  // object-to-world rows
+    uint32_t node_offset;
+    uint32_t tri_offset;
+    uint32_t vertex_offset;
+    uint32_t index_offset;
+    uint32_t material;
+    uint32_t num_triangles;
+    int32_t front_volume; // id.g (-1 none)
+    int32_t back_volume;  // id.b (-1 none)
+};
+static_assert(sizeof(DevInstance) == 128, "DevInstance must be 128 bytes");
+
+struct DevMaterial {
+    float4 albedo;
+    float4 mrao;
+    float4 emissive;
+    uint32_t tex1[4];
+    uint32_t tex2[4];
+    float4 uv_tiling;
+    uint32_t padding[8];
+};
+static_assert(sizeof(DevMaterial) == 128, "DevMaterial must be 128 bytes");
+
+struct DevLightInstance {
+    uint32_t info[4];
+    float4 position;
+    float4 position1;
+    float4 position2;
+    // host-precomputed transpose(inverse(M)) rows for mesh lights (the
+    // reference computes it per sample in lightSampling.glsl:80)
+    float4 nrm0, nrm1, nrm2;
+    float4 color; // LightData colour of point/directional lights
+};
+
+struct DevTexture {
+    uint32_t width, height, format, pad;
+    uint64_t offset; // byte offset into the texel pool
+};
+
+// Everything a kernel needs about the scene.
+struct SceneView {
+    const BVHNode *nodes;      // all BLAS nodes, then TLAS nodes
+    const TriVerts *tris;
+    const ShadeVertex *verts;
+    const uint32_t *indices;   // 3 per triangle, original order
+    const DevInstance *instances;
+    const uint32_t *tlas_order; // TLAS leaf order -> instance slot
+    uint32_t tlas_root;        // node index of the TLAS root
+    uint32_t num_instances;
+    const DevMaterial *materials;
+    uint32_t num_materials;
+    const DevLightInstance *lights;
+    uint32_t num_lights;
+    const DevTexture *textures;
+    uint32_t num_textures;
+    const uint8_t *texels;
+    int32_t env_texture;       // texture index of the equirect environment, -1 none
+    uint32_t has_transparent;  // any material with the transparent flag set
+};
+
+}  // namespace vvpt

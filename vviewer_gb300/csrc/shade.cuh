@@ -1,0 +1,371 @@
+// Device-side shading building blocks of the path tracer. Each function
+// restates one function of the reference's GLSL includes (file:line given in
+// the comment above it) with the same operation order and constants.
+#pragma once
+#include "scene_gpu.h"
+#include "vmath.cuh"
+
+namespace vvpt {
+
+// shaders/include/constants.glsl:1-9
+constexpr float kEps = 0.000001f;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.31830988618379067154f;
+constexpr float kInv4Pi = 0.079577472f;
+constexpr float kPiOver2 = 1.57079632679489661923f;
+constexpr float kPiOver4 = 0.78539816339744830961f;
+// shaders/pt/defines_pt.glsl:9
+constexpr uint32_t kRussianRouletteDepth = 3;
+
+// ---- RNG: shaders/include/rng/rng_def.glsl:4-36 (Ray Tracing Gems II ch. 14)
+
+__device__ __forceinline__ float rng_to_float(uint32_t x) { return __uint_as_float(0x3f800000u | (x >> 9)) - 1.0f; }
+__device__ __forceinline__ uint32_t xorshift32(uint32_t &s)
+{
+    s ^= s << 13;
+    s ^= s >> 17;
+    s ^= s << 5;
+    return s;
+}
+__device__ __forceinline__ float rand1(uint32_t &s) { return rng_to_float(xorshift32(s)); }
+__host__ __device__ __forceinline__ uint32_t jenkins_hash(uint32_t x)
+{
+    x += x << 10;
+    x ^= x >> 6;
+    x += x << 3;
+    x ^= x >> 11;
+    x += x << 15;
+    return x;
+}
+// pixelIdx = pixel.x * resolution.x + pixel.y, kept as in rng_def.glsl:33
+__host__ __device__ __forceinline__ uint32_t init_rng(uint32_t px, uint32_t py, uint32_t resx, uint32_t frame)
+{
+    uint32_t pixel_idx = px * resx + py;
+    return jenkins_hash(pixel_idx ^ jenkins_hash(frame));
+}
+
+// ---- Sampling warps: shaders/include/sampling.glsl:3-67
+
+__device__ __forceinline__ float3 cosine_sample_hemisphere(float u0, float u1, float &pdf)
+{
+    float rx = 2.0f * u0 - 1.0f;
+    float ry = 2.0f * u1 - 1.0f;
+    float3 dir = f3(0.0f);
+    if (rx == 0.0f && ry == 0.0f) {
+        dir.x = 0.0f;
+        dir.z = 0.0f;
+    } else if (fabsf(rx) > fabsf(ry)) {
+        float r = rx;
+        float phi = kPiOver4 * (ry / rx);
+        dir.x = r * cosf(phi);
+        dir.z = r * sinf(phi);
+    } else {
+        float r = ry;
+        float phi = kPiOver2 - kPiOver4 * (rx / ry);
+        dir.x = r * cosf(phi);
+        dir.z = r * sinf(phi);
+    }
+    dir.y = sqrtf(fmaxf(0.0f, 1.0f - dir.x * dir.x - dir.z * dir.z));
+    pdf = kInvPi * dir.y;
+    pdf = fmaxf(pdf, kEps);
+    return dir;
+}
+__device__ __forceinline__ float cosine_hemisphere_pdf(float cos_theta) { return cos_theta * kInvPi; }
+__device__ __forceinline__ float2 uniform_sample_triangle(float u0, float u1)
+{
+    const float a = sqrtf(1.0f - u0);
+    return make_float2(1.0f - a, a * u1);
+}
+__device__ __forceinline__ float2 concentric_sample_disk(float u0, float u1)
+{
+    float ox = 2.0f * u0 - 1.0f, oy = 2.0f * u1 - 1.0f;
+    if (ox == 0.0f && oy == 0.0f)
+        return make_float2(0.0f, 0.0f);
+    float theta, r;
+    if (fabsf(ox) > fabsf(oy)) {
+        r = ox;
+        theta = kPiOver4 * (oy / ox);
+    } else {
+        r = oy;
+        theta = kPiOver2 - kPiOver4 * (ox / oy);
+    }
+    return make_float2(r * cosf(theta), r * sinf(theta));
+}
+
+// ---- Frames: shaders/include/frame.glsl:7-88
+
+struct Frame {
+    float3 n, t, b;
+};
+// returns `flipped`
+__device__ __forceinline__ bool fix_frame(Frame &f, const float3 &ray)
+{
+    bool flipped = false;
+    if (dot3(f.n, ray) > 0.0f) {
+        f.n = -f.n;
+        f.t = -f.t;
+        flipped = true;
+    }
+    f.n = normalize3(f.n);
+    f.t = normalize3(f.t);
+    if (fabsf(dot3(f.n, f.t)) > 0.999f) {
+        f.b = fabsf(f.n.z) < 0.999f ? f3(0.0f, 0.0f, 1.0f) : f3(1.0f, 0.0f, 0.0f);
+        f.t = cross3(f.b, f.n);
+        f.b = cross3(f.n, f.t);
+    } else {
+        f.b = cross3(f.n, f.t);
+        f.t = cross3(f.b, f.n);
+    }
+    return flipped;
+}
+__device__ __forceinline__ float3 local_to_world(const Frame &f, const float3 &v) { return f.t * v.x + f.n * v.y + f.b * v.z; }
+__device__ __forceinline__ float3 world_to_local(const Frame &f, const float3 &v)
+{
+    return f3(dot3(v, f.t), dot3(v, f.n), dot3(v, f.b));
+}
+__device__ __forceinline__ void apply_normal_to_frame(Frame &f, const float3 &local_normal)
+{
+    float3 nw = local_to_world(f, local_normal);
+    f.n = nw;
+    f.t = cross3(f.n, f.b);
+    f.b = cross3(f.t, f.n);
+}
+__device__ __forceinline__ void create_coordinate_system(const float3 &v1, float3 &v2, float3 &v3)
+{
+    if (fabsf(v1.x) > fabsf(v1.y))
+        v2 = f3(-v1.z, 0.0f, v1.x) / sqrtf(v1.x * v1.x + v1.z * v1.z);
+    else
+        v2 = f3(0.0f, v1.z, -v1.y) / sqrtf(v1.y * v1.y + v1.z * v1.z);
+    v3 = cross3(v1, v2);
+}
+// shaders/include/utils.glsl:10-14
+__device__ __forceinline__ float3 normal_from_normal_map(const float3 &c)
+{
+    float3 N = c * 2.0f - f3(1.0f);
+    return normalize3(f3(N.x, N.z, -N.y));
+}
+
+// ---- BRDFs: shaders/include/brdfs/common.glsl:3-49, pbrStandard.glsl:1-165
+
+struct PBR {
+    float3 albedo;
+    float metallic;
+    float roughness;
+};
+__device__ __forceinline__ float schlick_weight(float cos_theta)
+{
+    float m = fminf(fmaxf(1.0f - cos_theta, 0.0f), 1.0f);
+    return (m * m) * (m * m) * m;
+}
+__device__ __forceinline__ float gtr2(float ndoth, float a)
+{
+    float a2 = a * a;
+    float t = 1.0f + (a2 - 1.0f) * ndoth * ndoth;
+    return a2 / (kPi * t * t);
+}
+__device__ __forceinline__ float smith_g_ggx(float ndotv, float alpha_g)
+{
+    float a = alpha_g * alpha_g;
+    float b = ndotv * ndotv;
+    return 1.0f / (fabsf(ndotv) + fmaxf(sqrtf(a + b - a * b), kEps));
+}
+__device__ __forceinline__ float3 eval_disney_diffuse(float ndotl, float ndotv, float ldoth, const PBR &p)
+{
+    float FL = schlick_weight(ndotl);
+    float FV = schlick_weight(ndotv);
+    float Fd90 = 0.5f + 2.0f * ldoth * ldoth * p.roughness;
+    float Fd = mixf(1.0f, Fd90, FL) * mixf(1.0f, Fd90, FV);
+    return (1.0f / kPi) * Fd * p.albedo;
+}
+__device__ __forceinline__ float3 eval_disney_microfacet(float ndotl, float ndotv, float ndoth, float ldoth, const PBR &p)
+{
+    float cdlum = 0.3f * p.albedo.x + 0.6f * p.albedo.y + 0.1f * p.albedo.z;
+    float3 ctint = cdlum > 0.0f ? p.albedo / cdlum : f3(1.0f);
+    const float specular = 0.5f, specular_tint = 0.0f;
+    float3 cspec0 = mix3(specular * 0.08f * mix3(f3(1.0f), ctint, specular_tint), p.albedo, p.metallic);
+    float a = fmaxf(0.001f, p.roughness * p.roughness);
+    float Ds = gtr2(ndoth, a);
+    float FH = schlick_weight(ldoth);
+    float3 Fs = mix3(cspec0, f3(1.0f), FH);
+    float Gs = smith_g_ggx(ndotl, a);
+    Gs *= smith_g_ggx(ndotv, a);
+    return Gs * Fs * Ds;
+}
+__device__ __forceinline__ float pdf_disney_microfacet(const float3 &wi, const float3 &wo, const PBR &p)
+{
+    if (!(wo.y > 0.0f))
+        return 0.0f;
+    if (!(wi.y > 0.0f))
+        return 0.0f;
+    float3 wh = normalize3(wo + wi);
+    float ndoth = fmaxf(wh.y, kEps);
+    float alpha2 = p.roughness * p.roughness;
+    alpha2 *= alpha2;
+    float cos2 = ndoth * ndoth;
+    float denom = cos2 * (alpha2 - 1.0f) + 1.0f;
+    if (denom == 0.0f)
+        return 0.0f;
+    float pdf_distribution = alpha2 * ndoth / (kPi * denom * denom);
+    return pdf_distribution / (4.0f * dot3(wo, wh));
+}
+__device__ __forceinline__ float diffuse_sampling_ratio(const PBR &p)
+{
+    float d = fmaxf(1.0f - p.metallic, 0.1f);
+    float g = fmaxf(1.0f - p.roughness, 0.1f);
+    return d / (d + g);
+}
+__device__ __forceinline__ float3 eval_pbr(const PBR &p, const float3 &wi, const float3 &wo, const float3 &H)
+{
+    float ndotl = wi.y, ndotv = wo.y;
+    if (ndotl < 0.0f || ndotv < 0.0f)
+        return f3(0.0f);
+    float ndoth = H.y;
+    float ldoth = dot3(wi, H);
+    float3 diffuse = eval_disney_diffuse(ndotl, ndotv, ldoth, p);
+    float3 glossy = eval_disney_microfacet(ndotl, ndotv, ndoth, ldoth, p);
+    return (diffuse * (1.0f - p.metallic) + glossy) * ndotl;
+}
+__device__ __forceinline__ float pdf_pbr(const float3 &wi, const float3 &wo, const PBR &p)
+{
+    float cos_theta = wi.y;
+    if (cos_theta < 0.0f)
+        return 0.0f;
+    float pd = cosine_hemisphere_pdf(cos_theta);
+    float pm = pdf_disney_microfacet(wi, wo, p);
+    float r = diffuse_sampling_ratio(p);
+    return pd * r + pm * (1.0f - r);
+}
+// samplePBRStandard (pbrStandard.glsl:188-214): draws u0,u1 then rnd
+__device__ __forceinline__ float3 sample_pbr(float3 &wi, const float3 &wo, float &pdf, const PBR &p, float u0, float u1,
+                                             float rnd)
+{
+    pdf = 0.0f;
+    wi = f3(0.0f);
+    float r = diffuse_sampling_ratio(p);
+    if (rnd <= r) {
+        wi = cosine_sample_hemisphere(u0, u1, pdf);
+    } else {
+        float phi = (2.0f * kPi) * u1;
+        float alpha = p.roughness * p.roughness;
+        float tan2 = alpha * alpha * u0 / (1.0f - u0);
+        float cos_theta = 1.0f / sqrtf(1.0f + tan2);
+        float sin_theta = sqrtf(fmaxf(kEps, 1.0f - cos_theta * cos_theta));
+        float3 wh = f3(sin_theta * cosf(phi), cos_theta, sin_theta * sinf(phi));
+        if (!(wh.y > 0.0f))
+            wh = wh * -1.0f;
+        // reflect(-wo, wh) = -wo - 2 dot(wh, -wo) wh
+        float3 I = -wo;
+        wi = I - 2.0f * dot3(wh, I) * wh;
+        pdf = pdf_disney_microfacet(wi, wo, p);
+    }
+    float3 F = eval_pbr(p, wi, wo, normalize3(wi + wo));
+    pdf = pdf_pbr(wi, wo, p);
+    if (pdf < kEps)
+        return f3(0.0f);
+    return F;
+}
+
+// ---- MIS: shaders/pt/MIS.glsl:5-10
+__device__ __forceinline__ float power_heuristic(float fpdf, float gpdf)
+{
+    float f = fpdf, g = gpdf;
+    return (f * f) / (f * f + g * g);
+}
+
+// ---- Phase function: shaders/include/phaseFunctions.glsl:1-31
+__device__ __forceinline__ float henyey_greenstein(float cos_theta, float g)
+{
+    float denom = 1.0f + g * g + 2.0f * g * cos_theta;
+    return kInv4Pi * (1.0f - g * g) / (denom * sqrtf(denom));
+}
+__device__ __forceinline__ float hg_sample(const float3 &wo, float3 &wi, float u0, float u1, float g)
+{
+    float cos_theta;
+    if (fabsf(g) < 1e-3f) {
+        cos_theta = 1.0f - 2.0f * u0;
+    } else {
+        float sqr = (1.0f - g * g) / (1.0f + g - 2.0f * g * u0);
+        cos_theta = -(1.0f + g * g - sqr * sqr) / (2.0f * g);
+    }
+    float sin_theta = sqrtf(fmaxf(0.0f, 1.0f - cos_theta * cos_theta));
+    float phi = 2.0f * kPi * u1;
+    float3 v1, v2;
+    create_coordinate_system(wo, v1, v2);
+    wi = sin_theta * cosf(phi) * v1 + sin_theta * sinf(phi) * v2 + cos_theta * wo;
+    return henyey_greenstein(cos_theta, g);
+}
+
+// ---- Textures: bilinear, repeat addressing, LOD 0 (sampler of
+// src/lib/vengine/vulkan/resources/VulkanTexture.cpp:219-230)
+
+__device__ __forceinline__ float srgb_to_linear(float c)
+{
+    return c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
+}
+__device__ __forceinline__ float4 texel(const SceneView &s, const DevTexture &t, int x, int y)
+{
+    size_t i = (size_t)y * t.width + (size_t)x;
+    if (t.format == 2) {
+        return __ldg(reinterpret_cast<const float4 *>(s.texels + t.offset) + i);
+    }
+    uchar4 c = __ldg(reinterpret_cast<const uchar4 *>(s.texels + t.offset) + i);
+    float4 v = make_float4(c.x / 255.0f, c.y / 255.0f, c.z / 255.0f, c.w / 255.0f);
+    if (t.format == 1) {
+        v.x = srgb_to_linear(v.x);
+        v.y = srgb_to_linear(v.y);
+        v.z = srgb_to_linear(v.z);
+    }
+    return v;
+}
+__device__ __forceinline__ int wrap_repeat(int i, int n)
+{
+    int m = i % n;
+    return m < 0 ? m + n : m;
+}
+__device__ __forceinline__ float4 tex2d(const SceneView &s, uint32_t index, float u, float v, bool clamp_v = false)
+{
+    if (index >= s.num_textures)
+        return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    const DevTexture t = s.textures[index];
+    if (t.width == 1 && t.height == 1)
+        return texel(s, t, 0, 0);
+    float x = u * (float)t.width - 0.5f;
+    float y = v * (float)t.height - 0.5f;
+    float fx = floorf(x), fy = floorf(y);
+    float ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    int x1 = x0 + 1, y1 = y0 + 1;
+    x0 = wrap_repeat(x0, (int)t.width);
+    x1 = wrap_repeat(x1, (int)t.width);
+    if (clamp_v) {
+        y0 = min(max(y0, 0), (int)t.height - 1);
+        y1 = min(max(y1, 0), (int)t.height - 1);
+    } else {
+        y0 = wrap_repeat(y0, (int)t.height);
+        y1 = wrap_repeat(y1, (int)t.height);
+    }
+    float4 c00 = texel(s, t, x0, y0), c10 = texel(s, t, x1, y0);
+    float4 c01 = texel(s, t, x0, y1), c11 = texel(s, t, x1, y1);
+    float w00 = (1.0f - ax) * (1.0f - ay), w10 = ax * (1.0f - ay), w01 = (1.0f - ax) * ay, w11 = ax * ay;
+    return make_float4(c00.x * w00 + c10.x * w10 + c01.x * w01 + c11.x * w11,
+                       c00.y * w00 + c10.y * w10 + c01.y * w01 + c11.y * w11,
+                       c00.z * w00 + c10.z * w10 + c01.z * w01 + c11.z * w11,
+                       c00.w * w00 + c10.w * w10 + c01.w * w01 + c11.w * w11);
+}
+
+// Environment lookup: equirect mapping of shaders/include/environmentMap.glsl:3-10
+// (the mapping the reference uses to fill its cubemap), read directly.
+__device__ __forceinline__ float3 env_lookup(const SceneView &s, const float3 &dir)
+{
+    if (s.env_texture < 0)
+        return f3(0.0f);
+    float3 v = normalize3(dir);
+    float u = atan2f(v.z, v.x) * 0.1591f + 0.5f;
+    float w = asinf(fminf(fmaxf(v.y, -1.0f), 1.0f)) * 0.3183f + 0.5f;
+    float x = u + 0.25f;
+    u = x - floorf(x);
+    float4 c = tex2d(s, (uint32_t)s.env_texture, u, w, true);
+    return f3(c.x, c.y, c.z);
+}
+
+}  // namespace vvpt

@@ -1,0 +1,360 @@
+// Closest-hit traversal of the two-level BVH (instance TLAS over per-mesh BLAS)
+// with a watertight ray/triangle test.
+//
+// Semantics replaced: traceRayEXT against a TLAS whose instances have culling
+// disabled (src/lib/vengine/vulkan/VulkanScene.cpp:375) and an any-hit shader
+// that accepts every candidate (shaders/pt/rayPrimary.rahit.glsl:32-71), i.e.
+// plain closest hit over [tmin, tmax]. Ties in t are broken by the smallest
+// (instance slot, primitive index) so the result does not depend on BVH
+// layout; the CPU oracle applies the same rule.
+//
+// The triangle test is the watertight algorithm of Woop, Benthin and Wald,
+// "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013, written with
+// explicitly rounded operations (no FMA contraction) so that it gives the same
+// bits as a plain IEEE float evaluation on the host.
+#pragma once
+#include "scene_gpu.h"
+#include "vmath.cuh"
+
+namespace vvpt {
+
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+constexpr int kTlasStack = 32;
+constexpr int kBlasStack = 64;
+// device status word bits
+constexpr uint32_t kErrStackOverflow = 1u;
+constexpr uint32_t kErrLoopCap = 2u;
+
+struct Hit {
+    float t, u, v;
+    uint32_t inst, prim;
+};
+
+// Per-ray constants of the watertight test.
+struct WatertightRay {
+    float3 org;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ WatertightRay wt_setup(const float3 &o, const float3 &d)
+{
+    WatertightRay r;
+    r.org = o;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    float dz = comp(d, kz);
+    if (dz < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = __fdiv_rn(comp(d, kx), dz);
+    r.Sy = __fdiv_rn(comp(d, ky), dz);
+    r.Sz = __fdiv_rn(1.0f, dz);
+    return r;
+}
+
+__device__ __forceinline__ float sel(const float4 &v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ float sel3(const float3 &v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// Returns true and writes t/u/v when the triangle is hit with t in
+// [tmin, best_t]; u, v are the barycentric weights of v1 and v2.
+__device__ __forceinline__ bool wt_intersect(const WatertightRay &r, const float4 &p0, const float4 &p1,
+                                             const float4 &p2, float tmin, float best_t, float &t_out,
+                                             float &u_out, float &v_out)
+{
+    const float ox = sel3(r.org, r.kx), oy = sel3(r.org, r.ky), oz = sel3(r.org, r.kz);
+    const float Ax = __fsub_rn(sel(p0, r.kx), ox), Ay = __fsub_rn(sel(p0, r.ky), oy), Az0 = __fsub_rn(sel(p0, r.kz), oz);
+    const float Bx = __fsub_rn(sel(p1, r.kx), ox), By = __fsub_rn(sel(p1, r.ky), oy), Bz0 = __fsub_rn(sel(p1, r.kz), oz);
+    const float Cx = __fsub_rn(sel(p2, r.kx), ox), Cy = __fsub_rn(sel(p2, r.ky), oy), Cz0 = __fsub_rn(sel(p2, r.kz), oz);
+    const float ax = __fsub_rn(Ax, __fmul_rn(r.Sx, Az0)), ay = __fsub_rn(Ay, __fmul_rn(r.Sy, Az0));
+    const float bx = __fsub_rn(Bx, __fmul_rn(r.Sx, Bz0)), by = __fsub_rn(By, __fmul_rn(r.Sy, Bz0));
+    const float cx = __fsub_rn(Cx, __fmul_rn(r.Sx, Cz0)), cy = __fsub_rn(Cy, __fmul_rn(r.Sy, Cz0));
+    float U = __fsub_rn(__fmul_rn(cx, by), __fmul_rn(cy, bx));
+    float V = __fsub_rn(__fmul_rn(ax, cy), __fmul_rn(ay, cx));
+    float W = __fsub_rn(__fmul_rn(bx, ay), __fmul_rn(by, ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // edge case: redo the 2D edge tests in double precision
+        double cxby = __dmul_rn((double)cx, (double)by), cybx = __dmul_rn((double)cy, (double)bx);
+        U = (float)__dsub_rn(cxby, cybx);
+        double axcy = __dmul_rn((double)ax, (double)cy), aycx = __dmul_rn((double)ay, (double)cx);
+        V = (float)__dsub_rn(axcy, aycx);
+        double bxay = __dmul_rn((double)bx, (double)ay), byax = __dmul_rn((double)by, (double)ax);
+        W = (float)__dsub_rn(bxay, byax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f))
+        return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f)
+        return false;
+    const float az = __fmul_rn(r.Sz, Az0), bz = __fmul_rn(r.Sz, Bz0), cz = __fmul_rn(r.Sz, Cz0);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, az), __fmul_rn(V, bz)), __fmul_rn(W, cz));
+    const float rcp = __fdiv_rn(1.0f, det);
+    const float t = __fmul_rn(T, rcp);
+    if (!(t >= tmin) || !(t <= best_t))
+        return false;
+    t_out = t;
+    u_out = __fmul_rn(V, rcp);
+    v_out = __fmul_rn(W, rcp);
+    return true;
+}
+
+// Strictly after `a` in (t, instance, primitive) order; a.inst == kNoHit
+// means no constraint. Used to walk any-hit candidates nearest first.
+__device__ __forceinline__ bool is_after(float t, uint32_t inst, uint32_t prim, const Hit &a)
+{
+    if (a.inst == kNoHit)
+        return true;
+    if (t != a.t)
+        return t > a.t;
+    if (inst != a.inst)
+        return inst > a.inst;
+    return prim > a.prim;
+}
+
+__device__ __forceinline__ bool better(float t, uint32_t inst, uint32_t prim, const Hit &h)
+{
+    if (t != h.t)
+        return t < h.t;
+    if (inst != h.inst)
+        return inst < h.inst;
+    return prim < h.prim;
+}
+
+// Conservative slab test (Pharr, Jakob, Humphreys, PBRT 3rd ed. sec. 3.9.2:
+// (lo - o) * invd with tfar scaled by 1 + 2*gamma(3)). Returns both children's
+// entry distances; a child is missed when its entry is +inf.
+__device__ __forceinline__ void box2(const BVHNode &n, const float3 &o, const float3 &invd, float tmin, float tmax,
+                                     float &tl, float &tr)
+{
+    const float kScale = 1.0f + 2.0f * 3.5762793e-07f; // 1 + 2*gamma(3), gamma(3) = 3u/(1-3u), u = 2^-24
+    float lx0 = __fmul_rn(__fsub_rn(n.lxy.x, o.x), invd.x), lx1 = __fmul_rn(__fsub_rn(n.lxy.y, o.x), invd.x);
+    float ly0 = __fmul_rn(__fsub_rn(n.lxy.z, o.y), invd.y), ly1 = __fmul_rn(__fsub_rn(n.lxy.w, o.y), invd.y);
+    float lz0 = __fmul_rn(__fsub_rn(n.lrz.x, o.z), invd.z), lz1 = __fmul_rn(__fsub_rn(n.lrz.y, o.z), invd.z);
+    float rx0 = __fmul_rn(__fsub_rn(n.rxy.x, o.x), invd.x), rx1 = __fmul_rn(__fsub_rn(n.rxy.y, o.x), invd.x);
+    float ry0 = __fmul_rn(__fsub_rn(n.rxy.z, o.y), invd.y), ry1 = __fmul_rn(__fsub_rn(n.rxy.w, o.y), invd.y);
+    float rz0 = __fmul_rn(__fsub_rn(n.lrz.z, o.z), invd.z), rz1 = __fmul_rn(__fsub_rn(n.lrz.w, o.z), invd.z);
+    float lnear = fmaxf(fmaxf(fminf(lx0, lx1), fminf(ly0, ly1)), fmaxf(fminf(lz0, lz1), tmin));
+    float lfar = fminf(fminf(fmaxf(lx0, lx1), fmaxf(ly0, ly1)), fminf(fmaxf(lz0, lz1), tmax)) * kScale;
+    float rnear = fmaxf(fmaxf(fminf(rx0, rx1), fminf(ry0, ry1)), fmaxf(fminf(rz0, rz1), tmin));
+    float rfar = fminf(fminf(fmaxf(rx0, rx1), fmaxf(ry0, ry1)), fminf(fmaxf(rz0, rz1), tmax)) * kScale;
+    // empty boxes (lo > hi) give near > far
+    tl = (lnear <= lfar && n.lxy.x <= n.lxy.y) ? lnear : __int_as_float(0x7f800000);
+    tr = (rnear <= rfar && n.rxy.x <= n.rxy.y) ? rnear : __int_as_float(0x7f800000);
+}
+
+__device__ __forceinline__ BVHNode load_node(const BVHNode *nodes, int idx)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
+    BVHNode n;
+    n.lxy = __ldg(p + 0);
+    n.rxy = __ldg(p + 1);
+    n.lrz = __ldg(p + 2);
+    float4 c = __ldg(p + 3);
+    n.c = make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), __float_as_int(c.w));
+    return n;
+}
+
+__device__ __forceinline__ float3 safe_inv(const float3 &d)
+{
+    return f3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+}
+
+// Object-space ray of an instance, with explicitly rounded arithmetic so the
+// host oracle reproduces it exactly: ((m0*x + m1*y) + m2*z) + m3.
+__device__ __forceinline__ float3 wt_xform_point(const float4 *rows, const float3 &p)
+{
+    float3 r;
+    r.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(rows[0].x, p.x), __fmul_rn(rows[0].y, p.y)), __fmul_rn(rows[0].z, p.z)), rows[0].w);
+    r.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(rows[1].x, p.x), __fmul_rn(rows[1].y, p.y)), __fmul_rn(rows[1].z, p.z)), rows[1].w);
+    r.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(rows[2].x, p.x), __fmul_rn(rows[2].y, p.y)), __fmul_rn(rows[2].z, p.z)), rows[2].w);
+    return r;
+}
+__device__ __forceinline__ float3 wt_xform_vector(const float4 *rows, const float3 &v)
+{
+    float3 r;
+    r.x = __fadd_rn(__fadd_rn(__fmul_rn(rows[0].x, v.x), __fmul_rn(rows[0].y, v.y)), __fmul_rn(rows[0].z, v.z));
+    r.y = __fadd_rn(__fadd_rn(__fmul_rn(rows[1].x, v.x), __fmul_rn(rows[1].y, v.y)), __fmul_rn(rows[1].z, v.z));
+    r.z = __fadd_rn(__fadd_rn(__fmul_rn(rows[2].x, v.x), __fmul_rn(rows[2].y, v.y)), __fmul_rn(rows[2].z, v.z));
+    return r;
+}
+
+// Walks one BLAS in object space, updating `best`. Returns false on stack overflow.
+__device__ __forceinline__ bool traverse_blas(const SceneView &s, const DevInstance &inst, uint32_t inst_id,
+                                              const float3 &o, const float3 &d, float tmin, const Hit &after, Hit &best)
+{
+    const float3 invd = safe_inv(d);
+    const WatertightRay wr = wt_setup(o, d);
+    const BVHNode *nodes = s.nodes + inst.node_offset;
+    const TriVerts *tris = s.tris + inst.tri_offset;
+    const float box_tmin = after.inst == kNoHit ? tmin : fmaxf(tmin, after.t);
+    int stack[kBlasStack];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        BVHNode n = load_node(nodes, node);
+        float tl, tr;
+        box2(n, o, invd, box_tmin, best.t, tl, tr);
+        int next = -1;
+        // leaves are intersected right away; internal children are descended
+        // nearest first
+        int push[2];
+        float pusht[2];
+        int np = 0;
+        const bool hl = tl <= best.t * 1.0000005f && n.c.x >= 0;
+        const bool hr = tr <= best.t * 1.0000005f && n.c.y >= 0;
+        if (hl) {
+            if (n.c.z > 0) {
+                for (int k = n.c.x; k < n.c.x + n.c.z; k++) {
+                    const float4 *tp = reinterpret_cast<const float4 *>(tris + k);
+                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                    float t, u, v;
+                    uint32_t prim = __float_as_uint(p0.w);
+                    if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
+                        is_after(t, inst_id, prim, after)) {
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.inst = inst_id;
+                        best.prim = prim;
+                    }
+                }
+            } else {
+                push[np] = n.c.x;
+                pusht[np++] = tl;
+            }
+        }
+        if (hr) {
+            if (n.c.w > 0) {
+                for (int k = n.c.y; k < n.c.y + n.c.w; k++) {
+                    const float4 *tp = reinterpret_cast<const float4 *>(tris + k);
+                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                    float t, u, v;
+                    uint32_t prim = __float_as_uint(p0.w);
+                    if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
+                        is_after(t, inst_id, prim, after)) {
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.inst = inst_id;
+                        best.prim = prim;
+                    }
+                }
+            } else {
+                push[np] = n.c.y;
+                pusht[np++] = tr;
+            }
+        }
+        if (np == 2) {
+            int nearc = pusht[0] <= pusht[1] ? push[0] : push[1];
+            int farc = pusht[0] <= pusht[1] ? push[1] : push[0];
+            if (sp >= kBlasStack)
+                return false;
+            stack[sp++] = farc;
+            next = nearc;
+        } else if (np == 1) {
+            next = push[0];
+        }
+        if (next < 0) {
+            if (sp == 0)
+                break;
+            next = stack[--sp];
+        }
+        node = next;
+    }
+    return true;
+}
+
+// Closest hit over all TLAS instances among candidates strictly after
+// `after`. `err` receives status bits.
+__device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
+                                           const Hit &after, uint32_t &err)
+{
+    Hit best;
+    best.t = tmax;
+    best.u = best.v = 0.0f;
+    best.inst = kNoHit;
+    best.prim = kNoHit;
+    const float3 invd = safe_inv(d);
+    const BVHNode *nodes = s.nodes + s.tlas_root;
+    const float box_tmin = after.inst == kNoHit ? tmin : fmaxf(tmin, after.t);
+    int stack[kTlasStack];
+    int sp = 0;
+    int node = 0;
+    for (;;) {
+        BVHNode n = load_node(nodes, node);
+        float tl, tr;
+        box2(n, o, invd, box_tmin, best.t, tl, tr);
+        int push[2];
+        float pusht[2];
+        int np = 0;
+        const bool hl = tl <= best.t * 1.0000005f && n.c.x >= 0;
+        const bool hr = tr <= best.t * 1.0000005f && n.c.y >= 0;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            const bool h = side == 0 ? hl : hr;
+            const int idx = side == 0 ? n.c.x : n.c.y;
+            const int cnt = side == 0 ? n.c.z : n.c.w;
+            if (!h)
+                continue;
+            if (cnt > 0) {
+                for (int k = idx; k < idx + cnt; k++) {
+                    uint32_t id = __ldg(s.tlas_order + k);
+                    const DevInstance &inst = s.instances[id];
+                    float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
+                    float3 oo = wt_xform_point(rows, o);
+                    float3 od = wt_xform_vector(rows, d);
+                    if (!traverse_blas(s, inst, id, oo, od, tmin, after, best))
+                        err |= kErrStackOverflow;
+                }
+            } else {
+                push[np] = idx;
+                pusht[np++] = side == 0 ? tl : tr;
+            }
+        }
+        int next = -1;
+        if (np == 2) {
+            int nearc = pusht[0] <= pusht[1] ? push[0] : push[1];
+            int farc = pusht[0] <= pusht[1] ? push[1] : push[0];
+            if (sp >= kTlasStack) {
+                err |= kErrStackOverflow;
+                break;
+            }
+            stack[sp++] = farc;
+            next = nearc;
+        } else if (np == 1) {
+            next = push[0];
+        }
+        if (next < 0) {
+            if (sp == 0)
+                break;
+            next = stack[--sp];
+        }
+        node = next;
+    }
+    return best;
+}
+
+__device__ __forceinline__ Hit no_hit()
+{
+    Hit h;
+    h.t = -1.0f;
+    h.u = h.v = 0.0f;
+    h.inst = kNoHit;
+    h.prim = kNoHit;
+    return h;
+}
+
+__device__ __forceinline__ Hit trace_closest(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
+                                             uint32_t &err)
+{
+    return trace_after(s, o, d, tmin, tmax, no_hit(), err);
+}
+
+}  // namespace vvpt

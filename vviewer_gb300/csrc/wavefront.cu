@@ -1,0 +1,1084 @@
+// Wavefront integrator kernels: regen (camera rays), extend (closest hit),
+// shade (surface / medium / miss events, light and BSDF sampling, Russian
+// roulette) and connect (shadow rays and BSDF-direction emitter rays).
+//
+// One iteration of the five kernels advances every live path by one traced
+// segment, i.e. one pass of the `for d < depth` loop of
+// src/lib/vengine/shaders/pt/raygen.rgen.glsl:100-124 with the closest-hit /
+// miss shader that follows it. The shadow and emitter rays the reference
+// traces inside its hit shaders (lightSampling.glsl:108-144,
+// next_event_estimation.glsl:1-33) are deferred to `connect`; they consume no
+// random numbers, so the RNG stream per path is the reference's.
+#include "shade.cuh"
+#include "traverse.cuh"
+#include "wavefront.cuh"
+
+namespace vvpt {
+
+// path flag bits
+constexpr uint32_t F_INSIDE = 1u;       // rayPayloadPrimary.insideVolume
+constexpr uint32_t F_DONE = 2u;         // sample finished, finalize in regen
+constexpr uint32_t F_ITEM = 4u;         // slot holds a work item
+constexpr uint32_t F_SHADOW = 8u;       // pending shadow connection
+constexpr uint32_t F_NEE = 16u;         // pending emitter connection
+constexpr int kDepthShift = 8;          // recursionDepth d
+constexpr int kSurfShift = 16;          // surfaceDepth
+constexpr uint32_t kByteMask = 0xFFu;
+
+constexpr float kExtTmin = 0.001f;      // raygen.rgen.glsl:110
+constexpr float kExtTmax = 10000.0f;
+constexpr float kConnTmin = 0.0001f;    // lightSampling.glsl:112, next_event_estimation.glsl:3
+constexpr int kCandidateCap = 1024;     // per-segment candidate bound for any-hit loops
+
+// Warp-aggregated queue append. Must be called by all 32 lanes of the warp
+// at a convergence point (the kernels below keep their loop bounds
+// warp-uniform); lanes with want == false get no slot.
+__device__ __forceinline__ uint32_t warp_append_all(bool want, uint32_t *counter)
+{
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    const int lane = threadIdx.x & 31;
+    const int leader = mask ? __ffs(mask) - 1 : 0;
+    uint32_t base = 0;
+    if (want && lane == leader)
+        base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ float4 mat4_mul(const float4 *cols, float x, float y, float z, float w)
+{
+    return make_float4(cols[0].x * x + cols[1].x * y + cols[2].x * z + cols[3].x * w,
+                       cols[0].y * x + cols[1].y * y + cols[2].y * z + cols[3].y * w,
+                       cols[0].z * x + cols[1].z * y + cols[2].z * z + cols[3].z * w,
+                       cols[0].w * x + cols[1].w * y + cols[2].w * z + cols[3].w * w);
+}
+
+// ---------------------------------------------------------------------------
+// Hit reconstruction (shaders/pt/process_hit.glsl:1-17, construct_frame.glsl:1-15)
+
+struct SurfaceHit {
+    float3 wpos;
+    float2 uv;
+    Frame frame;
+    bool flipped;
+    uint32_t material;
+    int32_t front_volume, back_volume;
+};
+
+__device__ __forceinline__ void fetch_triangle(const SceneView &s, const DevInstance &inst, uint32_t prim,
+                                               ShadeVertex &a, ShadeVertex &b, ShadeVertex &c)
+{
+    const uint32_t *ix = s.indices + inst.index_offset + 3u * prim;
+    uint32_t i0 = __ldg(ix), i1 = __ldg(ix + 1), i2 = __ldg(ix + 2);
+    const ShadeVertex *v = s.verts + inst.vertex_offset;
+    const float4 *p0 = reinterpret_cast<const float4 *>(v + i0);
+    const float4 *p1 = reinterpret_cast<const float4 *>(v + i1);
+    const float4 *p2 = reinterpret_cast<const float4 *>(v + i2);
+    a.pos_u = __ldg(p0); a.nrm_v = __ldg(p0 + 1); a.tan_ = __ldg(p0 + 2);
+    b.pos_u = __ldg(p1); b.nrm_v = __ldg(p1 + 1); b.tan_ = __ldg(p1 + 2);
+    c.pos_u = __ldg(p2); c.nrm_v = __ldg(p2 + 1); c.tan_ = __ldg(p2 + 2);
+}
+
+__device__ __forceinline__ Affine34 rows_of(const float4 *r) { return Affine34{r[0], r[1], r[2]}; }
+
+// Full hit record with the shading frame; `ray_dir` is gl_WorldRayDirectionEXT.
+__device__ __forceinline__ SurfaceHit make_surface_hit(const SceneView &s, uint32_t inst_id, uint32_t prim, float hu,
+                                                       float hv, const float3 &ray_dir)
+{
+    const DevInstance &inst = s.instances[inst_id];
+    ShadeVertex a, b, c;
+    fetch_triangle(s, inst, prim, a, b, c);
+    const float bx = 1.0f - hu - hv, by = hu, bz = hv;
+    SurfaceHit h;
+    h.uv = make_float2(a.pos_u.w * bx + b.pos_u.w * by + c.pos_u.w * bz, a.nrm_v.w * bx + b.nrm_v.w * by + c.nrm_v.w * bz);
+    float3 lp = f3(a.pos_u) * bx + f3(b.pos_u) * by + f3(c.pos_u) * bz;
+    Affine34 o2w = rows_of(inst.o2w), w2o = rows_of(inst.w2o);
+    h.wpos = xform_point(o2w, lp);
+    float3 ln = f3(a.nrm_v) * bx + f3(b.nrm_v) * by + f3(c.nrm_v) * bz;
+    float3 lt = f3(a.tan_) * bx + f3(b.tan_) * by + f3(c.tan_) * bz;
+    h.frame.n = normalize3(xform_normal_transposed(w2o, ln));
+    h.frame.t = normalize3(xform_normal_transposed(w2o, lt));
+    h.frame.b = f3(0.0f, 0.0f, 1.0f); // overwritten by fix_frame in both branches
+    h.flipped = fix_frame(h.frame, ray_dir);
+    h.material = inst.material;
+    h.front_volume = inst.front_volume;
+    h.back_volume = inst.back_volume;
+    return h;
+}
+
+__device__ __forceinline__ float3 material_emissive(const SceneView &s, const DevMaterial &m, float2 tuv)
+{
+    float4 te = tex2d(s, m.tex2[0], tuv.x, tuv.y);
+    return (m.emissive.w * f3(m.emissive)) * f3(te);
+}
+__device__ __forceinline__ float material_alpha(const SceneView &s, const DevMaterial &m, float2 tuv)
+{
+    return m.albedo.w * tex2d(s, m.tex2[3], tuv.x, tuv.y).x;
+}
+
+// ---------------------------------------------------------------------------
+// Light sampling (shaders/pt/lightSampling.glsl:1-106), without the shadow
+// trace, which `connect` performs.
+
+struct LightSample {
+    float3 dir;
+    float3 radiance;
+    float pdf;
+    float tmax;
+    bool delta;
+};
+
+__device__ __forceinline__ LightSample sample_light(const SceneView &s, const RenderParams &p, const float3 &origin,
+                                                    uint32_t &rng)
+{
+    LightSample ls;
+    ls.delta = true;
+    ls.radiance = f3(0.0f);
+    ls.pdf = 1.0f;
+    ls.dir = f3(0.0f);
+    ls.tmax = 10000.0f;
+    const uint32_t total = p.num_lights;
+    if (total == 0)
+        return ls;
+    float pdf = 1.0f / (float)total;
+    uint32_t li = (uint32_t)(rand1(rng) * (float)total);
+    if (li >= total)
+        li = total - 1;
+    const DevLightInstance &L = s.lights[li];
+    const uint32_t type = L.info[3];
+    if (type == 0) {
+        float3 lp = f3(L.position);
+        float3 dir = lp - origin;
+        float tmax = length3(dir);
+        ls.tmax = tmax;
+        ls.dir = dir / tmax;
+        float dist = length3(origin - lp);
+        ls.radiance = f3(L.color) * (1.0f / (dist * dist)) * L.color.w;
+        ls.pdf = pdf * 1.0f;
+        ls.delta = true;
+    } else if (type == 1) {
+        ls.dir = -f3(L.position);
+        ls.tmax = p.zfar;
+        ls.radiance = f3(L.color) * L.color.w;
+        ls.pdf = pdf * 1.0f;
+        ls.delta = true;
+    } else if (type == 2) {
+        const uint32_t mesh_inst = L.info[1];
+        const DevInstance &inst = s.instances[mesh_inst];
+        const DevMaterial &m = s.materials[inst.material];
+        uint32_t tri = (uint32_t)(rand1(rng) * (float)inst.num_triangles);
+        if (tri >= inst.num_triangles)
+            tri = inst.num_triangles - 1;
+        float tri_pdf = 1.0f / (float)inst.num_triangles;
+        float u0 = rand1(rng);
+        float u1 = rand1(rng);
+        float2 bc = uniform_sample_triangle(u0, u1);
+        float b0 = bc.x, b1 = bc.y, b2 = 1.0f - bc.x - bc.y;
+        ShadeVertex a, b, c;
+        fetch_triangle(s, inst, tri, a, b, c);
+        Affine34 M{L.position, L.position1, L.position2};
+        float3 p0 = xform_point(M, f3(a.pos_u)), p1 = xform_point(M, f3(b.pos_u)), p2 = xform_point(M, f3(c.pos_u));
+        float area = 0.5f * length3(cross3(p1 - p0, p2 - p0));
+        float point_pdf = 1.0f / area;
+        float3 sp = f3(a.pos_u) * b0 + f3(b.pos_u) * b1 + f3(c.pos_u) * b2;
+        float3 sn = f3(a.nrm_v) * b0 + f3(b.nrm_v) * b1 + f3(c.nrm_v) * b2;
+        float2 suv = make_float2(a.pos_u.w * b0 + b.pos_u.w * b1 + c.pos_u.w * b2,
+                                 a.nrm_v.w * b0 + b.nrm_v.w * b1 + c.nrm_v.w * b2);
+        sp = xform_point(M, sp);
+        Affine34 N{L.nrm0, L.nrm1, L.nrm2};
+        sn = xform_vector(N, sn);
+        float3 dir = sp - origin;
+        float tmax = length3(dir);
+        ls.tmax = tmax;
+        ls.dir = dir / tmax;
+        float dp = dot3(-ls.dir, sn);
+        if (dp > 0.0f) {
+            float2 tuv = make_float2(suv.x * m.uv_tiling.x, suv.y * m.uv_tiling.y);
+            ls.radiance = material_emissive(s, m, tuv);
+            float dist = length3(origin - sp);
+            ls.pdf = pdf * tri_pdf * point_pdf * (dist * dist) / dp;
+        } else {
+            ls.radiance = f3(0.0f);
+            ls.pdf = 0.0f;
+        }
+        ls.delta = false;
+    }
+    return ls;
+}
+
+// ---------------------------------------------------------------------------
+// Homogeneous medium free flight (shaders/pt/process_volume_hit.glsl:1-40)
+
+struct Medium {
+    float3 sigma_s, sigma_t;
+    float g;
+};
+__device__ __forceinline__ Medium load_medium(const SceneView &s, uint32_t vol)
+{
+    const DevMaterial &m = s.materials[vol];
+    Medium md;
+    float3 sa = f3(m.albedo);
+    md.sigma_s = fmax3(f3(m.mrao), kEps);
+    md.sigma_t = sa + md.sigma_s;
+    md.g = fmaxf(fminf(m.emissive.x, 0.99f), -0.99f);
+    return md;
+}
+// process_volume_transmittance.glsl:1-9
+__device__ __forceinline__ float3 medium_transmittance(const SceneView &s, uint32_t vol, float vtstart, float vtend)
+{
+    const DevMaterial &m = s.materials[vol];
+    float3 ss = fmax3(f3(m.mrao), kEps);
+    float3 st = f3(m.albedo) + ss;
+    float dist = fmaxf(vtend - vtstart, kEps);
+    return f3(expf(-st.x * dist), expf(-st.y * dist), expf(-st.z * dist));
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+
+__global__ void k_init_slots(Queues q, PathState ps, uint32_t slots)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+        q.regen[0][i] = i;
+        ps.flags[i] = 0u;
+        ps.item[i] = 0xFFFFFFFFu;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int c = 0; c < C_COUNT; c++)
+            q.counters[c] = 0u;
+        q.counters[C_REGEN0] = slots;
+    }
+}
+
+__global__ void k_begin(Queues q, int pp)
+{
+    if (threadIdx.x == 0) {
+        q.counters[C_SHADE_L] = 0u;
+        q.counters[C_SHADE_P] = 0u;
+        q.counters[C_SHADE_M] = 0u;
+        q.counters[C_CONN] = 0u;
+        q.counters[C_EXT0 + (1 - pp)] = 0u;
+        q.counters[C_REGEN0 + (1 - pp)] = 0u;
+    }
+}
+
+// Finalizes finished samples, hands out work items, and generates camera
+// rays (raygen.rgen.glsl:24-99, 126-129).
+__global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
+                                               Queues q, BatchResults br, int pp)
+{
+    const RenderParams &p = *pp_;
+    const uint32_t n = q.counters[C_REGEN0 + pp];
+    const uint32_t *queue = q.regen[pp];
+    // per-slot body; returns true when the slot emits a camera ray
+    auto body = [&](const uint32_t slot) -> bool {
+        uint32_t flags = ps.flags[slot];
+        uint32_t sample = ps.sample[slot];
+        uint32_t item = ps.item[slot];
+        float3 cr, ca, cn;
+        if (flags & F_ITEM) {
+            cr = f3(ps.cum_rad[slot]);
+            ca = f3(ps.cum_alb[slot]);
+            cn = f3(ps.cum_nrm[slot]);
+        } else {
+            cr = ca = cn = f3(0.0f);
+        }
+        if (flags & F_DONE) {
+            const float total = (float)p.total_samples;
+            cr += f3(ps.rad[slot]) / total;
+            ca += f3(ps.alb[slot]) / total;
+            cn += f3(ps.nrm[slot]) / total;
+            sample++;
+            atomicAdd(&q.counters[C_PATHS], 1u);
+        }
+        bool fresh = false;
+        if ((flags & F_ITEM) && sample >= p.batch_size) {
+            br.rad[item] = f4(cr, 1.0f);
+            br.alb[item] = f4(ca, 1.0f);
+            br.nrm[item] = f4(cn, 1.0f);
+            flags &= ~F_ITEM;
+            atomicSub(&q.counters[C_ACTIVE], 1u);
+        }
+        if (!(flags & F_ITEM)) {
+            item = atomicAdd(&q.counters[C_NEXT_ITEM], 1u);
+            if (item >= p.total_items) {
+                ps.flags[slot] = 0u;
+                ps.item[slot] = 0xFFFFFFFFu;
+                return false;
+            }
+            atomicAdd(&q.counters[C_ACTIVE], 1u);
+            flags = F_ITEM;
+            sample = 0;
+            fresh = true;
+            cr = ca = cn = f3(0.0f);
+        }
+        const uint32_t npix = p.width * p.height;
+        const uint32_t batch = item / npix;
+        const uint32_t pix = item - batch * npix;
+        const uint32_t px = pix % p.width, py = pix / p.width;
+        uint32_t rng;
+        float3 alb, nrm;
+        if (fresh) {
+            rng = init_rng(px, py, p.width, batch);
+            alb = nrm = f3(0.0f);
+        } else {
+            rng = ps.rng[slot];
+            alb = f3(ps.alb[slot]);
+            nrm = f3(ps.nrm[slot]);
+        }
+        // camera ray, raygen.rgen.glsl:63-91
+        float ox = rand1(rng);
+        float oy = rand1(rng);
+        float uvx = ((float)px + ox) / (float)p.width;
+        float uvy = ((float)py + oy) / (float)p.height;
+        float dx = uvx * 2.0f - 1.0f, dy = uvy * 2.0f - 1.0f;
+        float4 target = mat4_mul(p.proj_inv, dx, dy, 1.0f, 1.0f);
+        float3 dcam = normalize3(f3(target.x, target.y, target.z));
+        float3 ocam = f3(0.0f);
+        if (p.lens_radius > 0.0f) {
+            float lx = rand1(rng);
+            float ly = rand1(rng);
+            float2 disk = concentric_sample_disk(lx, ly);
+            float2 lens = make_float2(p.lens_radius * disk.x, p.lens_radius * disk.y);
+            float ft = p.focal_distance / (-dcam.z);
+            float3 focus = dcam * ft;
+            ocam = f3(lens.x, lens.y, 0.0f);
+            dcam = normalize3(focus - ocam);
+        }
+        float4 wo = mat4_mul(p.view_inv, ocam.x, ocam.y, ocam.z, 1.0f);
+        float4 wd = mat4_mul(p.view_inv, dcam.x, dcam.y, dcam.z, 0.0f);
+        ps.o[slot] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+        ps.d[slot] = make_float4(wd.x, wd.y, wd.z, 0.0f);
+        ps.beta[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        ps.rad[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ps.alb[slot] = f4(alb, 0.0f);
+        ps.nrm[slot] = f4(nrm, 0.0f);
+        ps.cum_rad[slot] = f4(cr, 0.0f);
+        ps.cum_alb[slot] = f4(ca, 0.0f);
+        ps.cum_nrm[slot] = f4(cn, 0.0f);
+        ps.rng[slot] = rng;
+        uint32_t nf = F_ITEM;
+        if (p.cam_volume != -1)
+            nf |= F_INSIDE;
+        ps.flags[slot] = nf;
+        ps.vol[slot] = (uint32_t)p.cam_volume;
+        ps.item[slot] = item;
+        ps.sample[slot] = sample;
+        return true;
+    };
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t slot = 0;
+        bool emit = false;
+        if (i < n) {
+            slot = queue[i];
+            emit = body(slot);
+        }
+        const uint32_t pos = warp_append_all(emit, &q.counters[C_EXT0 + pp]);
+        if (emit)
+            q.ext[pp][pos] = slot;
+    }
+}
+
+// Closest hit for every queued extension ray; hits are binned by material
+// model into the shade queues (material-sorted shading).
+__global__ void __launch_bounds__(256) k_extend(SceneView s, PathState ps, Queues q, int pp)
+{
+    const uint32_t n = q.counters[C_EXT0 + pp];
+    const uint32_t *queue = q.ext[pp];
+    uint32_t err = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t slot = 0;
+        int key = -1; // 0 Lambert, 1 PBR, 2 miss
+        if (i < n) {
+            slot = queue[i];
+            const float3 o = f3(ps.o[slot]);
+            const float3 d = f3(ps.d[slot]);
+            Hit h = trace_closest(s, o, d, kExtTmin, kExtTmax, err);
+            ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+            ps.hit_inst[slot] = h.inst;
+            if (h.inst == kNoHit)
+                key = 2;
+            else
+                key = (uint32_t)s.materials[s.instances[h.inst].material].uv_tiling.z == 2u ? 0 : 1;
+        }
+        // material-sorted shade queues
+        uint32_t pos = warp_append_all(key == 0, &q.counters[C_SHADE_L]);
+        if (key == 0)
+            q.shade_l[pos] = slot;
+        pos = warp_append_all(key == 1, &q.counters[C_SHADE_P]);
+        if (key == 1)
+            q.shade_p[pos] = slot;
+        pos = warp_append_all(key == 2, &q.counters[C_SHADE_M]);
+        if (key == 2)
+            q.shade_m[pos] = slot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(&q.counters[C_SEGMENTS], n);
+    if (err)
+        atomicOr(&q.counters[C_ERR], err);
+}
+
+// Volume free flight on the current segment; returns true when the path
+// scattered in the medium (sampledMedium) and writes the scatter point.
+__device__ __forceinline__ bool medium_event(const SceneView &s, uint32_t vol, float vtstart, float vtend,
+                                             const float3 &origin, const float3 &raydir, float3 &beta, uint32_t &rng,
+                                             float3 &scatter_pos, float &g)
+{
+    Medium md = load_medium(s, vol);
+    g = md.g;
+    float3 dirn = normalize3(raydir);
+    float dist_in = fmaxf(vtend - vtstart, kEps);
+    uint32_t channel = min((uint32_t)(rand1(rng) * 3.0f), 2u);
+    float u = rand1(rng);
+    float hit_dist = -logf(1.0f - u) / comp(md.sigma_t, channel);
+    bool sampled = hit_dist < dist_in;
+    float td = fminf(hit_dist, dist_in);
+    float3 tr = f3(expf(-md.sigma_t.x * td), expf(-md.sigma_t.y * td), expf(-md.sigma_t.z * td));
+    float3 density = sampled ? md.sigma_t * tr : tr;
+    float pdf = 0.0f;
+    pdf += density.x;
+    pdf += density.y;
+    pdf += density.z;
+    pdf *= 0.3333333f;
+    if (pdf == 0.0f)
+        pdf = 1.0f;
+    float3 F = sampled ? (tr * md.sigma_s / pdf) : (tr / pdf);
+    beta *= F;
+    if (sampled)
+        scatter_pos = origin + (vtstart + hit_dist) * dirn;
+    return sampled;
+}
+
+// One shading event per queued path: the body of rayPrimary*.rchit.glsl:45-175
+// (hits) or rayPrimary.rmiss.glsl:40-106 (misses), followed by Russian
+// roulette (russian_roulette.glsl:1-11).
+__global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *__restrict__ pp_, PathState ps, Queues q,
+                                               int pp)
+{
+    const RenderParams &p = *pp_;
+    const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
+    const uint32_t n = nl + np + nm;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t slot = 0;
+        bool want_conn = false, want_done = false, want_ext = false;
+        if (i < n) {
+        if (i < nl)
+            slot = q.shade_l[i];
+        else if (i < nl + np)
+            slot = q.shade_p[i - nl];
+        else
+            slot = q.shade_m[i - nl - np];
+
+        uint32_t flags = ps.flags[slot];
+        uint32_t rng = ps.rng[slot];
+        float3 beta = f3(ps.beta[slot]);
+        float3 rad = f3(ps.rad[slot]);
+        float3 origin = f3(ps.o[slot]);
+        float3 dir = f3(ps.d[slot]);
+        uint32_t vol = ps.vol[slot];
+        const uint32_t d = (flags >> kDepthShift) & kByteMask;
+        uint32_t sdepth = (flags >> kSurfShift) & kByteMask;
+        bool inside = (flags & F_INSIDE) != 0;
+        const float4 hv = ps.hit[slot];
+        const uint32_t inst_id = ps.hit_inst[slot];
+        const bool is_hit = inst_id != kNoHit;
+
+        bool stop = false;
+        bool terminal_no_rr = false; // returns before the RR block
+        bool has_shadow = false, has_nee = false;
+        float3 sh_dir = f3(0.0f), sh_c = f3(0.0f);
+        float sh_tmax = 0.0f;
+        float3 nee_beta = f3(0.0f);
+        float nee_pdf = 0.0f;
+        bool write_alb = false;
+        float3 new_alb = f3(0.0f), new_nrm = f3(0.0f);
+
+        // ---- medium along the segment
+        bool sampled_medium = false;
+        float3 scatter_pos = f3(0.0f);
+        float g = 0.0f;
+        if (inside && vol < s.num_materials) {
+            float vtend = is_hit ? hv.x : fminf(p.zfar_trunc, kExtTmax);
+            sampled_medium = medium_event(s, vol, kExtTmin, vtend, origin, dir, beta, rng, scatter_pos, g);
+        }
+        if (sampled_medium) {
+            // light sample at the scatter point with the HG phase function
+            // (process_volume_hit.glsl:42-79)
+            float3 wo = -normalize3(dir);
+            LightSample ls = sample_light(s, p, scatter_pos, rng);
+            if (!is_black(ls.radiance)) {
+                float ph = henyey_greenstein(dot3(wo, ls.dir), g);
+                float3 F = f3(ph);
+                if (!is_black(F)) {
+                    float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, ph);
+                    has_shadow = true;
+                    sh_dir = ls.dir;
+                    sh_tmax = ls.tmax;
+                    sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
+                }
+            }
+            float3 wi;
+            float u0 = rand1(rng);
+            float u1 = rand1(rng);
+            float spdf = hg_sample(wo, wi, u0, u1, g);
+            origin = scatter_pos;
+            dir = wi;
+            has_nee = true;
+            nee_beta = beta;
+            nee_pdf = spdf;
+        } else if (!is_hit) {
+            // miss: background (rayPrimary.rmiss.glsl:53-103)
+            stop = true;
+            terminal_no_rr = true;
+            const int mode = (int)p.env_type;
+            if (mode == 0) {
+                if (sdepth == 0) {
+                    write_alb = true;
+                    new_alb = p.background;
+                    new_nrm = f3(0.0f);
+                }
+                rad += p.background * beta;
+            } else if (mode == 1) {
+                float3 bg = p.env_intensity * env_lookup(s, dir);
+                if (sdepth == 0) {
+                    write_alb = true;
+                    new_alb = bg;
+                    new_nrm = f3(0.0f);
+                }
+                rad += bg * beta;
+            } else if (mode == 2) {
+                if (sdepth == 0) {
+                    write_alb = true;
+                    new_alb = p.background;
+                    new_nrm = f3(0.0f);
+                    rad += p.background * beta;
+                } else {
+                    rad += env_lookup(s, dir) * beta;
+                }
+            }
+        } else {
+            // surface event
+            const uint32_t prim = __float_as_uint(hv.w);
+            SurfaceHit h = make_surface_hit(s, inst_id, prim, hv.y, hv.z, dir);
+            const DevMaterial &m = s.materials[h.material];
+            const float2 tuv = make_float2(h.uv.x * m.uv_tiling.x, h.uv.y * m.uv_tiling.y);
+            const bool lambert = (uint32_t)m.uv_tiling.z == 2u;
+            bool passthrough = false;
+            if (m.mrao.w > 0.0f) {
+                float alpha = material_alpha(s, m, tuv);
+                float r = rand1(rng);
+                if (alpha < kEps || r > alpha) {
+                    if (h.front_volume != h.back_volume) {
+                        inside = false;
+                        int nv = h.flipped ? h.front_volume : h.back_volume;
+                        if (nv != -1) {
+                            inside = true;
+                            vol = (uint32_t)nv;
+                        }
+                    }
+                    origin = h.wpos;
+                    dir = normalize3(dir);
+                    passthrough = true;
+                }
+            }
+            if (passthrough) {
+                terminal_no_rr = true; // returns without RR and without stop
+            } else {
+                float4 nm = tex2d(s, m.tex2[1], tuv.x, tuv.y);
+                apply_normal_to_frame(h.frame, normal_from_normal_map(f3(nm)));
+                float3 albedo = f3(m.albedo) * f3(tex2d(s, m.tex1[0], tuv.x, tuv.y));
+                float3 emissive = material_emissive(s, m, tuv);
+                PBR pbr;
+                if (!lambert) {
+                    pbr.albedo = albedo;
+                    pbr.metallic = m.mrao.x * tex2d(s, m.tex1[1], tuv.x, tuv.y).x;
+                    pbr.roughness = m.mrao.y * tex2d(s, m.tex1[2], tuv.x, tuv.y).x;
+                    pbr.roughness = fmaxf(pbr.roughness, 0.035f);
+                }
+                if (sdepth == 0) {
+                    write_alb = true;
+                    new_alb = albedo;
+                    new_nrm = h.frame.n * 0.5f + f3(0.5f);
+                }
+                const float em_eps = lambert ? 0.05f : 0.1f;
+                if (sdepth == 0 && !is_black_eps(emissive, em_eps) && !h.flipped) {
+                    rad += emissive * beta;
+                    stop = true;
+                    terminal_no_rr = true;
+                } else {
+                    sdepth = min(sdepth + 1u, 255u);
+                    const float3 wo = world_to_local(h.frame, -dir);
+                    LightSample ls = sample_light(s, p, h.wpos, rng);
+                    if (!is_black(ls.radiance)) {
+                        float3 wi = world_to_local(h.frame, ls.dir);
+                        float3 F;
+                        float bpdf;
+                        if (lambert) {
+                            float ct = fminf(fmaxf(wi.y, 0.0f), 1.0f);
+                            F = albedo * kInvPi * ct;
+                            bpdf = cosine_hemisphere_pdf(ct);
+                        } else {
+                            F = eval_pbr(pbr, wi, wo, normalize3(wo + wi));
+                            bpdf = ls.delta ? 0.0f : pdf_pbr(wi, wo, pbr);
+                        }
+                        if (!is_black(F)) {
+                            float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, bpdf);
+                            has_shadow = true;
+                            sh_dir = ls.dir;
+                            sh_tmax = ls.tmax;
+                            sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
+                        }
+                    }
+                    // BSDF sampling
+                    float spdf;
+                    float3 sdir_local;
+                    bool black_f = false;
+                    float3 Fs;
+                    if (lambert) {
+                        float u0 = rand1(rng);
+                        float u1 = rand1(rng);
+                        sdir_local = cosine_sample_hemisphere(u0, u1, spdf);
+                    } else {
+                        float u0 = rand1(rng);
+                        float u1 = rand1(rng);
+                        float r = rand1(rng);
+                        Fs = sample_pbr(sdir_local, wo, spdf, pbr, u0, u1, r);
+                        black_f = is_black(Fs);
+                    }
+                    float3 sdir = local_to_world(h.frame, sdir_local);
+                    origin = h.wpos;
+                    dir = sdir;
+                    if (lambert) {
+                        beta *= albedo;
+                        has_nee = true;
+                    } else if (black_f) {
+                        stop = true;
+                        terminal_no_rr = true;
+                    } else {
+                        beta *= clamp3(Fs / spdf, 0.0f, 1.0f);
+                        has_nee = true;
+                    }
+                    nee_beta = beta;
+                    nee_pdf = spdf;
+                }
+            }
+        }
+        // Russian roulette (russian_roulette.glsl:1-11) for events that reach it
+        if (!terminal_no_rr) {
+            float rr = rand1(rng);
+            if (d > kRussianRouletteDepth) {
+                float mb = fmaxf(beta.x, fmaxf(beta.y, beta.z));
+                if (rr >= mb)
+                    stop = true;
+                else
+                    beta = beta * (1.0f / mb);
+            }
+        }
+        if (has_nee && p.num_lights == 0u) {
+            // With no lights the reference's emitter pdf is
+            // lightDirectPdf * (1 / 0) = inf (rayNEE.rahit.glsl:124), so the
+            // MIS weight and the contribution are zero: skip the ray.
+            has_nee = false;
+        }
+
+        const bool last = (d + 1u >= p.depth);
+        const bool done = stop || last;
+        uint32_t nf = F_ITEM | (inside ? F_INSIDE : 0u) | ((min(d + 1u, 255u)) << kDepthShift) | (sdepth << kSurfShift);
+        if (done)
+            nf |= F_DONE;
+        if (has_shadow)
+            nf |= F_SHADOW;
+        if (has_nee)
+            nf |= F_NEE;
+        ps.flags[slot] = nf;
+        ps.rng[slot] = rng;
+        ps.beta[slot] = f4(beta, 0.0f);
+        ps.rad[slot] = f4(rad, 0.0f);
+        ps.o[slot] = f4(origin, 0.0f);
+        ps.d[slot] = f4(dir, 0.0f);
+        ps.vol[slot] = vol;
+        if (write_alb) {
+            ps.alb[slot] = f4(new_alb, 0.0f);
+            ps.nrm[slot] = f4(new_nrm, 0.0f);
+        }
+        if (has_shadow) {
+            ps.sh_dir[slot] = f4(sh_dir, sh_tmax);
+            ps.sh_c[slot] = f4(sh_c, 0.0f);
+        }
+        if (has_nee)
+            ps.nee_b[slot] = f4(nee_beta, nee_pdf);
+        want_conn = has_shadow || has_nee;
+        want_done = done;
+        want_ext = !done;
+        }
+        uint32_t pos = warp_append_all(want_conn, &q.counters[C_CONN]);
+        if (want_conn)
+            q.conn[pos] = slot;
+        pos = warp_append_all(want_done, &q.counters[C_REGEN0 + (1 - pp)]);
+        if (want_done)
+            q.regen[1 - pp][pos] = slot;
+        pos = warp_append_all(want_ext, &q.counters[C_EXT0 + (1 - pp)]);
+        if (want_ext)
+            q.ext[1 - pp][pos] = slot;
+    }
+}
+
+// Shadow ray with transparent surfaces and media (lightSampling.glsl:108-144,
+// raySecondary.rahit.glsl:31-72, raySecondary.rchit.glsl:32-78,
+// raySecondary.rmiss.glsl:17-44). Candidates are processed nearest first.
+__device__ float3 shadow_transmittance(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir,
+                                       float tmax_light, bool inside, uint32_t vol, uint32_t &err)
+{
+    const float tmin = kConnTmin;
+    float3 T = f3(1.0f);
+    bool shadowed = false;
+    bool stop = false;
+    float distT = tmax_light - tmin;
+    for (uint32_t seg = 0; seg < p.depth; seg++) {
+        float vtmin = tmin;
+        Hit after = no_hit();
+        bool accepted = false;
+        Hit acc;
+        int guard = 0;
+        for (;;) {
+            Hit h = trace_after(s, o, dir, tmin, distT, after, err);
+            if (h.inst == kNoHit)
+                break;
+            if (++guard > kCandidateCap) {
+                err |= kErrLoopCap;
+                stop = shadowed = true;
+                accepted = true;
+                acc = h;
+                break;
+            }
+            const DevInstance &inst = s.instances[h.inst];
+            const DevMaterial &m = s.materials[inst.material];
+            if (!(m.mrao.w >= 0.99f)) {
+                stop = shadowed = true;
+                accepted = true;
+                acc = h;
+                break;
+            }
+            // alpha needs the hit's uv
+            ShadeVertex a, b, c;
+            fetch_triangle(s, inst, h.prim, a, b, c);
+            float bx = 1.0f - h.u - h.v;
+            float2 uv = make_float2(a.pos_u.w * bx + b.pos_u.w * h.u + c.pos_u.w * h.v,
+                                    a.nrm_v.w * bx + b.nrm_v.w * h.u + c.nrm_v.w * h.v);
+            float alpha = material_alpha(s, m, make_float2(uv.x * m.uv_tiling.x, uv.y * m.uv_tiling.y));
+            T *= f3(1.0f - alpha);
+            if (inst.front_volume != inst.back_volume) {
+                accepted = true;
+                acc = h;
+                break;
+            }
+            if (max3f(T) > kEps) {
+                shadowed = false;
+                after = h;
+                continue;
+            }
+            stop = shadowed = true;
+            accepted = true;
+            acc = h;
+            break;
+        }
+        if (!accepted) {
+            // miss shader
+            stop = true;
+            shadowed = false;
+            if (inside && vol < s.num_materials) {
+                float vtend = fminf(p.zfar_trunc, distT);
+                T *= medium_transmittance(s, vol, vtmin, vtend);
+                shadowed = !(max3f(T) > kEps);
+            }
+        } else if (!stop) {
+            // closest hit on a volume boundary
+            SurfaceHit sh = make_surface_hit(s, acc.inst, acc.prim, acc.u, acc.v, dir);
+            bool ended = false;
+            if (inside && vol < s.num_materials) {
+                T *= medium_transmittance(s, vol, vtmin, acc.t);
+                if (max3f(T) < kEps) {
+                    stop = shadowed = true;
+                    ended = true;
+                }
+            }
+            if (!ended) {
+                vtmin = acc.t;
+                inside = false;
+                int nv = sh.flipped ? sh.front_volume : sh.back_volume;
+                if (nv != -1) {
+                    inside = true;
+                    vol = (uint32_t)nv;
+                }
+                o = sh.wpos;
+            }
+        }
+        distT -= vtmin;
+        if (stop)
+            break;
+    }
+    if (shadowed)
+        T = f3(0.0f);
+    return T;
+}
+
+// BSDF-direction emitter ray (next_event_estimation.glsl:1-33,
+// rayNEE.rahit.glsl:32-132, rayNEE.rchit.glsl:33-82, rayNEE.rmiss.glsl:12-19).
+// Returns the emitter radiance times throughput and its light pdf.
+__device__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir, bool inside,
+                            uint32_t vol, float3 &out_em_T, float3 &out_T, float3 &out_em, float &out_pdf, uint32_t &err)
+{
+    const float tmin = kConnTmin;
+    const float tmax = p.zfar;
+    float3 T = f3(1.0f);
+    float3 em = f3(0.0f);
+    float pdf = 0.0f;
+    bool stop = false;
+    for (uint32_t seg = 0; seg < p.depth; seg++) {
+        float vtmin = tmin;
+        Hit after = no_hit();
+        bool accepted = false;
+        Hit acc;
+        int guard = 0;
+        for (;;) {
+            Hit h = trace_after(s, o, dir, tmin, tmax, after, err);
+            if (h.inst == kNoHit)
+                break;
+            if (++guard > kCandidateCap) {
+                err |= kErrLoopCap;
+                stop = true;
+                T = f3(0.0f);
+                em = f3(0.0f);
+                accepted = true;
+                acc = h;
+                break;
+            }
+            const DevInstance &inst = s.instances[h.inst];
+            const DevMaterial &m = s.materials[inst.material];
+            ShadeVertex a, b, c;
+            fetch_triangle(s, inst, h.prim, a, b, c);
+            float bx = 1.0f - h.u - h.v;
+            float2 uv = make_float2(a.pos_u.w * bx + b.pos_u.w * h.u + c.pos_u.w * h.v,
+                                    a.nrm_v.w * bx + b.nrm_v.w * h.u + c.nrm_v.w * h.v);
+            float2 tuv = make_float2(uv.x * m.uv_tiling.x, uv.y * m.uv_tiling.y);
+            float3 e = material_emissive(s, m, tuv);
+            const bool transparent = m.mrao.w >= 0.99f;
+            if (is_black_eps(e, 0.05f)) {
+                if (!transparent) {
+                    stop = true;
+                    T = f3(0.0f);
+                    em = f3(0.0f);
+                    accepted = true;
+                    acc = h;
+                    break;
+                }
+                float alpha = material_alpha(s, m, tuv);
+                T *= f3(1.0f - alpha);
+                if (inst.front_volume != inst.back_volume) {
+                    accepted = true;
+                    acc = h;
+                    break;
+                }
+                after = h;
+                continue;
+            }
+            // emissive surface
+            stop = true;
+            accepted = true;
+            acc = h;
+            if (inside && vol < s.num_materials) {
+                T *= medium_transmittance(s, vol, vtmin, h.t);
+                if (max3f(T) < kEps) {
+                    T = f3(0.0f);
+                    em = f3(0.0f);
+                    break;
+                }
+            }
+            Affine34 w2o = rows_of(inst.w2o), o2w = rows_of(inst.o2w);
+            float3 ln = f3(a.nrm_v) * bx + f3(b.nrm_v) * h.u + f3(c.nrm_v) * h.v;
+            float3 wn = normalize3(xform_normal_transposed(w2o, ln));
+            bool flipped = dot3(wn, dir) > 0.0f;
+            if (flipped) {
+                em = f3(0.0f);
+                T = f3(0.0f);
+                break;
+            }
+            em = e;
+            float3 lp = f3(a.pos_u) * bx + f3(b.pos_u) * h.u + f3(c.pos_u) * h.v;
+            float3 wp = xform_point(o2w, lp);
+            float3 p0 = xform_point(o2w, f3(a.pos_u)), p1 = xform_point(o2w, f3(b.pos_u)), p2 = xform_point(o2w, f3(c.pos_u));
+            float area = 0.5f * length3(cross3(p1 - p0, p2 - p0));
+            float point_pdf = (1.0f / (float)inst.num_triangles) * (1.0f / area);
+            float dp = dot3(-dir, wn);
+            if (dp > 0.0f) {
+                // distance from the object-space ray origin, as rayNEE.rahit.glsl:122
+                float3 obj_o = xform_point(w2o, o);
+                float dist = length3(obj_o - wp);
+                float light_pdf = point_pdf * (dist * dist) / dp;
+                pdf = light_pdf * (1.0f / (float)p.num_lights);
+            } else {
+                pdf = 0.0f;
+                em = f3(0.0f);
+            }
+            break;
+        }
+        if (!accepted) {
+            stop = true;
+            em = f3(0.0f);
+            pdf = 0.0f;
+        } else if (!stop) {
+            SurfaceHit sh = make_surface_hit(s, acc.inst, acc.prim, acc.u, acc.v, dir);
+            bool ended = false;
+            if (inside && vol < s.num_materials) {
+                T *= medium_transmittance(s, vol, vtmin, acc.t);
+                if (max3f(T) < kEps) {
+                    stop = true;
+                    T = f3(0.0f);
+                    em = f3(0.0f);
+                    ended = true;
+                }
+            }
+            if (!ended) {
+                vtmin = acc.t;
+                inside = false;
+                int nv = sh.flipped ? sh.front_volume : sh.back_volume;
+                if (nv != -1) {
+                    inside = true;
+                    vol = (uint32_t)nv;
+                }
+                o = sh.wpos;
+            }
+        }
+        if (stop)
+            break;
+    }
+    out_T = T;
+    out_em = em;
+    out_pdf = pdf;
+    out_em_T = T * em;
+}
+
+__global__ void __launch_bounds__(256) k_connect(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
+                                                 Queues q)
+{
+    const RenderParams &p = *pp_;
+    const uint32_t n = q.counters[C_CONN];
+    uint32_t err = 0;
+    uint32_t nsh = 0, nnee = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = q.conn[i];
+        const uint32_t flags = ps.flags[slot];
+        const bool inside = (flags & F_INSIDE) != 0;
+        const uint32_t vol = ps.vol[slot];
+        const float3 o = f3(ps.o[slot]);
+        float3 rad = f3(ps.rad[slot]);
+        if (flags & F_SHADOW) {
+            float4 sd = ps.sh_dir[slot];
+            float3 c = f3(ps.sh_c[slot]);
+            float3 T = shadow_transmittance(s, p, o, f3(sd), sd.w, inside, vol, err);
+            if (!is_black(T))
+                rad += c * T;
+            nsh++;
+        }
+        if (flags & F_NEE) {
+            float4 nb = ps.nee_b[slot];
+            float3 emT, T, em;
+            float lpdf;
+            emitter_ray(s, p, o, f3(ps.d[slot]), inside, vol, emT, T, em, lpdf, err);
+            if (!is_black(em)) {
+                float w = power_heuristic(nb.w, lpdf);
+                rad += w * T * em * f3(nb);
+            }
+            nnee++;
+        }
+        ps.rad[slot] = f4(rad, 0.0f);
+        ps.flags[slot] = flags & ~(F_SHADOW | F_NEE);
+    }
+    if (nsh)
+        atomicAdd(&q.counters[C_SHADOW], nsh);
+    if (nnee)
+        atomicAdd(&q.counters[C_NEE], nnee);
+    if (err)
+        atomicOr(&q.counters[C_ERR], err);
+}
+
+// Final image: per pixel, add the per-batch sums in batch order starting from
+// zero, exactly the sequence of read-modify-writes of raygen.rgen.glsl:134-144.
+__global__ void k_reduce(RenderParams p, BatchResults br, float4 *rad, float4 *alb, float4 *nrm, float4 *m2)
+{
+    const uint32_t npix = p.width * p.height;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
+        float3 r = f3(0.0f), a = f3(0.0f), nn = f3(0.0f), q2 = f3(0.0f);
+        for (uint32_t b = 0; b < p.batches; b++) {
+            const size_t it = (size_t)b * npix + pix;
+            float3 rb = f3(br.rad[it]);
+            r = r + rb;
+            a = a + f3(br.alb[it]);
+            nn = nn + f3(br.nrm[it]);
+            q2 = q2 + rb * rb;
+        }
+        if (rad)
+            rad[pix] = f4(r, 1.0f);
+        if (alb)
+            alb[pix] = f4(a, 1.0f);
+        if (nrm)
+            nrm[pix] = f4(nn, 1.0f);
+        if (m2)
+            m2[pix] = f4(q2, 1.0f);
+    }
+}
+
+__global__ void k_trace_closest(SceneView s, const float4 *rays, uint32_t n, float4 *tuv, uint32_t *ids, uint32_t *err_out)
+{
+    uint32_t err = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = rays[2 * i], b = rays[2 * i + 1];
+        Hit h = trace_closest(s, f3(a), f3(b), a.w, b.w, err);
+        tuv[i] = make_float4(h.t, h.u, h.v, 0.0f);
+        ids[2 * i] = h.inst;
+        ids[2 * i + 1] = h.prim;
+    }
+    if (err)
+        atomicOr(err_out, err);
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+
+void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cudaStream_t stream)
+{
+    int grid = (int)std::min<uint32_t>((slots + 255) / 256, 65535u);
+    k_init_slots<<<grid, 256, 0, stream>>>(q, ps, slots);
+}
+
+void launch_iteration(const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
+                      const BatchResults &br, int pp, const LaunchShape &shape, cudaStream_t stream)
+{
+    k_begin<<<1, 32, 0, stream>>>(q, pp);
+    k_regen<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, br, pp);
+    k_extend<<<shape.grid, shape.block, 0, stream>>>(s, ps, q, pp);
+    k_shade<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, pp);
+    k_connect<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+}
+
+void launch_reduce(const RenderParams &hp, const BatchResults &br, float4 *radiance, float4 *albedo, float4 *normal,
+                   float4 *radiance_m2, cudaStream_t stream)
+{
+    uint32_t npix = hp.width * hp.height;
+    int grid = (int)std::min<uint32_t>((npix + 255) / 256, 65535u);
+    k_reduce<<<grid, 256, 0, stream>>>(hp, br, radiance, albedo, normal, radiance_m2);
+}
+
+void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, float4 *tuv, uint32_t *ids, uint32_t *err,
+                          cudaStream_t stream)
+{
+    int grid = (int)std::min<uint32_t>((n + 255) / 256, 65535u);
+    if (grid < 1)
+        grid = 1;
+    k_trace_closest<<<grid, 256, 0, stream>>>(s, rays, n, tuv, ids, err);
+}
+
+}  // namespace vvpt

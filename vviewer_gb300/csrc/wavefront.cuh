@@ -1,0 +1,108 @@
+// Wavefront path-tracer state and launch interface.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "scene_gpu.h"
+
+namespace vvpt {
+
+// Per-render constants (SceneData + PathTracingData of the reference,
+// src/lib/vengine/core/Scene.hpp:27-35 and
+// src/lib/vengine/vulkan/renderers/VulkanRendererPathTracing.hpp:57-61).
+struct RenderParams {
+    float4 view_inv[4]; // columns
+    float4 proj_inv[4]; // columns
+    float3 background;
+    float env_type;     // background.a: 0 solid, 1 HDRI, 2 solid + HDRI lighting
+    float lens_radius;
+    float focal_distance;
+    float env_intensity;
+    float zfar;          // sceneData.volumes.b
+    float zfar_trunc;    // float(uint(zfar)), rayPrimary.rmiss.glsl:49
+    int32_t cam_volume;  // sceneData.volumes.r (-1: camera not in a medium)
+    uint32_t width, height;
+    uint32_t batch_size, batches, depth, total_samples;
+    uint32_t num_lights;  // pathTracingData.lights.r
+    uint32_t total_items; // width * height * batches
+    uint32_t want_m2;
+};
+
+// Structure-of-arrays path state, one entry per slot. A slot runs one
+// (pixel, batch) work item: its batch_size samples in order, because the
+// RTGEMS state carries from one sample to the next (raygen.rgen.glsl:36-55).
+struct PathState {
+    float4 *o;       // ray origin (xyz)
+    float4 *d;       // ray direction (xyz)
+    float4 *beta;    // throughput (xyz)
+    float4 *rad;     // sample radiance (xyz)
+    float4 *alb;     // first-hit albedo carried across samples (payload semantics)
+    float4 *nrm;     // first-hit normal carried across samples
+    float4 *cum_rad; // per-batch sums (cumRadiance/cumAlbedo/cumNormal)
+    float4 *cum_alb;
+    float4 *cum_nrm;
+    float4 *hit;     // t, u, v, prim bits
+    uint32_t *hit_inst;
+    float4 *sh_dir;  // shadow direction (xyz), tmax (w)
+    float4 *sh_c;    // unoccluded light contribution (xyz)
+    float4 *nee_b;   // beta for the emitter-ray contribution (xyz), BSDF pdf (w)
+    uint32_t *rng;
+    uint32_t *flags;
+    uint32_t *vol;
+    uint32_t *item;
+    uint32_t *sample;
+};
+
+enum CounterIndex {
+    C_EXT0 = 0,
+    C_EXT1 = 1,
+    C_SHADE_L = 2,
+    C_SHADE_P = 3,
+    C_SHADE_M = 4,
+    C_CONN = 5,
+    C_REGEN0 = 6,
+    C_REGEN1 = 7,
+    C_NEXT_ITEM = 8,
+    C_ACTIVE = 9,
+    C_ERR = 10,
+    C_SEGMENTS = 11,
+    C_SHADOW = 12,
+    C_NEE = 13,
+    C_PATHS = 14,
+    C_COUNT = 16
+};
+
+struct Queues {
+    uint32_t *ext[2];
+    uint32_t *shade_l, *shade_p, *shade_m;
+    uint32_t *conn;
+    uint32_t *regen[2];
+    uint32_t *counters; // CounterIndex
+};
+
+// Per-(pixel, batch) sums written when a work item finishes, reduced in batch
+// order at the end so the image equals the reference's per-batch
+// read-modify-write sequence (raygen.rgen.glsl:134-144).
+struct BatchResults {
+    float4 *rad;
+    float4 *alb;
+    float4 *nrm;
+};
+
+struct LaunchShape {
+    int grid;
+    int block;
+};
+
+// Kernel launchers (wavefront.cu). Each reads its work count from `counters`,
+// so a sequence of them can be captured in a CUDA graph.
+void launch_iteration(const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
+                      const BatchResults &br, int pingpong, const LaunchShape &shape, cudaStream_t stream);
+void launch_reduce(const RenderParams &hparams, const BatchResults &br, float4 *radiance, float4 *albedo,
+                   float4 *normal, float4 *radiance_m2, cudaStream_t stream);
+void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cudaStream_t stream);
+void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, float4 *hits_tuv, uint32_t *hits_ids,
+                          uint32_t *err, cudaStream_t stream);
+constexpr int kKernelsPerIteration = 5;
+
+}  // namespace vvpt

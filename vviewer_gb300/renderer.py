@@ -1,0 +1,248 @@
+"""RendererPathTracing adapter over the C ABI.
+
+Mirrors src/lib/vengine/core/Renderer.hpp:11-39 (RenderInfo, render,
+renderProgress, isRayTracingEnabled) and the output step of
+src/lib/vengine/vulkan/renderers/VulkanRendererPathTracing.cpp:958-1027 and
+src/lib/vengine/core/ImageUtils.cpp:39-76 (exposure for PNG, RGBE or sRGB PNG).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import struct
+import warnings
+import zlib
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import _native as N
+from .assets import srgb_encode, write_hdr
+from .scene import Engine, FlatScene
+
+
+@dataclass
+class RenderInfo:
+    samples: int = 256
+    depth: int = 9
+    batch_size: int = 4
+    filename: str = "test"
+    file_type: str = "hdr"  # "hdr" or "png"
+    exposure: float = 0.0
+    width: int = 1080
+    height: int = 1080
+    denoise: bool = False
+    write_all_files: bool = False
+    write_files: bool = True
+
+
+@dataclass
+class RenderResult:
+    radiance: np.ndarray  # H x W x 4 float32
+    albedo: np.ndarray
+    normal: np.ndarray
+    radiance_m2: np.ndarray | None
+    stats: N.RenderStats
+    batches: int
+
+
+class Context:
+    """One CUDA device context of the library (vvpt_create / vvpt_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.load()
+        h = C.c_void_p()
+        st = self.lib.vvpt_create(device, C.byref(h))
+        if st != N.VVPT_OK:
+            raise N.VvptError(st, "vvpt_create failed (no usable CUDA device)")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.vvpt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st: int) -> None:
+        N.check(st, self.handle)
+
+    def upload(self, flat: FlatScene) -> "GpuScene":
+        d = flat.desc()
+        h = C.c_void_p()
+        self.check(self.lib.vvpt_scene_upload(self.handle, C.byref(d), C.byref(h)))
+        return GpuScene(self, h, flat)
+
+    def set_tuning(self, slots=0, blocks_per_sm=0, threads_per_block=0, iterations_per_graph=0) -> None:
+        t = N.Tuning(slots, blocks_per_sm, threads_per_block, iterations_per_graph)
+        self.check(self.lib.vvpt_set_tuning(self.handle, C.byref(t)))
+
+    def stats(self) -> N.RenderStats:
+        s = N.RenderStats()
+        self.check(self.lib.vvpt_last_render_stats(self.handle, C.byref(s)))
+        return s
+
+
+class GpuScene:
+    """A scene resident on the device (vvpt_scene_upload)."""
+
+    def __init__(self, ctx: Context, handle, flat: FlatScene):
+        self.ctx = ctx
+        self.handle = handle
+        self.flat = flat
+
+    def release(self) -> None:
+        if self.handle:
+            self.ctx.lib.vvpt_scene_release(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def device_bytes(self) -> int:
+        b = C.c_uint64()
+        self.ctx.check(self.ctx.lib.vvpt_scene_device_bytes(self.ctx.handle, self.handle, C.byref(b)))
+        return int(b.value)
+
+    def render(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
+               outputs: dict | None = None) -> RenderResult | None:
+        """Renders into host arrays, or into device pointers when `outputs`
+        maps radiance/albedo/normal/radiance_m2 to device addresses."""
+        ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height,
+                          N.RENDER_WANT_BATCH_M2 if want_m2 else 0)
+        if outputs is not None:
+            o = N.Outputs(outputs.get("radiance"), outputs.get("albedo"), outputs.get("normal"),
+                          outputs.get("radiance_m2"), 1)
+            self.ctx.check(self.ctx.lib.vvpt_render(self.ctx.handle, self.handle, C.byref(scene_data), C.byref(ri),
+                                                    C.byref(o)))
+            return None
+        H, W = info.height, info.width
+        rad = np.zeros((H, W, 4), dtype=np.float32)
+        alb = np.zeros((H, W, 4), dtype=np.float32)
+        nrm = np.zeros((H, W, 4), dtype=np.float32)
+        m2 = np.zeros((H, W, 4), dtype=np.float32) if want_m2 else None
+        o = N.Outputs(rad.ctypes.data, alb.ctypes.data, nrm.ctypes.data, m2.ctypes.data if want_m2 else None, 0)
+        self.ctx.check(self.ctx.lib.vvpt_render(self.ctx.handle, self.handle, C.byref(scene_data), C.byref(ri),
+                                                C.byref(o)))
+        return RenderResult(rad, alb, nrm, m2, self.ctx.stats(), info.samples // info.batch_size)
+
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        """rays: N x 8 float32 (origin, tmin, direction, tmax) -> structured hits."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        hits = np.zeros(n, dtype=HIT_DTYPE)
+        self.ctx.check(self.ctx.lib.vvpt_trace_closest(self.ctx.handle, self.handle, rays.ctypes.data, n,
+                                                       hits.ctypes.data, 0))
+        return hits
+
+
+HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), ("instance", np.uint32),
+                      ("primitive", np.uint32)])
+
+
+def write_png(path: str | Path, rgba8: np.ndarray) -> None:
+    """Minimal PNG writer (8-bit RGBA, no filtering)."""
+    h, w, c = rgba8.shape
+    raw = b"".join(b"\x00" + rgba8[y].tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    color_type = 6 if c == 4 else 2
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, color_type, 0, 0, 0))
+    png += chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b"")
+    Path(path).write_bytes(png)
+
+
+def write_to_disk(data: np.ndarray, filename: str, file_type: str) -> None:
+    """ImageUtils.cpp:51-76: RGBE HDR of the first three channels, or sRGB 8-bit PNG."""
+    if file_type == "png":
+        rgba = np.clip(data, 0.0, 1.0)
+        rgb8 = (255.0 * srgb_encode(rgba[..., :3])).astype(np.uint8)
+        a8 = (255.0 * srgb_encode(rgba[..., 3:4])).astype(np.uint8)
+        write_png(filename + ".png", np.concatenate([rgb8, a8], axis=-1))
+    else:
+        write_hdr(filename + ".hdr", data)
+
+
+def apply_exposure(data: np.ndarray, exposure: float) -> np.ndarray:
+    out = data.copy()
+    out[..., :3] = out[..., :3] * np.float32(2.0 ** exposure)
+    return out
+
+
+class RendererPathTracing:
+    """engine.renderer().rendererPathTracing() of the reference."""
+
+    def __init__(self, engine: Engine, device: int = 0, context: Context | None = None):
+        self.engine = engine
+        self._ctx = context
+        self._device = device
+        self._info = RenderInfo()
+        self._progress = 0.0
+        self._in_progress = False
+        self.last_result: RenderResult | None = None
+
+    def render_info(self) -> RenderInfo:
+        return self._info
+
+    @property
+    def context(self) -> Context:
+        if self._ctx is None:
+            self._ctx = Context(self._device)
+        return self._ctx
+
+    def is_ray_tracing_enabled(self) -> bool:
+        try:
+            return self.context.handle is not None
+        except N.VvptError:
+            return False
+
+    def render_progress(self) -> float:
+        if self._ctx is None:
+            return self._progress
+        p = C.c_float()
+        self._ctx.lib.vvpt_progress(self._ctx.handle, C.byref(p))
+        return float(p.value)
+
+    def render(self) -> RenderResult | None:
+        if self._in_progress:
+            return None
+        scene = self.engine.scene
+        if not scene.objects_flat():
+            warnings.warn("Trying to render an empty scene")
+            return None
+        self._in_progress = True
+        try:
+            info = self._info
+            flat = scene.build()
+            gpu = self.context.upload(flat)
+            try:
+                res = gpu.render(scene.scene_data(info.width, info.height), info)
+            finally:
+                gpu.release()
+            self.last_result = res
+            if info.write_files:
+                self.store_to_disk(res)
+            return res
+        finally:
+            self._in_progress = False
+
+    def store_to_disk(self, res: RenderResult) -> None:
+        info = self._info
+        if info.write_all_files:
+            write_to_disk(res.albedo, info.filename + "_albedo", "hdr")
+            write_to_disk(res.normal, info.filename + "_normal", "hdr")
+        radiance = res.radiance
+        if info.denoise:
+            raise NotImplementedError("denoise=True needs the learned denoiser, which this build does not ship yet")
+        if info.file_type == "png" and info.exposure != 0.0:
+            radiance = apply_exposure(radiance, info.exposure)
+        write_to_disk(radiance, info.filename, info.file_type)
