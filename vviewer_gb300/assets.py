@@ -119,73 +119,81 @@ def load_obj(path: str | Path) -> Mesh:
 
 
 def calc_tangent_space(pos: np.ndarray, uv: np.ndarray, nrm: np.ndarray, max_angle_deg: float = 45.0):
-    """Per-corner tangents/bitangents (corners grouped in threes)."""
+    """Per-corner tangents/bitangents (corners grouped in threes), restating
+    assimp 5.2.5's CalcTangentSpace step in float32:
+
+    1. per face, with v = p1 - p0, w = p2 - p0 and UV deltas (sx, sy), (tx, ty):
+       tangent = (w*sy - v*ty) * dirCorrection, bitangent = (v*tx - w*sx) * dirCorrection,
+       dirCorrection = -1 when tx*sy - ty*sx < 0; degenerate UVs use (0,1),(1,0);
+    2. per corner, both projected onto the plane of the corner's normal and
+       normalised;
+    3. smoothing, visiting corners in index order: a corner not yet assigned
+       gathers every unassigned corner within the position epsilon
+       (1e-4 x bounding-box diagonal) whose normal has a dot product >= 0.9999
+       and whose tangent and bitangent are within the smoothing angle of its
+       own. The seed corner is part of the neighbour search as well, so it
+       enters the sum twice. The normalised sums replace all gathered values.
+    """
+    from scipy.spatial import cKDTree
+
     n = pos.shape[0]
-    p = pos.astype(np.float64).reshape(-1, 3, 3)
-    t = uv.astype(np.float64).reshape(-1, 3, 2)
+    p = pos.astype(f32).reshape(-1, 3, 3)
+    t = uv.astype(f32).reshape(-1, 3, 2)
     v = p[:, 1] - p[:, 0]
     w = p[:, 2] - p[:, 0]
     sx = t[:, 1, 0] - t[:, 0, 0]
     sy = t[:, 1, 1] - t[:, 0, 1]
     tx = t[:, 2, 0] - t[:, 0, 0]
     ty = t[:, 2, 1] - t[:, 0, 1]
-    dir_corr = np.where(tx * sy - ty * sx < 0.0, -1.0, 1.0)
+    dir_corr = np.where(tx * sy - ty * sx < 0, f32(-1), f32(1)).astype(f32)
     degen = sx * ty == sy * tx
-    sx = np.where(degen, 0.0, sx)
-    sy = np.where(degen, 1.0, sy)
-    tx = np.where(degen, 1.0, tx)
-    ty = np.where(degen, 0.0, ty)
-    tan_f = (w * sy[:, None] - v * ty[:, None]) * dir_corr[:, None]
-    bit_f = (w * sx[:, None] - v * tx[:, None]) * dir_corr[:, None]
-    tan_c = np.repeat(tan_f, 3, axis=0)
-    bit_c = np.repeat(bit_f, 3, axis=0)
-    nn = nrm.astype(np.float64)
-    lt = tan_c - nn * (tan_c * nn).sum(1, keepdims=True)
-    lb = bit_c - nn * (bit_c * nn).sum(1, keepdims=True)
+    sx = np.where(degen, 0, sx).astype(f32)
+    sy = np.where(degen, 1, sy).astype(f32)
+    tx = np.where(degen, 1, tx).astype(f32)
+    ty = np.where(degen, 0, ty).astype(f32)
+    tan = np.repeat(((w * sy[:, None] - v * ty[:, None]) * dir_corr[:, None]).astype(f32), 3, axis=0)
+    bit = np.repeat(((-w * sx[:, None] + v * tx[:, None]) * dir_corr[:, None]).astype(f32), 3, axis=0)
+    nn = nrm.astype(f32)
+    lt = (tan - nn * (tan * nn).sum(1, keepdims=True)).astype(f32)
+    lb = (bit - nn * (bit * nn).sum(1, keepdims=True)).astype(f32)
 
-    def _norm(a):
+    def _normalize_safe(a):
         ln = np.sqrt((a * a).sum(1, keepdims=True))
-        ok = (ln[:, 0] > 0) & np.isfinite(ln[:, 0])
-        out = np.where(ok[:, None], a / np.where(ln > 0, ln, 1.0), np.nan)
-        return out, ok
+        return np.where(ln > 0, a / np.where(ln > 0, ln, 1), a).astype(f32)
 
-    lt, okt = _norm(lt)
-    lb, okb = _norm(lb)
-    # invalid tangents: any vector orthogonal to the normal
-    bad = ~(okt & okb)
-    if bad.any():
-        for i in np.nonzero(bad)[0]:
-            a = np.array([1.0, 0.0, 0.0]) if abs(nn[i, 0]) < 0.9 else np.array([0.0, 1.0, 0.0])
-            tt = np.cross(nn[i], a)
-            tt /= np.linalg.norm(tt)
-            lt[i] = tt
-            lb[i] = np.cross(nn[i], tt)
-    # smoothing over corners sharing a position
-    cos_max = math.cos(math.radians(max_angle_deg))
-    keys = np.round(pos.astype(np.float64) * 1e5).astype(np.int64)
-    order = np.lexsort((keys[:, 2], keys[:, 1], keys[:, 0]))
-    ks = keys[order]
-    brk = np.nonzero(np.any(ks[1:] != ks[:-1], axis=1))[0] + 1
-    groups = np.split(order, brk)
-    out_t = lt.copy()
-    out_b = lb.copy()
+    lt = _normalize_safe(lt)
+    lb = _normalize_safe(lb)
+    # non-finite frames: rebuild from the normal
+    bad = ~(np.isfinite(lt).all(1) & np.isfinite(lb).all(1)) | ~(np.abs(lt).sum(1) > 0)
+    for i in np.nonzero(bad)[0]:
+        a = np.array([1.0, 0.0, 0.0]) if abs(nn[i, 0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        tt = np.cross(nn[i], a)
+        lt[i] = tt / np.linalg.norm(tt)
+        lb[i] = np.cross(nn[i], lt[i])
+
+    eps = float(np.linalg.norm(pos.max(0) - pos.min(0))) * 1e-4
+    neighbours = cKDTree(pos.astype(np.float64)).query_ball_point(pos.astype(np.float64), r=max(eps, 1e-12))
+    limit = f32(math.cos(math.radians(max_angle_deg)))
+    T = lt.copy()
+    B = lb.copy()
     done = np.zeros(n, dtype=bool)
-    for g in groups:
-        if len(g) == 1:
+    for a in range(n):
+        if done[a]:
             continue
-        for i in g:
-            if done[i]:
-                continue
-            close = [j for j in g if (nn[i] @ nn[j]) >= cos_max and (lt[i] @ lt[j]) >= cos_max]
-            st = lt[close].sum(0)
-            sb = lb[close].sum(0)
-            st /= max(np.linalg.norm(st), 1e-30)
-            sb /= max(np.linalg.norm(sb), 1e-30)
-            for j in close:
-                out_t[j] = st
-                out_b[j] = sb
-                done[j] = True
-    return out_t.astype(f32), out_b.astype(f32)
+        found = np.sort(np.asarray(neighbours[a], dtype=np.int64))
+        found = found[~done[found]]
+        if found.size <= 1:
+            continue  # only itself: the normalised value stays
+        keep = ((nn[found] @ nn[a]) >= f32(0.9999)) & ((T[found] @ lt[a]) >= limit) & ((B[found] @ lb[a]) >= limit)
+        group = np.concatenate([[a], found[keep]])
+        done[found[keep]] = True
+        st = T[group].sum(0, dtype=f32)
+        sb = B[group].sum(0, dtype=f32)
+        st = (st / np.sqrt(st @ st)).astype(f32)
+        sb = (sb / np.sqrt(sb @ sb)).astype(f32)
+        T[group] = st
+        B[group] = sb
+    return T.astype(f32), B.astype(f32)
 
 
 # ---------------------------------------------------------------- RGBE (Radiance .hdr)
