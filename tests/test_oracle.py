@@ -5,8 +5,9 @@ Pin: the reference's golden images (src/bin/unittests/RenderTests.cpp, RGBE
 stream, scene conventions and assimp tangent frames, so it reproduces the
 goldens far below Monte Carlo noise: each scene must meet the reference's own
 MSE tolerance (CompareImages, RenderTests.cpp:7-33) with at least 90% of
-pixels RGBE-identical. Evaluated on a 1-in-64 pixel lattice to keep the CPU
-suite short.
+pixels RGBE-identical. Evaluated on a 1-in-16 pixel lattice (4096 pixels) to
+keep the CPU suite short; the MSE is the reference's whole-image statistic
+estimated on that lattice.
 """
 import numpy as np
 import pytest
@@ -17,8 +18,8 @@ from vviewer_gb300 import scenes
 from vviewer_gb300.assets import rgbe_decode, rgbe_encode
 
 
-def lattice(stride=8, w=256, h=256):
-    ys, xs = np.meshgrid(np.arange(stride // 2, h, stride), np.arange(stride // 2, w, stride), indexing="ij")
+def lattice(stride=4, w=256, h=256):
+    ys, xs = np.meshgrid(np.arange(0, h, stride), np.arange(0, w, stride), indexing="ij")
     return (ys * w + xs).reshape(-1)
 
 
@@ -41,7 +42,7 @@ def test_oracle_reproduces_reference_golden(name):
     e, info, tol = R.BUILDERS[name]()
     fs = e.scene.build()
     sd = e.scene.scene_data(info.width, info.height)
-    pix = lattice(8)
+    pix = lattice(4)
     out = oracle.render(fs, sd, info, pixels=pix)
     mse, indep, exact = golden_check(name, out["radiance_m2"], out["radiance"], pix, info.samples // info.batch_size)
     assert mse <= tol, f"{name}: mse {mse:.3e} > reference tolerance {tol:.0e} (independent-noise mse {indep:.3e})"
