@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 path tracer.
+
+Workload (default): the Cornell room filled with a homogeneous isotropic
+medium (sigma_a 0.05, sigma_s 0.2) plus 998,560 triangles as eight seeded
+Perlin-displaced geodesic spheres with metallic/roughness materials,
+1920 x 1080, 256 samples per pixel, depth 12, batch size 4: 530,841,600 paths
+per step. A step is one full render through the C ABI (vvpt_render).
+
+Our arm prints one JSON line: value = paths/s with the scene resident and the
+outputs in device memory, timed with CUDA events on the stream the kernels run
+on, a 512 MB L2 flush before every step; e2e = the same render with host
+(pinned) output buffers, so the three RGBA32F images come back every step;
+roofline = the dominant wavefront kernel's algorithmic bytes per launch over
+its CUDA-event launch time (from a profiled render of the same workload);
+cpu_baseline = the CPU oracle on a bounded pixel sample of the same workload.
+
+--impl reference times the reference's path on the host cores. The reference
+implements this path only as GLSL ray-tracing shaders that need a Vulkan RT
+device, so the CPU restatement of those shaders (the oracle) stands in for it.
+
+N > 1 GPUs (torchrun): every rank renders the full workload as an
+independent replica (the path needs no exchange; replicas only), value is the
+aggregate paths/s over the max per-rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "paths/sec"
+UNIT = "paths/s"
+
+
+def workload(name: str):
+    from vviewer_gb300 import scenes
+    if name == "cornell_medium":
+        engine, info = scenes.cornell_medium(seed=1)
+        desc = {"workload": "cornell_medium_1080p", "width": info.width, "height": info.height,
+                "spp": info.samples, "depth": info.depth, "batch_size": info.batch_size,
+                "triangles": 998596, "medium": {"sigma_a": 0.05, "sigma_s": 0.2, "g": 0.0},
+                "materials": "Lambert walls, metallic/roughness spheres", "seed": 1}
+    elif name == "cornell":
+        engine, info = scenes.cornell_box(seed=1)
+        desc = {"workload": "cornell_256", "width": info.width, "height": info.height, "spp": info.samples,
+                "depth": info.depth, "batch_size": info.batch_size, "triangles": 36, "seed": 1}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return engine, info, desc
+
+
+def apply_overrides(engine, info, desc, args):
+    """Smaller cases of the same scene (profiling captures); the default is the full workload."""
+    if args.width or args.height or args.spp:
+        info.width = args.width or info.width
+        info.height = args.height or info.height
+        info.samples = args.spp or info.samples
+        desc = {**desc, "workload": f"{desc['workload']}_{info.width}x{info.height}_{info.samples}spp",
+                "width": info.width, "height": info.height, "spp": info.samples}
+    return engine, info, desc
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        text = f.read_text()
+        m = re.search(rf"traffic_per_launch\[{re.escape(kernel)}@{re.escape(workload_name)}\]\s*=\s*([0-9.eE+]+)", text)
+        if m:
+            return float(m.group(1)), f.name
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(engine, info, target_s: float = 15.0) -> dict:
+    """The CPU oracle on a bounded, evenly spread pixel sample at full spp."""
+    from oracle import oracle
+    flat = engine.scene.build()
+    sd = engine.scene.scene_data(info.width, info.height)
+    npix = info.width * info.height
+    cores = os.cpu_count() or 1
+
+    def run(k):
+        pix = np.linspace(0, npix - 1, k).astype(np.uint32)
+        t = time.perf_counter()
+        oracle.render(flat, sd, info, pixels=pix, threads=cores)
+        return time.perf_counter() - t
+
+    k = 4 * cores
+    dt = run(k)
+    while dt < 1.0 and k < npix:
+        k = min(npix, k * 4)
+        dt = run(k)
+    k = int(min(npix, max(k, k * target_s / max(dt, 1e-6))))
+    dt = run(k)
+    paths = k * (info.samples // info.batch_size) * info.batch_size
+    return {"value": paths / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{k} of {npix} pixels evenly spread, all {info.samples} spp, depth {info.depth}: "
+                      f"{paths} paths in {dt:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    engine, info, desc = apply_overrides(*workload(args.workload), args)
+    flat = engine.scene.build()
+    sd = engine.scene.scene_data(info.width, info.height)
+    npix = info.width * info.height
+    cores = os.cpu_count() or 1
+    spp = (info.samples // info.batch_size) * info.batch_size
+    # size one step at about 6 s of CPU work
+    def timed(k):
+        t = time.perf_counter()
+        oracle.render(flat, sd, info, pixels=np.linspace(0, npix - 1, k).astype(np.uint32), threads=cores)
+        return time.perf_counter() - t
+
+    k = 8 * cores
+    dt = timed(k)
+    while dt < 1.0 and k < npix:
+        k = min(npix, k * 4)
+        dt = timed(k)
+    k = int(min(npix, max(k, k * 6.0 / max(dt, 1e-6))))
+    pix = np.linspace(0, npix - 1, k).astype(np.uint32)
+    for _ in range(args.warmup):
+        oracle.render(flat, sd, info, pixels=pix, threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle.render(flat, sd, info, pixels=pix, threads=cores)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = k * spp * args.steps / total
+    sample = f"{k} of {npix} pixels evenly spread per step, all {info.samples} spp, depth {info.depth}"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": desc, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference implements this path only as Vulkan ray-tracing shaders; its CPU "
+                    "restatement (oracle/) runs on all host cores"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    from vviewer_gb300 import Context
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    engine, info, desc = apply_overrides(*workload(args.workload), args)
+    t0 = time.perf_counter()
+    flat = engine.scene.build()
+    sd = engine.scene.scene_data(info.width, info.height)
+    scene_prep_s = time.perf_counter() - t0
+    ctx = Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    gpu = ctx.upload(flat)
+    upload_s = time.perf_counter() - t0
+    H, W = info.height, info.width
+    dev = {k: torch.zeros((H, W, 4), dtype=torch.float32, device="cuda") for k in ("radiance", "albedo", "normal")}
+    dev_ptrs = {k: v.data_ptr() for k, v in dev.items()}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    paths_per_step = W * H * (info.samples // info.batch_size) * info.batch_size
+
+    for _ in range(args.warmup):
+        gpu.render(sd, info, outputs=dev_ptrs)
+    torch.cuda.synchronize()
+
+    step_ms = []
+    launches = 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # evict L2 between steps
+            barrier()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gpu.render(sd, info, outputs=dev_ptrs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            step_ms.append(e0.elapsed_time(e1))
+            launches += int(ctx.stats().kernel_launches)
+    clock = clocks.summary()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * paths_per_step * args.steps / (total_ms / 1e3)
+    stats = ctx.stats()
+
+    # e2e: host (pinned) output buffers, SceneData/RenderInfo from the host every step
+    pinned = {k: torch.zeros((H, W, 4), dtype=torch.float32).pin_memory() for k in ("radiance", "albedo", "normal")}
+    host_ptrs = {k: v.data_ptr() for k, v in pinned.items()}
+    e2e_s = []
+    for i in range(args.warmup + args.steps):
+        sd_step = engine.scene.scene_data(W, H)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        barrier()
+        t = time.perf_counter()
+        gpu.render(sd_step, info, host_outputs=host_ptrs)
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            e2e_s.append(dt)
+    e2e_total = sum(e2e_s)
+    if world > 1:
+        t = torch.tensor([e2e_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    import ctypes as C
+
+    from vviewer_gb300 import _native as N
+    e2e = {"value": world * paths_per_step * args.steps / e2e_total, "unit": UNIT,
+           "h2d_bytes_per_step": C.sizeof(N.SceneData) + C.sizeof(N.RenderInfo),
+           "d2h_bytes_per_step": 3 * H * W * 16}
+
+    # roofline of the dominant kernel from one profiled render of the same workload
+    gpu.render(sd, info, outputs=dev_ptrs, profile=True)
+    prof = [k for k in ctx.kernel_profile() if k["name"] != "k_begin"]
+    total_prof = sum(k["total_ms"] for k in ctx.kernel_profile())
+    dom = max(prof, key=lambda k: k["total_ms"])
+    avg_ms = dom["total_ms"] / max(dom["launches"], 1)
+    bytes_per_launch = dom["units"] * dom["bytes_per_unit"] / max(dom["launches"], 1)
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic, traffic_src = profiled_traffic(dom["name"], desc["workload"])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dom["name"], "peak_source": f"{peak_kind} hbm_gbs (copy)",
+                "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
+                "traffic_source": traffic_src,
+                "kernels": [{**k, "share": k["total_ms"] / total_prof} for k in ctx.kernel_profile()]}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {**desc, "parallelism": f"replicas x{world}",
+                       "l2": "512 MB L2 flush before every step; working set (path state + per-batch sums) > L2"},
+            "e2e": e2e, "roofline": roofline, "gpu_launches": launches, "clocks": clock,
+            "segments_per_step": int(stats.segments), "shadow_rays_per_step": int(stats.shadow_rays),
+            "emitter_rays_per_step": int(stats.emitter_rays), "scene_prep_s": scene_prep_s,
+            "scene_upload_bvh_s": upload_s}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(engine, info)
+    gpu.release()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["cornell_medium", "cornell"], default="cornell_medium")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=0)
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

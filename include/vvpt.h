@@ -205,7 +205,10 @@ typedef struct vvpt_render_info {
 enum {
     /* also return per-pixel sum over batches of the squared batch sums
      * (radiance only), for Monte Carlo error estimates */
-    VVPT_RENDER_WANT_BATCH_M2 = 1u
+    VVPT_RENDER_WANT_BATCH_M2 = 1u,
+    /* launch the wavefront kernels one by one with CUDA events around each
+     * (no graphs) and record per-kernel times: see vvpt_last_kernel_profile */
+    VVPT_RENDER_PROFILE_KERNELS = 2u
 };
 
 /* Output images, RGBA32F row-major W*H*4 floats each, A = 1 (the three
@@ -295,6 +298,29 @@ typedef struct vvpt_render_stats {
     double device_ms;
 } vvpt_render_stats;
 VVPT_API vvpt_status vvpt_last_render_stats(vvpt_ctx *ctx, vvpt_render_stats *out_stats);
+
+/* Per-kernel profile of the last render made with
+ * VVPT_RENDER_PROFILE_KERNELS: for each wavefront kernel, launches, work
+ * units (queue entries) processed, summed CUDA-event time, and the kernel's
+ * algorithmic bytes per unit (compulsory path-state and queue traffic plus
+ * shading-vertex fetches; BVH nodes and textures excluded). */
+typedef struct vvpt_kernel_profile_entry {
+    char name[24];
+    uint64_t launches;
+    uint64_t units;
+    double total_ms;
+    double bytes_per_unit;
+} vvpt_kernel_profile_entry;
+typedef struct vvpt_kernel_profile {
+    uint32_t count;
+    vvpt_kernel_profile_entry kernels[8];
+} vvpt_kernel_profile;
+VVPT_API vvpt_status vvpt_last_kernel_profile(vvpt_ctx *ctx, vvpt_kernel_profile *out_profile);
+
+/* Runs the context's work on a caller-owned CUDA stream (a cudaStream_t
+ * passed as void*); NULL restores the context's own stream. Calls stay
+ * synchronous with respect to the host. */
+VVPT_API vvpt_status vvpt_set_stream(vvpt_ctx *ctx, void *cuda_stream);
 
 /* Tuning knobs (path-slot pool size and blocks per SM for the wavefront
  * kernels); 0 = automatic. */

@@ -1,0 +1,280 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the CPU oracle
+and against the reference's golden images.
+
+Tolerances:
+  * closest hit: instance, primitive, t, u, v bit-identical (integer/index
+    work and an exactly rounded triangle test);
+  * renders vs the oracle (same RTGEMS stream, FP32 path arithmetic): image
+    mean within 1e-4 relative, >= 95% of pixels within 1e-3 relative, and the
+    remaining pixels within Monte Carlo noise (|z| > 4 on < 0.5%);
+  * renders vs the reference goldens: the reference's own MSE tolerance
+    (CompareImages, src/bin/unittests/RenderTests.cpp:7-33).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import reference_scenes as R
+from oracle import oracle
+from vviewer_gb300 import _native as N
+from vviewer_gb300 import scenes
+from vviewer_gb300.assets import rgbe_decode, rgbe_encode
+from vviewer_gb300.renderer import RenderInfo
+from vviewer_gb300.scene import EnvironmentType, Engine, MaterialLambert, Transform
+
+pytestmark = pytest.mark.gpu
+
+
+def world_triangles(fs):
+    """World-space vertices of every TLAS triangle: (T x 3 x 3)."""
+    out = []
+    for inst in fs.instances:
+        if not inst.flags & 1:
+            continue
+        m = fs.meshes[inst.mesh_index]
+        M = np.array(list(inst.model), dtype=np.float64).reshape(4, 4).T
+        p = m.vertices["position"][m.indices.astype(np.int64)].astype(np.float64)
+        w = p @ M[:3, :3].T + M[:3, 3]
+        out.append(w)
+    return np.concatenate(out)
+
+
+def make_rays(fs, n, seed, lo, hi):
+    rng = np.random.default_rng(seed)
+    tris = world_triangles(fs)
+    k = n // 2
+    # random rays
+    o1 = rng.uniform(lo, hi, (k, 3))
+    d1 = rng.normal(size=(k, 3))
+    # rays aimed at triangle interiors, edges and vertices (watertightness, ties)
+    pick = tris[rng.integers(0, len(tris), n - k)]
+    bc = rng.dirichlet([1, 1, 1], n - k)
+    kind = rng.integers(0, 3, n - k)
+    bc[kind == 1, 2] = 0.0  # edge v0-v1
+    bc[kind == 2] = [1.0, 0.0, 0.0]  # vertex
+    bc /= bc.sum(1, keepdims=True)
+    target = (pick * bc[:, :, None]).sum(1)
+    o2 = rng.uniform(lo, hi, (n - k, 3))
+    d2 = target - o2
+    o = np.concatenate([o1, o2])
+    d = np.concatenate([d1, d2])
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tmin = np.where(rng.random(n) < 0.5, 0.0, 1e-3)
+    rays = np.concatenate([o, tmin[:, None], d, np.full((n, 1), 1e4)], 1).astype(np.float32)
+    return rays
+
+
+def assert_hits_equal(hg, ho):
+    for f in ("instance", "primitive", "t", "u", "v"):
+        eq = hg[f] == ho[f]
+        assert eq.all(), f"{f}: {np.count_nonzero(~eq)} of {len(eq)} differ, first {np.nonzero(~eq)[0][:5]}"
+
+
+HIT_SCENES = {
+    "cornell": (lambda: scenes.cornell_box(1)[0], (-0.2, 1.2)),
+    "two_balls_mesh_light": (lambda: R.mesh_light()[0], (-3.0, 4.0)),
+    "volume_cube": (lambda: R.volume(9)[0], (-3.0, 4.0)),
+    "shared_components": (lambda: R.shared_components()[0], (-160.0, 160.0)),
+    "displaced_spheres": (lambda: scenes.cornell_medium(3, freq=12, spheres=8)[0], (-0.2, 1.2)),
+}
+
+
+@pytest.mark.parametrize("name", list(HIT_SCENES))
+def test_closest_hit_bit_exact(ctx, name):
+    build, (lo, hi) = HIT_SCENES[name]
+    fs = build().scene.build()
+    g = ctx.upload(fs)
+    rays = make_rays(fs, 200_000 if name != "shared_components" else 50_000, 7, lo, hi)
+    hg = g.trace_closest(rays)
+    ho = oracle.trace_closest(fs, rays)
+    assert (hg["instance"] != 0xFFFFFFFF).mean() > 0.3
+    assert_hits_equal(hg, ho)
+    g.release()
+
+
+def test_closest_hit_empty_and_degenerate(ctx):
+    e = Engine()
+    s = e.scene
+    so = s.add_scene_object("light", Transform((0, 1, 0)))
+    so.light = e.light("defaultPointLight")
+    fs = s.build()
+    g = ctx.upload(fs)
+    rays = np.array([[0, 0, 0, 0, 0, 0, 1, 10], [0, 0, 0, 0, 1, 0, 0, 10]], dtype=np.float32)
+    h = g.trace_closest(rays)
+    assert (h["instance"] == 0xFFFFFFFF).all()
+    g.release()
+
+
+def compare_renders(a, b, m2a, batches):
+    a = a[..., :3].astype(np.float64)
+    b = b[..., :3].astype(np.float64)
+    rel_mean = abs(a.mean() - b.mean()) / max(b.mean(), 1e-12)
+    close = np.isclose(a, b, rtol=1e-3, atol=1e-7).all(-1)
+    var = np.maximum(batches * m2a[..., :3].astype(np.float64) - a * a, 0.0) / max(batches - 1, 1)
+    z = np.abs(a - b) / np.sqrt(2.0 * var + 1e-20)
+    return rel_mean, close.mean(), (z > 4).any(-1).mean()
+
+
+def render_pair(ctx, engine, info, **kw):
+    fs = engine.scene.build()
+    sd = engine.scene.scene_data(info.width, info.height)
+    g = ctx.upload(fs)
+    res = g.render(sd, info, want_m2=True)
+    g.release()
+    ref = oracle.render(fs, sd, info, **kw)
+    return res, ref
+
+
+def test_cornell_render_matches_oracle(ctx):
+    e, info = scenes.cornell_box(1, 128, 128, 64, 8, 4)
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+    assert (res.albedo == ref["albedo"]).all(-1).mean() >= 0.99
+    assert (res.normal == ref["normal"]).all(-1).mean() >= 0.99
+    assert res.stats.paths == 128 * 128 * 64
+    assert res.stats.kernel_launches > 0
+
+
+def test_medium_scene_matches_oracle(ctx):
+    e, info = scenes.cornell_medium(2, 96, 54, 16, 12, 4, freq=10, spheres=8)
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-3 and close >= 0.9 and z4 < 0.01, (rel, close, z4)
+
+
+def test_thin_lens_and_non_square_match_oracle(ctx):
+    e, info = scenes.cornell_box(4, 80, 48, 16, 8, 4)
+    cam = e.scene.camera
+    cam.lens_radius = 0.05
+    cam.focal_distance = 1.8
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+
+
+@pytest.mark.parametrize("mode", [EnvironmentType.HDRI, EnvironmentType.SOLID_COLOR_WITH_HDRI_LIGHTING])
+def test_environment_map_matches_oracle(ctx, mode):
+    e, info = scenes.cornell_box(5, 64, 64, 16, 8, 4)
+    s = e.scene
+    # open the room to the sky: remove the back wall's occlusion by moving the camera out
+    s.camera.transform = Transform((0.5, 0.5, 3.0))
+    h, w = 32, 64
+    yy, xx = np.meshgrid(np.linspace(0, 1, h), np.linspace(0, 1, w), indexing="ij")
+    env = np.stack([0.2 + xx, 0.3 + yy, 1.0 - 0.5 * yy, np.ones_like(xx)], -1).astype(np.float32)
+    s.environment_map = env
+    s.environment_type = mode
+    s.environment_intensity = 0.7
+    s.background_color = [0.1, 0.2, 0.3]
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+
+
+@pytest.mark.parametrize("name", list(R.BUILDERS))
+def test_gpu_render_meets_reference_golden(ctx, name):
+    e, info, tol = R.BUILDERS[name]()
+    fs = e.scene.build()
+    sd = e.scene.scene_data(256, 256)
+    g = ctx.upload(fs)
+    res = g.render(sd, info)
+    g.release()
+    enc = rgbe_encode(res.radiance[..., :3])
+    mse = R.compare_images(rgbe_decode(enc), R.golden(name))
+    exact = (enc == R.golden_rgbe(name)).all(-1).mean()
+    assert mse <= tol, f"{name}: mse {mse:.3e} > reference tolerance {tol:.0e} (RGBE-identical {exact:.3f})"
+    assert exact >= 0.9
+
+
+def test_render_is_deterministic_across_schedules(ctx):
+    e, info = scenes.cornell_box(6, 64, 64, 32, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(64, 64)
+    g = ctx.upload(fs)
+    a = g.render(sd, info)
+    b = g.render(sd, info)
+    ctx.set_tuning(slots=1000, blocks_per_sm=1, threads_per_block=128, iterations_per_graph=2)
+    try:
+        c = g.render(sd, info)
+    finally:
+        ctx.set_tuning()
+    g.release()
+    for k in ("radiance", "albedo", "normal"):
+        assert (getattr(a, k) == getattr(b, k)).all()
+        assert (getattr(a, k) == getattr(c, k)).all()
+
+
+def test_render_edge_cases(ctx):
+    e, info = scenes.cornell_box(1, 32, 32, 8, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(32, 32)
+    g = ctx.upload(fs)
+    info.depth = 0
+    assert (g.render(sd, info).radiance == 0).all()
+    info.depth, info.samples = 8, 3  # batches = 3 / 4 = 0
+    assert (g.render(sd, info).radiance == 0).all()
+    info.samples, info.batch_size = 8, 8  # one batch
+    r = g.render(sd, info)
+    assert np.isfinite(r.radiance).all() and r.radiance[..., :3].sum() > 0
+    assert (r.radiance[..., 3] == 1.0).all()
+    g.release()
+
+
+def test_light_only_scene_renders_background(ctx):
+    e = Engine()
+    s = e.scene
+    so = s.add_scene_object("light", Transform((0, 1, 0)))
+    so.light = e.light("defaultPointLight")
+    s.background_color = [0.25, 0.5, 0.75]
+    info = RenderInfo(samples=4, depth=4, batch_size=2, width=16, height=16, write_files=False)
+    g = ctx.upload(s.build())
+    r = g.render(s.scene_data(16, 16), info)
+    g.release()
+    assert np.allclose(r.radiance[..., :3], [0.25, 0.5, 0.75], atol=1e-6)
+    assert np.allclose(r.albedo[..., :3], [0.25, 0.5, 0.75], atol=1e-6)
+
+
+def test_device_outputs_equal_host_outputs(ctx):
+    torch = pytest.importorskip("torch")
+    e, info = scenes.cornell_box(2, 48, 32, 8, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(48, 32)
+    g = ctx.upload(fs)
+    host = g.render(sd, info)
+    bufs = {k: torch.zeros((32, 48, 4), dtype=torch.float32, device="cuda") for k in ("radiance", "albedo", "normal")}
+    g.render(sd, info, outputs={k: v.data_ptr() for k, v in bufs.items()})
+    torch.cuda.synchronize()
+    g.release()
+    for k, v in bufs.items():
+        assert (v.cpu().numpy() == getattr(host, k)).all()
+
+
+def test_invalid_arguments_are_reported(ctx):
+    e, info = scenes.cornell_box(1, 16, 16, 4, 4, 4)
+    fs = e.scene.build()
+    fs.instances[0].material_index = 999
+    with pytest.raises(N.VvptError) as ei:
+        ctx.upload(fs)
+    assert ei.value.status == 1 and "material" in str(ei.value)
+    fs = e.scene.build()
+    g = ctx.upload(fs)
+    sd = e.scene.scene_data(16, 16)
+    info.width = 0
+    with pytest.raises(N.VvptError):
+        g.render(sd, info)
+    info.width = 16
+    sd.volumes[0] = 999.0
+    with pytest.raises(N.VvptError):
+        g.render(sd, info)
+    g.release()
+
+
+def test_progress_reaches_one(ctx):
+    e, info = scenes.cornell_box(1, 16, 16, 4, 4, 4)
+    g = ctx.upload(e.scene.build())
+    g.render(e.scene.scene_data(16, 16), info)
+    p = C.c_float()
+    ctx.lib.vvpt_progress(ctx.handle, C.byref(p))
+    assert p.value == 1.0
+    g.release()

@@ -116,6 +116,18 @@ class Tuning(C.Structure):
                 ("iterations_per_graph", C.c_uint32)]
 
 
+class KernelProfileEntry(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("launches", C.c_uint64), ("units", C.c_uint64), ("total_ms", C.c_double),
+                ("bytes_per_unit", C.c_double)]
+
+
+class KernelProfile(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("kernels", KernelProfileEntry * 8)]
+
+
+RENDER_PROFILE_KERNELS = 2
+
+
 # every symbol include/vvpt.h declares, with its ctypes signature
 _SIGNATURES = {
     "vvpt_version": (C.c_char_p, []),
@@ -132,6 +144,8 @@ _SIGNATURES = {
     "vvpt_last_render_stats": (C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     "vvpt_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "vvpt_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "vvpt_last_kernel_profile": (C.c_int, [C.c_void_p, C.POINTER(KernelProfile)]),
+    "vvpt_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

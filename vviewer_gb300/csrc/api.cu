@@ -5,6 +5,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -84,12 +85,16 @@ struct vvpt_ctx {
     vvpt_render_stats stats{};
     vvpt_tuning tuning{};
     // render buffers (grow-only, reused across renders)
-    DevBuf state, queues, results, params, outputs, counters_host_dummy;
+    DevBuf state, queues, results, params, outputs;
     uint32_t *counters_pinned = nullptr;
     DevBuf rays, hits_tuv, hits_ids, err_word;
+    cudaStream_t user_stream = nullptr;
+    vvpt_kernel_profile profile{};
 };
 
 namespace {
+
+inline cudaStream_t vv_stream(const vvpt_ctx *ctx) { return ctx->user_stream ? ctx->user_stream : ctx->stream; }
 
 vvpt_status fail(vvpt_ctx *ctx, vvpt_status code, const std::string &msg)
 {
@@ -155,7 +160,7 @@ vvpt_status upload(vvpt_ctx *ctx, DevBuf &buf, const std::vector<T> &v, uint64_t
     size_t n = v.size() * sizeof(T);
     VV_CUDA(buf.alloc(n), "cudaMalloc scene buffer");
     if (n)
-        VV_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), n, cudaMemcpyHostToDevice, ctx->stream), "upload scene buffer");
+        VV_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), n, cudaMemcpyHostToDevice, vv_stream(ctx)), "upload scene buffer");
     bytes += buf.bytes;
     return VVPT_OK;
 }
@@ -206,7 +211,7 @@ VVPT_API vvpt_status vvpt_destroy(vvpt_ctx *ctx)
     if (!ctx)
         return VVPT_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(vv_stream(ctx));
     if (ctx->counters_pinned)
         cudaFreeHost(ctx->counters_pinned);
     cudaStreamDestroy(ctx->stream);
@@ -564,7 +569,7 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
         return st;
     if ((st = upload(ctx, scene->texels, texels, bytes)) != VVPT_OK)
         return st;
-    VV_CUDA(cudaStreamSynchronize(ctx->stream), "scene upload");
+    VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "scene upload");
 
     SceneView &v = scene->view;
     v.nodes = scene->nodes.as<BVHNode>();
@@ -596,7 +601,7 @@ VVPT_API vvpt_status vvpt_scene_release(vvpt_ctx *ctx, vvpt_scene *scene)
         return VVPT_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(vv_stream(ctx));
     delete scene;
     return VVPT_OK;
 }
@@ -622,6 +627,25 @@ VVPT_API vvpt_status vvpt_last_render_stats(vvpt_ctx *ctx, vvpt_render_stats *ou
     if (!ctx || !out)
         return VVPT_ERR_INVALID_ARG;
     *out = ctx->stats;
+    return VVPT_OK;
+}
+
+VVPT_API vvpt_status vvpt_last_kernel_profile(vvpt_ctx *ctx, vvpt_kernel_profile *out)
+{
+    if (!ctx || !out)
+        return VVPT_ERR_INVALID_ARG;
+    *out = ctx->profile;
+    return VVPT_OK;
+}
+
+VVPT_API vvpt_status vvpt_set_stream(vvpt_ctx *ctx, void *cuda_stream)
+{
+    if (!ctx)
+        return VVPT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(vv_stream(ctx));
+    ctx->user_stream = reinterpret_cast<cudaStream_t>(cuda_stream);
     return VVPT_OK;
 }
 
@@ -690,7 +714,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         // nothing traced: the reference's images stay zero (alpha untouched)
         for (int k = 0; k < 4; k++)
             if (d_out[k])
-                VV_CUDA(cudaMemsetAsync(d_out[k], 0, img_bytes, ctx->stream), "clear outputs");
+                VV_CUDA(cudaMemsetAsync(d_out[k], 0, img_bytes, vv_stream(ctx)), "clear outputs");
     } else {
         // ---- path state and queues
         uint32_t slots = ctx->tuning.slots ? ctx->tuning.slots : (1u << 20);
@@ -754,7 +778,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
 
         VV_CUDA(ctx->params.reserve(sizeof(RenderParams)), "cudaMalloc params");
         RenderParams *dparams = ctx->params.as<RenderParams>();
-        VV_CUDA(cudaMemcpyAsync(dparams, &hp, sizeof(hp), cudaMemcpyHostToDevice, ctx->stream), "upload params");
+        VV_CUDA(cudaMemcpyAsync(dparams, &hp, sizeof(hp), cudaMemcpyHostToDevice, vv_stream(ctx)), "upload params");
 
         LaunchShape shape;
         shape.block = ctx->tuning.threads_per_block ? (int)ctx->tuning.threads_per_block : 256;
@@ -762,18 +786,92 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         shape.grid = std::max(1, ctx->num_sms * bps);
         const int K = ctx->tuning.iterations_per_graph ? (int)ctx->tuning.iterations_per_graph : 8;
 
-        launch_init_slots(q, ps, slots, ctx->stream);
+        cudaEvent_t tev[2];
+        cudaEventCreate(&tev[0]);
+        cudaEventCreate(&tev[1]);
+        struct EventGuard {
+            cudaEvent_t *e;
+            ~EventGuard()
+            {
+                cudaEventDestroy(e[0]);
+                cudaEventDestroy(e[1]);
+            }
+        } tev_guard{tev};
+        VV_CUDA(cudaEventRecord(tev[0], vv_stream(ctx)), "event");
+        launch_init_slots(q, ps, slots, vv_stream(ctx));
         stats.kernel_launches += 1;
         VV_CUDA(cudaGetLastError(), "launch init");
+        const uint64_t max_iters =
+            (uint64_t)hp.batch_size * (hp.depth + 1) * ((hp.total_items + slots - 1) / slots + 1) + 64;
 
+        if (info->flags & VVPT_RENDER_PROFILE_KERNELS) {
+            // one kernel at a time with events around each launch
+            static const char *names[K_NUM] = {"k_begin", "k_regen", "k_extend", "k_shade", "k_connect"};
+            static const double bpu[K_NUM] = {0.0, kBytesRegen, kBytesExtend, kBytesShade, kBytesConnect};
+            vvpt_kernel_profile prof{};
+            prof.count = K_NUM;
+            for (int k = 0; k < K_NUM; k++) {
+                std::snprintf(prof.kernels[k].name, sizeof(prof.kernels[k].name), "%s", names[k]);
+                prof.kernels[k].bytes_per_unit = bpu[k];
+            }
+            cudaEvent_t ka, kb;
+            cudaEventCreate(&ka);
+            cudaEventCreate(&kb);
+            uint64_t it = 0;
+            vvpt_status pst = VVPT_OK;
+            for (;; it++) {
+                const int pp = (int)(it & 1);
+                for (int k = 0; k < K_NUM; k++) {
+                    VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t),
+                                            cudaMemcpyDeviceToHost, vv_stream(ctx)),
+                            "read counters");
+                    VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "profile sync");
+                    const uint32_t *c = ctx->counters_pinned;
+                    uint64_t units = k == K_REGEN    ? c[C_REGEN0 + pp]
+                                     : k == K_EXTEND ? c[C_EXT0 + pp]
+                                     : k == K_SHADE  ? (uint64_t)c[C_SHADE_L] + c[C_SHADE_P] + c[C_SHADE_M]
+                                     : k == K_CONNECT ? c[C_CONN]
+                                                      : 1;
+                    cudaEventRecord(ka, vv_stream(ctx));
+                    launch_kernel((KernelId)k, scene->view, dparams, ps, q, br, pp, shape, vv_stream(ctx));
+                    cudaEventRecord(kb, vv_stream(ctx));
+                    VV_CUDA(cudaEventSynchronize(kb), "profile kernel");
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, ka, kb);
+                    prof.kernels[k].launches += 1;
+                    prof.kernels[k].units += units;
+                    prof.kernels[k].total_ms += ms;
+                    stats.kernel_launches += 1;
+                }
+                VV_CUDA(cudaMemcpy(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+                        "read counters");
+                const uint32_t *c = ctx->counters_pinned;
+                if (c[C_ERR]) {
+                    pst = fail(ctx, VVPT_ERR_DEVICE, "device status word set: " + std::to_string(c[C_ERR]));
+                    break;
+                }
+                if (c[C_NEXT_ITEM] >= hp.total_items && c[C_ACTIVE] == 0)
+                    break;
+                if (it > max_iters) {
+                    pst = fail(ctx, VVPT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+                    break;
+                }
+            }
+            cudaEventDestroy(ka);
+            cudaEventDestroy(kb);
+            if (pst != VVPT_OK)
+                return pst;
+            ctx->profile = prof;
+            stats.iterations = it + 1;
+        } else {
         // capture K iterations (K even keeps the ping-pong phase aligned)
         const int Ke = (K + 1) & ~1;
         cudaGraph_t graph;
         cudaGraphExec_t exec;
-        VV_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        VV_CUDA(cudaStreamBeginCapture(vv_stream(ctx), cudaStreamCaptureModeThreadLocal), "begin capture");
         for (int it = 0; it < Ke; it++)
-            launch_iteration(scene->view, dparams, ps, q, br, it & 1, shape, ctx->stream);
-        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+            launch_iteration(scene->view, dparams, ps, q, br, it & 1, shape, vv_stream(ctx));
+        cudaError_t ce = cudaStreamEndCapture(vv_stream(ctx), &graph);
         if (ce != cudaSuccess)
             return cuda_fail(ctx, ce, "end capture");
         ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -784,27 +882,25 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         cudaEvent_t ev[2];
         cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
-        // Bound on iterations: every slot-iteration advances a path by one
-        // segment, so the total is at most items * samples * depth segments
-        // spread over the slots, plus one regen per sample.
-        const uint64_t max_iters =
-            (uint64_t)hp.batch_size * (hp.depth + 1) * ((hp.total_items + slots - 1) / slots + 1) + 64;
+        // Bound on iterations (max_iters): every slot-iteration advances a
+        // path by one segment, so the total is at most samples * depth
+        // segments per work item times the work items per slot.
         uint64_t iters = 0;
         int launched = 0;
         bool done = false;
         vvpt_status loop_status = VVPT_OK;
         // keep one graph in flight ahead of the counter check
-        VV_CUDA(cudaGraphLaunch(exec, ctx->stream), "graph launch");
-        VV_CUDA(cudaEventRecord(ev[0], ctx->stream), "event");
+        VV_CUDA(cudaGraphLaunch(exec, vv_stream(ctx)), "graph launch");
+        VV_CUDA(cudaEventRecord(ev[0], vv_stream(ctx)), "event");
         launched = 1;
         iters += Ke;
         while (!done) {
             VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t),
-                                    cudaMemcpyDeviceToHost, ctx->stream),
+                                    cudaMemcpyDeviceToHost, vv_stream(ctx)),
                     "read counters");
-            VV_CUDA(cudaEventRecord(ev[launched & 1], ctx->stream), "event");
+            VV_CUDA(cudaEventRecord(ev[launched & 1], vv_stream(ctx)), "event");
             int check = launched & 1;
-            VV_CUDA(cudaGraphLaunch(exec, ctx->stream), "graph launch");
+            VV_CUDA(cudaGraphLaunch(exec, vv_stream(ctx)), "graph launch");
             launched++;
             iters += Ke;
             VV_CUDA(cudaEventSynchronize(ev[check]), "wait counters");
@@ -827,7 +923,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                 break;
             }
         }
-        VV_CUDA(cudaStreamSynchronize(ctx->stream), "render");
+        VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "render");
         cudaGraphExecDestroy(exec);
         cudaEventDestroy(ev[0]);
         cudaEventDestroy(ev[1]);
@@ -835,6 +931,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
             return loop_status;
         stats.iterations = iters;
         stats.kernel_launches += (uint64_t)iters * kKernelsPerIteration;
+        }
         VV_CUDA(cudaMemcpy(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost),
                 "final counters");
         stats.segments = ctx->counters_pinned[C_SEGMENTS];
@@ -844,19 +941,24 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         if (ctx->counters_pinned[C_ERR])
             return fail(ctx, VVPT_ERR_DEVICE, "device status word set: " + std::to_string(ctx->counters_pinned[C_ERR]));
 
-        launch_reduce(hp, br, d_out[0], d_out[1], d_out[2], d_out[3], ctx->stream);
+        launch_reduce(hp, br, d_out[0], d_out[1], d_out[2], d_out[3], vv_stream(ctx));
         stats.kernel_launches += 1;
         VV_CUDA(cudaGetLastError(), "launch reduce");
+        VV_CUDA(cudaEventRecord(tev[1], vv_stream(ctx)), "event");
+        VV_CUDA(cudaEventSynchronize(tev[1]), "render");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, tev[0], tev[1]);
+        stats.device_ms = ms;
     }
 
     if (!out->on_device) {
         for (int k = 0; k < 4; k++)
             if (host_out[k])
-                VV_CUDA(cudaMemcpyAsync(host_out[k], d_out[k], img_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+                VV_CUDA(cudaMemcpyAsync(host_out[k], d_out[k], img_bytes, cudaMemcpyDeviceToHost, vv_stream(ctx)),
                         "download outputs");
     }
-    VV_CUDA(cudaStreamSynchronize(ctx->stream), "render finish");
-    stats.device_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "render finish");
+    (void)t_start;
     ctx->stats = stats;
     ctx->progress.store(1.0f);
     return VVPT_OK;
@@ -877,23 +979,23 @@ VVPT_API vvpt_status vvpt_trace_closest(vvpt_ctx *ctx, vvpt_scene *scene, const 
         d_rays = reinterpret_cast<const float4 *>(rays);
     } else {
         VV_CUDA(ctx->rays.reserve((size_t)n * 32), "cudaMalloc rays");
-        VV_CUDA(cudaMemcpyAsync(ctx->rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream), "upload rays");
+        VV_CUDA(cudaMemcpyAsync(ctx->rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, vv_stream(ctx)), "upload rays");
         d_rays = ctx->rays.as<float4>();
     }
     VV_CUDA(ctx->hits_tuv.reserve((size_t)n * 16), "cudaMalloc hits");
     VV_CUDA(ctx->hits_ids.reserve((size_t)n * 8), "cudaMalloc hits");
     VV_CUDA(ctx->err_word.reserve(16), "cudaMalloc err");
-    VV_CUDA(cudaMemsetAsync(ctx->err_word.ptr, 0, 4, ctx->stream), "clear err");
+    VV_CUDA(cudaMemsetAsync(ctx->err_word.ptr, 0, 4, vv_stream(ctx)), "clear err");
     launch_trace_closest(scene->view, d_rays, n, ctx->hits_tuv.as<float4>(), ctx->hits_ids.as<uint32_t>(),
-                         ctx->err_word.as<uint32_t>(), ctx->stream);
+                         ctx->err_word.as<uint32_t>(), vv_stream(ctx));
     VV_CUDA(cudaGetLastError(), "launch trace");
     std::vector<float4> tuv(n);
     std::vector<uint32_t> ids(2 * (size_t)n);
     uint32_t err = 0;
-    VV_CUDA(cudaMemcpyAsync(tuv.data(), ctx->hits_tuv.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
-    VV_CUDA(cudaMemcpyAsync(ids.data(), ctx->hits_ids.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
-    VV_CUDA(cudaMemcpyAsync(&err, ctx->err_word.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
-    VV_CUDA(cudaStreamSynchronize(ctx->stream), "trace");
+    VV_CUDA(cudaMemcpyAsync(tuv.data(), ctx->hits_tuv.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost, vv_stream(ctx)), "d2h");
+    VV_CUDA(cudaMemcpyAsync(ids.data(), ctx->hits_ids.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, vv_stream(ctx)), "d2h");
+    VV_CUDA(cudaMemcpyAsync(&err, ctx->err_word.ptr, 4, cudaMemcpyDeviceToHost, vv_stream(ctx)), "d2h");
+    VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "trace");
     std::vector<vvpt_hit> hv(n);
     for (uint32_t i = 0; i < n; i++) {
         hv[i].t = tuv[i].x;

@@ -1064,6 +1064,30 @@ void launch_iteration(const SceneView &s, const RenderParams *dparams, const Pat
     k_connect<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
 }
 
+void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
+                   const BatchResults &br, int pp, const LaunchShape &shape, cudaStream_t stream)
+{
+    switch (k) {
+    case K_BEGIN:
+        k_begin<<<1, 32, 0, stream>>>(q, pp);
+        break;
+    case K_REGEN:
+        k_regen<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, br, pp);
+        break;
+    case K_EXTEND:
+        k_extend<<<shape.grid, shape.block, 0, stream>>>(s, ps, q, pp);
+        break;
+    case K_SHADE:
+        k_shade<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, pp);
+        break;
+    case K_CONNECT:
+        k_connect<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        break;
+    default:
+        break;
+    }
+}
+
 void launch_reduce(const RenderParams &hp, const BatchResults &br, float4 *radiance, float4 *albedo, float4 *normal,
                    float4 *radiance_m2, cudaStream_t stream)
 {

@@ -105,4 +105,20 @@ void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, fl
                           uint32_t *err, cudaStream_t stream);
 constexpr int kKernelsPerIteration = 5;
 
+// One wavefront kernel, launched on its own (profiling mode).
+enum KernelId { K_BEGIN = 0, K_REGEN = 1, K_EXTEND = 2, K_SHADE = 3, K_CONNECT = 4, K_NUM = 5 };
+void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
+                   const BatchResults &br, int pingpong, const LaunchShape &shape, cudaStream_t stream);
+
+// Algorithmic bytes per work unit of each kernel: the path-state, queue and
+// hit-record loads and stores the kernel's code performs for one queue entry
+// (nominal branch), plus the three shading vertices and their indices read by
+// shade. BVH nodes, triangles and textures are excluded.
+constexpr double kBytesRegen = 4 + 3 * 4 + 3 * sizeof(float4) + 3 * sizeof(float4) + 4 + 9 * sizeof(float4) + 5 * 4 + 4;
+constexpr double kBytesExtend = 4 + 2 * sizeof(float4) + sizeof(float4) + 4 + 4;
+constexpr double kBytesShade = 4 + (4 + 4 + 4 + 4) + 5 * sizeof(float4) /* beta rad o d hit */ + 3 * 4 +
+                               3 * sizeof(ShadeVertex) /* vertices */ + (4 + 4 + 4) + 4 * sizeof(float4) /* writes */ +
+                               5 * sizeof(float4) /* alb nrm sh_dir sh_c nee_b */ + 2 * 4;
+constexpr double kBytesConnect = 4 + 4 + 4 + 6 * sizeof(float4) /* o rad sh_dir sh_c d nee_b */ + sizeof(float4) + 4;
+
 }  // namespace vvpt

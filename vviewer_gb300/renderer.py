@@ -86,6 +86,18 @@ class Context:
         self.check(self.lib.vvpt_last_render_stats(self.handle, C.byref(s)))
         return s
 
+    def kernel_profile(self) -> list[dict]:
+        """Per-kernel profile of the last render made with profile=True."""
+        p = N.KernelProfile()
+        self.check(self.lib.vvpt_last_kernel_profile(self.handle, C.byref(p)))
+        return [{"name": k.name.decode(), "launches": int(k.launches), "units": int(k.units),
+                 "total_ms": float(k.total_ms), "bytes_per_unit": float(k.bytes_per_unit)}
+                for k in p.kernels[:p.count]]
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Runs the context's work on a caller-owned CUDA stream (None: its own)."""
+        self.check(self.lib.vvpt_set_stream(self.handle, cuda_stream or None))
+
 
 class GpuScene:
     """A scene resident on the device (vvpt_scene_upload)."""
@@ -112,11 +124,19 @@ class GpuScene:
         return int(b.value)
 
     def render(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
-               outputs: dict | None = None) -> RenderResult | None:
-        """Renders into host arrays, or into device pointers when `outputs`
-        maps radiance/albedo/normal/radiance_m2 to device addresses."""
-        ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height,
-                          N.RENDER_WANT_BATCH_M2 if want_m2 else 0)
+               outputs: dict | None = None, profile: bool = False,
+               host_outputs: dict | None = None) -> RenderResult | None:
+        """Renders into new host arrays, into caller-provided host arrays
+        (`host_outputs`), or into device pointers when `outputs` maps
+        radiance/albedo/normal/radiance_m2 to device addresses."""
+        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_PROFILE_KERNELS if profile else 0)
+        ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
+        if host_outputs is not None:
+            o = N.Outputs(host_outputs.get("radiance"), host_outputs.get("albedo"), host_outputs.get("normal"),
+                          host_outputs.get("radiance_m2"), 0)
+            self.ctx.check(self.ctx.lib.vvpt_render(self.ctx.handle, self.handle, C.byref(scene_data), C.byref(ri),
+                                                    C.byref(o)))
+            return None
         if outputs is not None:
             o = N.Outputs(outputs.get("radiance"), outputs.get("albedo"), outputs.get("normal"),
                           outputs.get("radiance_m2"), 1)
