@@ -343,6 +343,13 @@ bool wtest(const WRay &r, const Tri &tr, float tmin, float tmax, float &t, float
     return true;
 }
 
+// Culling margins: a node is kept unless its entry lies clearly beyond the
+// best hit (relative slack 1e-5), so rounding in the slab and triangle
+// distances never drops a candidate, in particular equal-t ties on coplanar
+// geometry that the (instance, primitive) order must see.
+inline float cull_far(float best_t) { return best_t * (1.0f + 1e-5f) + 1e-30f; }
+inline float cull_near(float tmin) { return tmin - std::fabs(tmin) * 1e-5f; }
+
 // box test widened generously: culling only needs to be conservative
 inline bool box_hit(const Node &n, V3 o, V3 inv, float tmin, float tmax)
 {
@@ -375,13 +382,13 @@ void trace_mesh(const Scene &s, uint32_t inst_id, V3 o, V3 d, float tmin, const 
     V3 od = xvector(in.w2o, d);
     V3 inv = {1.0f / od.x, 1.0f / od.y, 1.0f / od.z};
     WRay wr = wsetup(oo, od);
-    float box_tmin = after.inst == NOHIT ? tmin : std::max(tmin, after.t);
+    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t));
     int stack[128];
     int sp = 0;
     stack[sp++] = 0;
     while (sp) {
         const Node &n = m.bvh.nodes[stack[--sp]];
-        if (!box_hit(n, oo, inv, box_tmin, best.t))
+        if (!box_hit(n, oo, inv, box_tmin, cull_far(best.t)))
             continue;
         if (n.left < 0) {
             for (int k = n.first; k < n.first + n.count; k++) {
@@ -415,10 +422,10 @@ Hit trace_after(const Scene &s, V3 o, V3 d, float tmin, float tmax, const Hit &a
     int stack[128];
     int sp = 0;
     stack[sp++] = 0;
-    float box_tmin = after.inst == NOHIT ? tmin : std::max(tmin, after.t);
+    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t));
     while (sp) {
         const Node &n = s.tlas.nodes[stack[--sp]];
-        if (!box_hit(n, o, inv, box_tmin, best.t))
+        if (!box_hit(n, o, inv, box_tmin, cull_far(best.t)))
             continue;
         if (n.left < 0) {
             for (int k = n.first; k < n.first + n.count; k++)

@@ -469,7 +469,7 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
                 for (int a = 0; a < 3; a++) {
                     // widen by a few ulps: the box must contain every
                     // object-space hit mapped back to world space
-                    double pad = 1e-6 * (std::fabs(q[a]) + 1.0);
+                    double pad = 1e-5 * (std::fabs(q[a]) + 1.0);
                     w.lo[a] = std::min(w.lo[a], (float)(q[a] - pad));
                     w.hi[a] = std::max(w.hi[a], (float)(q[a] + pad));
                 }

@@ -149,6 +149,15 @@ __device__ __forceinline__ void box2(const BVHNode &n, const float3 &o, const fl
     tr = (rnear <= rfar && n.rxy.x <= n.rxy.y) ? rnear : __int_as_float(0x7f800000);
 }
 
+// Culling bounds with slack. A node is skipped when its entry distance lies
+// beyond the current best hit. The slab distances and the triangle test's t
+// carry independent rounding errors of a few ulps, so for a triangle on a
+// node's face (coplanar geometry, axis-aligned walls) the computed entry can
+// exceed the computed hit t; a relative margin of 1e-5 keeps such nodes (and
+// equal-t ties, which the (instance, primitive) order resolves) in the search.
+__device__ __forceinline__ float cull_far(float best_t) { return best_t * (1.0f + 1e-5f) + 1e-30f; }
+__device__ __forceinline__ float cull_near(float tmin) { return tmin - fabsf(tmin) * 1e-5f; }
+
 __device__ __forceinline__ BVHNode load_node(const BVHNode *nodes, int idx)
 {
     const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
@@ -193,22 +202,22 @@ __device__ __forceinline__ bool traverse_blas(const SceneView &s, const DevInsta
     const WatertightRay wr = wt_setup(o, d);
     const BVHNode *nodes = s.nodes + inst.node_offset;
     const TriVerts *tris = s.tris + inst.tri_offset;
-    const float box_tmin = after.inst == kNoHit ? tmin : fmaxf(tmin, after.t);
+    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t));
     int stack[kBlasStack];
     int sp = 0;
     int node = 0;
     for (;;) {
         BVHNode n = load_node(nodes, node);
         float tl, tr;
-        box2(n, o, invd, box_tmin, best.t, tl, tr);
+        box2(n, o, invd, box_tmin, cull_far(best.t), tl, tr);
         int next = -1;
         // leaves are intersected right away; internal children are descended
         // nearest first
         int push[2];
         float pusht[2];
         int np = 0;
-        const bool hl = tl <= best.t * 1.0000005f && n.c.x >= 0;
-        const bool hr = tr <= best.t * 1.0000005f && n.c.y >= 0;
+        const bool hl = tl <= cull_far(best.t) && n.c.x >= 0;
+        const bool hr = tr <= cull_far(best.t) && n.c.y >= 0;
         if (hl) {
             if (n.c.z > 0) {
                 for (int k = n.c.x; k < n.c.x + n.c.z; k++) {
@@ -283,19 +292,19 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     best.prim = kNoHit;
     const float3 invd = safe_inv(d);
     const BVHNode *nodes = s.nodes + s.tlas_root;
-    const float box_tmin = after.inst == kNoHit ? tmin : fmaxf(tmin, after.t);
+    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t));
     int stack[kTlasStack];
     int sp = 0;
     int node = 0;
     for (;;) {
         BVHNode n = load_node(nodes, node);
         float tl, tr;
-        box2(n, o, invd, box_tmin, best.t, tl, tr);
+        box2(n, o, invd, box_tmin, cull_far(best.t), tl, tr);
         int push[2];
         float pusht[2];
         int np = 0;
-        const bool hl = tl <= best.t * 1.0000005f && n.c.x >= 0;
-        const bool hr = tr <= best.t * 1.0000005f && n.c.y >= 0;
+        const bool hl = tl <= cull_far(best.t) && n.c.x >= 0;
+        const bool hr = tr <= cull_far(best.t) && n.c.y >= 0;
 #pragma unroll
         for (int side = 0; side < 2; side++) {
             const bool h = side == 0 ? hl : hr;
