@@ -753,7 +753,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         ps.sample = (uint32_t *)take(u4);
         take(u4);
 
-        size_t qneed = 8 * aligned(u4) + aligned(C_COUNT * sizeof(uint32_t));
+        size_t qneed = 10 * aligned(u4) + aligned(C_COUNT * sizeof(uint32_t));
         VV_CUDA(ctx->queues.reserve(qneed), "cudaMalloc queues");
         base = ctx->queues.as<char>();
         Queues q;
@@ -763,6 +763,8 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         q.shade_p = (uint32_t *)take(u4);
         q.shade_m = (uint32_t *)take(u4);
         q.conn = (uint32_t *)take(u4);
+        q.ext_key = (uint32_t *)take(u4);
+        q.walk = (uint32_t *)take(u4);
         q.regen[0] = (uint32_t *)take(u4);
         q.regen[1] = (uint32_t *)take(u4);
         q.counters = (uint32_t *)take(C_COUNT * sizeof(uint32_t));
@@ -806,8 +808,10 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
 
         if (info->flags & VVPT_RENDER_PROFILE_KERNELS) {
             // one kernel at a time with events around each launch
-            static const char *names[K_NUM] = {"k_begin", "k_regen", "k_extend", "k_shade", "k_connect"};
-            static const double bpu[K_NUM] = {0.0, kBytesRegen, kBytesExtend, kBytesShade, kBytesConnect};
+            static const char *names[K_NUM] = {"k_begin", "k_regen",  "k_extend", "k_partition",
+                                               "k_walk",  "k_shade", "k_shadow", "k_emitter"};
+            static const double bpu[K_NUM] = {0.0,        kBytesRegen, kBytesExtend, kBytesPartition,
+                                              kBytesWalk, kBytesShade, kBytesShadow, kBytesEmitter};
             vvpt_kernel_profile prof{};
             prof.count = K_NUM;
             for (int k = 0; k < K_NUM; k++) {
@@ -828,9 +832,10 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "profile sync");
                     const uint32_t *c = ctx->counters_pinned;
                     uint64_t units = k == K_REGEN    ? c[C_REGEN0 + pp]
-                                     : k == K_EXTEND ? c[C_EXT0 + pp]
+                                     : (k == K_EXTEND || k == K_PARTITION) ? c[C_EXT0 + pp]
+                                     : k == K_WALK   ? c[C_WALK]
                                      : k == K_SHADE  ? (uint64_t)c[C_SHADE_L] + c[C_SHADE_P] + c[C_SHADE_M]
-                                     : k == K_CONNECT ? c[C_CONN]
+                                     : (k == K_SHADOW || k == K_EMITTER) ? c[C_CONN]
                                                       : 1;
                     cudaEventRecord(ka, vv_stream(ctx));
                     launch_kernel((KernelId)k, scene->view, dparams, ps, q, br, pp, shape, vv_stream(ctx));

@@ -20,7 +20,9 @@ constexpr uint32_t F_INSIDE = 1u;       // rayPayloadPrimary.insideVolume
 constexpr uint32_t F_DONE = 2u;         // sample finished, finalize in regen
 constexpr uint32_t F_ITEM = 4u;         // slot holds a work item
 constexpr uint32_t F_SHADOW = 8u;       // pending shadow connection
-constexpr uint32_t F_NEE = 16u;         // pending emitter connection
+constexpr uint32_t F_NEE = 16u;         // pending emitter connection (path ends at this event)
+constexpr uint32_t F_NEE_FUSED = 32u;   // emitter ray rides on the next extension ray
+constexpr uint32_t F_NEE_FULL = 64u;    // ... but needs the full candidate walk (set by extend)
 constexpr int kDepthShift = 8;          // recursionDepth d
 constexpr int kSurfShift = 16;          // surfaceDepth
 constexpr uint32_t kByteMask = 0xFFu;
@@ -256,6 +258,7 @@ __global__ void k_begin(Queues q, int pp)
         q.counters[C_SHADE_L] = 0u;
         q.counters[C_SHADE_P] = 0u;
         q.counters[C_SHADE_M] = 0u;
+        q.counters[C_WALK] = 0u;
         q.counters[C_CONN] = 0u;
         q.counters[C_EXT0 + (1 - pp)] = 0u;
         q.counters[C_REGEN0 + (1 - pp)] = 0u;
@@ -387,35 +390,98 @@ __global__ void __launch_bounds__(256) k_extend(SceneView s, PathState ps, Queue
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
     uint32_t err = 0;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        uint32_t slot = 0;
-        int key = -1; // 0 Lambert, 1 PBR, 2 miss
-        if (i < n) {
-            slot = queue[i];
-            const float3 o = f3(ps.o[slot]);
-            const float3 d = f3(ps.d[slot]);
-            Hit h = trace_closest(s, o, d, kExtTmin, kExtTmax, err);
-            ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-            ps.hit_inst[slot] = h.inst;
-            if (h.inst == kNoHit)
-                key = 2;
-            else
-                key = (uint32_t)s.materials[s.instances[h.inst].material].uv_tiling.z == 2u ? 0 : 1;
+    // Lanes run independently: a lane takes its next ray as soon as its
+    // current one is done, so a warp is never held by its slowest ray. The
+    // shade bin is written per queue entry and compacted by k_partition.
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = queue[i];
+        const float3 o = f3(ps.o[slot]);
+        const float3 d = f3(ps.d[slot]);
+        const uint32_t flags = ps.flags[slot];
+        // with an emitter ray riding on this ray, start at its tmin
+        const bool fused = (flags & F_NEE_FUSED) != 0;
+        Hit h = trace_closest(s, o, d, fused ? kConnTmin : kExtTmin, kExtTmax, err);
+        uint32_t key = 0;
+        if (fused && h.inst != kNoHit && h.t < kExtTmin) {
+            // the emitter ray's first candidate lies below the extension
+            // ray's tmin: the emitter ray takes the full candidate walk
+            key = 4;
+            h = trace_closest(s, o, d, kExtTmin, kExtTmax, err);
         }
-        // material-sorted shade queues
-        uint32_t pos = warp_append_all(key == 0, &q.counters[C_SHADE_L]);
-        if (key == 0)
-            q.shade_l[pos] = slot;
-        pos = warp_append_all(key == 1, &q.counters[C_SHADE_P]);
-        if (key == 1)
-            q.shade_p[pos] = slot;
-        pos = warp_append_all(key == 2, &q.counters[C_SHADE_M]);
-        if (key == 2)
-            q.shade_m[pos] = slot;
+        ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+        ps.hit_inst[slot] = h.inst;
+        if (h.inst == kNoHit) {
+            key |= 2;
+        } else {
+            const DevMaterial &m = s.materials[s.instances[h.inst].material];
+            key |= (uint32_t)m.uv_tiling.z == 2u ? 0u : 1u;
+            // a transparent first candidate also needs the walk
+            if (fused && h.t <= kExtTmax && m.mrao.w >= 0.99f)
+                key |= 4;
+        }
+        q.ext_key[i] = key;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
         atomicAdd(&q.counters[C_SEGMENTS], n);
+    if (err)
+        atomicOr(&q.counters[C_ERR], err);
+}
+
+// Compacts the extension queue into the material-sorted shade queues and the
+// emitter-walk queue (warp-uniform loop; uniform, cheap work per entry).
+__global__ void __launch_bounds__(256) k_partition(PathState ps, Queues q, int pp)
+{
+    const uint32_t n = q.counters[C_EXT0 + pp];
+    const uint32_t *queue = q.ext[pp];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t slot = 0, key = 0xFFu;
+        if (i < n) {
+            slot = queue[i];
+            key = q.ext_key[i];
+        }
+        const uint32_t bin = key & 3u;
+        uint32_t pos = warp_append_all(bin == 0, &q.counters[C_SHADE_L]);
+        if (bin == 0)
+            q.shade_l[pos] = slot;
+        pos = warp_append_all(bin == 1, &q.counters[C_SHADE_P]);
+        if (bin == 1)
+            q.shade_p[pos] = slot;
+        pos = warp_append_all(bin == 2, &q.counters[C_SHADE_M]);
+        if (bin == 2)
+            q.shade_m[pos] = slot;
+        const bool walk = key != 0xFFu && (key & 4u);
+        pos = warp_append_all(walk, &q.counters[C_WALK]);
+        if (walk)
+            q.walk[pos] = slot;
+    }
+}
+
+__device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir,
+                                         bool inside, uint32_t vol, float3 &out_em_T, float3 &out_T, float3 &out_em,
+                                         float &out_pdf, uint32_t &err);
+
+// The pending emitter rays whose first candidate is transparent (or below the
+// extension ray's tmin): the full candidate walk, before shade adds this
+// iteration's contributions.
+__global__ void __launch_bounds__(256) k_walk(SceneView s, const RenderParams *__restrict__ pp_, PathState ps, Queues q)
+{
+    const RenderParams &p = *pp_;
+    const uint32_t n = q.counters[C_WALK];
+    uint32_t err = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = q.walk[i];
+        const uint32_t flags = ps.flags[slot];
+        const float4 nb = ps.nee_b[slot];
+        float3 emT, T, em;
+        float lpdf;
+        emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf, err);
+        if (!is_black(em))
+            ps.rad[slot] = f4(f3(ps.rad[slot]) + power_heuristic(nb.w, lpdf) * T * em * f3(nb), 0.0f);
+        ps.flags[slot] = flags & ~(F_NEE_FUSED | F_NEE_FULL);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n)
+        atomicAdd(&q.counters[C_NEE], n);
     if (err)
         atomicOr(&q.counters[C_ERR], err);
 }
@@ -451,6 +517,10 @@ __device__ __forceinline__ bool medium_event(const SceneView &s, uint32_t vol, f
     return sampled;
 }
 
+__device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams &p, bool full, bool is_hit,
+                                         uint32_t inst_id, float4 hv, float3 o, float3 dir, bool inside, uint32_t vol,
+                                         float4 nb, uint32_t &err, uint32_t &walks);
+
 // One shading event per queued path: the body of rayPrimary*.rchit.glsl:45-175
 // (hits) or rayPrimary.rmiss.glsl:40-106 (misses), followed by Russian
 // roulette (russian_roulette.glsl:1-11).
@@ -460,6 +530,7 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
     const RenderParams &p = *pp_;
     const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
     const uint32_t n = nl + np + nm;
+    uint32_t err = 0, walks = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         uint32_t slot = 0;
@@ -485,6 +556,13 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
         const float4 hv = ps.hit[slot];
         const uint32_t inst_id = ps.hit_inst[slot];
         const bool is_hit = inst_id != kNoHit;
+
+        // the previous event's emitter ray, added before this event's own
+        // contributions (next_event_estimation.glsl:28-32 runs inside the
+        // previous hit shader)
+        if (flags & F_NEE_FUSED)
+            rad += fused_nee(s, p, (flags & F_NEE_FULL) != 0, is_hit, inst_id, hv, origin, dir, inside, vol,
+                             ps.nee_b[slot], err, walks);
 
         bool stop = false;
         bool terminal_no_rr = false; // returns before the RR block
@@ -691,8 +769,11 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
             nf |= F_DONE;
         if (has_shadow)
             nf |= F_SHADOW;
+        // a continuing path's emitter ray shares origin and direction with its
+        // next extension ray and is resolved from that traversal
+        const bool fuse = has_nee && !done && p.zfar <= kExtTmax;
         if (has_nee)
-            nf |= F_NEE;
+            nf |= fuse ? F_NEE_FUSED : F_NEE;
         ps.flags[slot] = nf;
         ps.rng[slot] = rng;
         ps.beta[slot] = f4(beta, 0.0f);
@@ -710,7 +791,7 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
         }
         if (has_nee)
             ps.nee_b[slot] = f4(nee_beta, nee_pdf);
-        want_conn = has_shadow || has_nee;
+        want_conn = has_shadow || (has_nee && !fuse);
         want_done = done;
         want_ext = !done;
         }
@@ -724,6 +805,10 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
         if (want_ext)
             q.ext[1 - pp][pos] = slot;
     }
+    if (walks)
+        atomicAdd(&q.counters[C_NEE], walks);
+    if (err)
+        atomicOr(&q.counters[C_ERR], err);
 }
 
 // Shadow ray with transparent surfaces and media (lightSampling.glsl:108-144,
@@ -825,10 +910,54 @@ __device__ float3 shadow_transmittance(const SceneView &s, const RenderParams &p
     return T;
 }
 
+// An emitter reached by the BSDF-direction ray (rayNEE.rahit.glsl:73-131):
+// medium transmittance up to the hit, back-face rejection, and the light pdf
+// of having sampled that point, with the squared distance measured from the
+// object-space ray origin as the reference does (rayNEE.rahit.glsl:122).
+__device__ __forceinline__ void emitter_eval(const SceneView &s, const RenderParams &p, const DevInstance &inst,
+                                             const ShadeVertex &a, const ShadeVertex &b, const ShadeVertex &c,
+                                             const Hit &h, const float3 &e, const float3 &o, const float3 &dir,
+                                             bool inside, uint32_t vol, float vtmin, float3 &T, float3 &em, float &pdf)
+{
+    if (inside && vol < s.num_materials) {
+        T *= medium_transmittance(s, vol, vtmin, h.t);
+        if (max3f(T) < kEps) {
+            T = f3(0.0f);
+            em = f3(0.0f);
+            return;
+        }
+    }
+    const float bx = 1.0f - h.u - h.v;
+    Affine34 w2o = rows_of(inst.w2o), o2w = rows_of(inst.o2w);
+    float3 ln = f3(a.nrm_v) * bx + f3(b.nrm_v) * h.u + f3(c.nrm_v) * h.v;
+    float3 wn = normalize3(xform_normal_transposed(w2o, ln));
+    if (dot3(wn, dir) > 0.0f) { // back face
+        em = f3(0.0f);
+        T = f3(0.0f);
+        return;
+    }
+    em = e;
+    float3 lp = f3(a.pos_u) * bx + f3(b.pos_u) * h.u + f3(c.pos_u) * h.v;
+    float3 wp = xform_point(o2w, lp);
+    float3 p0 = xform_point(o2w, f3(a.pos_u)), p1 = xform_point(o2w, f3(b.pos_u)), p2 = xform_point(o2w, f3(c.pos_u));
+    float area = 0.5f * length3(cross3(p1 - p0, p2 - p0));
+    float point_pdf = (1.0f / (float)inst.num_triangles) * (1.0f / area);
+    float dp = dot3(-dir, wn);
+    if (dp > 0.0f) {
+        float3 obj_o = xform_point(w2o, o);
+        float dist = length3(obj_o - wp);
+        float light_pdf = point_pdf * (dist * dist) / dp;
+        pdf = light_pdf * (1.0f / (float)p.num_lights);
+    } else {
+        pdf = 0.0f;
+        em = f3(0.0f);
+    }
+}
+
 // BSDF-direction emitter ray (next_event_estimation.glsl:1-33,
 // rayNEE.rahit.glsl:32-132, rayNEE.rchit.glsl:33-82, rayNEE.rmiss.glsl:12-19).
 // Returns the emitter radiance times throughput and its light pdf.
-__device__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir, bool inside,
+__device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir, bool inside,
                             uint32_t vol, float3 &out_em_T, float3 &out_T, float3 &out_em, float &out_pdf, uint32_t &err)
 {
     const float tmin = kConnTmin;
@@ -889,40 +1018,7 @@ __device__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o,
             stop = true;
             accepted = true;
             acc = h;
-            if (inside && vol < s.num_materials) {
-                T *= medium_transmittance(s, vol, vtmin, h.t);
-                if (max3f(T) < kEps) {
-                    T = f3(0.0f);
-                    em = f3(0.0f);
-                    break;
-                }
-            }
-            Affine34 w2o = rows_of(inst.w2o), o2w = rows_of(inst.o2w);
-            float3 ln = f3(a.nrm_v) * bx + f3(b.nrm_v) * h.u + f3(c.nrm_v) * h.v;
-            float3 wn = normalize3(xform_normal_transposed(w2o, ln));
-            bool flipped = dot3(wn, dir) > 0.0f;
-            if (flipped) {
-                em = f3(0.0f);
-                T = f3(0.0f);
-                break;
-            }
-            em = e;
-            float3 lp = f3(a.pos_u) * bx + f3(b.pos_u) * h.u + f3(c.pos_u) * h.v;
-            float3 wp = xform_point(o2w, lp);
-            float3 p0 = xform_point(o2w, f3(a.pos_u)), p1 = xform_point(o2w, f3(b.pos_u)), p2 = xform_point(o2w, f3(c.pos_u));
-            float area = 0.5f * length3(cross3(p1 - p0, p2 - p0));
-            float point_pdf = (1.0f / (float)inst.num_triangles) * (1.0f / area);
-            float dp = dot3(-dir, wn);
-            if (dp > 0.0f) {
-                // distance from the object-space ray origin, as rayNEE.rahit.glsl:122
-                float3 obj_o = xform_point(w2o, o);
-                float dist = length3(obj_o - wp);
-                float light_pdf = point_pdf * (dist * dist) / dp;
-                pdf = light_pdf * (1.0f / (float)p.num_lights);
-            } else {
-                pdf = 0.0f;
-                em = f3(0.0f);
-            }
+            emitter_eval(s, p, inst, a, b, c, h, e, o, dir, inside, vol, vtmin, T, em, pdf);
             break;
         }
         if (!accepted) {
@@ -961,44 +1057,102 @@ __device__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o,
     out_em_T = T * em;
 }
 
-__global__ void __launch_bounds__(256) k_connect(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
+// The previous event's BSDF-direction emitter ray, resolved from this
+// iteration's extension hit: the two rays share origin and direction, and the
+// extension traversal starts at the emitter ray's tmin (1e-4) when one is
+// pending, so the extension hit is the emitter ray's first candidate unless
+// extend flagged a candidate below 1e-3 (`full`). Candidates beyond zfar are a
+// miss for the emitter ray; a transparent first candidate needs the complete
+// candidate walk of emitter_ray.
+__device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams &p, bool full, bool is_hit,
+                                         uint32_t inst_id, float4 hv, float3 o, float3 dir, bool inside, uint32_t vol,
+                                         float4 nb, uint32_t &err, uint32_t &walks)
+{
+    float3 T = f3(1.0f), em = f3(0.0f);
+    float pdf = 0.0f;
+    if (!full && is_hit && hv.x <= p.zfar) {
+        Hit h;
+        h.t = hv.x;
+        h.u = hv.y;
+        h.v = hv.z;
+        h.inst = inst_id;
+        h.prim = __float_as_uint(hv.w);
+        const DevInstance &inst = s.instances[inst_id];
+        const DevMaterial &m = s.materials[inst.material];
+        ShadeVertex a, b, c;
+        fetch_triangle(s, inst, h.prim, a, b, c);
+        const float bx = 1.0f - h.u - h.v;
+        float2 uv = make_float2(a.pos_u.w * bx + b.pos_u.w * h.u + c.pos_u.w * h.v,
+                                a.nrm_v.w * bx + b.nrm_v.w * h.u + c.nrm_v.w * h.v);
+        float2 tuv = make_float2(uv.x * m.uv_tiling.x, uv.y * m.uv_tiling.y);
+        float3 e = material_emissive(s, m, tuv);
+        if (is_black_eps(e, 0.05f)) {
+            if (m.mrao.w >= 0.99f)
+                full = true; // transparent: walk the candidates
+        } else {
+            emitter_eval(s, p, inst, a, b, c, h, e, o, dir, inside, vol, kConnTmin, T, em, pdf);
+        }
+    }
+    if (full) {
+        float3 emT;
+        emitter_ray(s, p, o, dir, inside, vol, emT, T, em, pdf, err);
+        walks++;
+    }
+    if (is_black(em))
+        return f3(0.0f);
+    return power_heuristic(nb.w, pdf) * T * em * f3(nb);
+}
+
+// Shadow rays of the events shaded this iteration.
+__global__ void __launch_bounds__(256) k_shadow(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
+                                                Queues q)
+{
+    const RenderParams &p = *pp_;
+    const uint32_t n = q.counters[C_CONN];
+    uint32_t err = 0;
+    uint32_t nsh = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = q.conn[i];
+        const uint32_t flags = ps.flags[slot];
+        if (!(flags & F_SHADOW))
+            continue;
+        const float4 sd = ps.sh_dir[slot];
+        const float3 T = shadow_transmittance(s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
+                                              ps.vol[slot], err);
+        if (!is_black(T))
+            ps.rad[slot] = f4(f3(ps.rad[slot]) + f3(ps.sh_c[slot]) * T, 0.0f);
+        ps.flags[slot] = flags & ~F_SHADOW;
+        nsh++;
+    }
+    if (nsh)
+        atomicAdd(&q.counters[C_SHADOW], nsh);
+    if (err)
+        atomicOr(&q.counters[C_ERR], err);
+}
+
+// BSDF-direction emitter rays of paths that end at this event (their next
+// extension ray is never traced, so the emitter ray cannot ride on it).
+__global__ void __launch_bounds__(256) k_emitter(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
                                                  Queues q)
 {
     const RenderParams &p = *pp_;
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
-    uint32_t nsh = 0, nnee = 0;
+    uint32_t nnee = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = q.conn[i];
         const uint32_t flags = ps.flags[slot];
-        const bool inside = (flags & F_INSIDE) != 0;
-        const uint32_t vol = ps.vol[slot];
-        const float3 o = f3(ps.o[slot]);
-        float3 rad = f3(ps.rad[slot]);
-        if (flags & F_SHADOW) {
-            float4 sd = ps.sh_dir[slot];
-            float3 c = f3(ps.sh_c[slot]);
-            float3 T = shadow_transmittance(s, p, o, f3(sd), sd.w, inside, vol, err);
-            if (!is_black(T))
-                rad += c * T;
-            nsh++;
-        }
-        if (flags & F_NEE) {
-            float4 nb = ps.nee_b[slot];
-            float3 emT, T, em;
-            float lpdf;
-            emitter_ray(s, p, o, f3(ps.d[slot]), inside, vol, emT, T, em, lpdf, err);
-            if (!is_black(em)) {
-                float w = power_heuristic(nb.w, lpdf);
-                rad += w * T * em * f3(nb);
-            }
-            nnee++;
-        }
-        ps.rad[slot] = f4(rad, 0.0f);
-        ps.flags[slot] = flags & ~(F_SHADOW | F_NEE);
+        if (!(flags & F_NEE))
+            continue;
+        const float4 nb = ps.nee_b[slot];
+        float3 emT, T, em;
+        float lpdf;
+        emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf, err);
+        if (!is_black(em))
+            ps.rad[slot] = f4(f3(ps.rad[slot]) + power_heuristic(nb.w, lpdf) * T * em * f3(nb), 0.0f);
+        ps.flags[slot] = flags & ~F_NEE;
+        nnee++;
     }
-    if (nsh)
-        atomicAdd(&q.counters[C_SHADOW], nsh);
     if (nnee)
         atomicAdd(&q.counters[C_NEE], nnee);
     if (err)
@@ -1057,11 +1211,8 @@ void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cud
 void launch_iteration(const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
                       const BatchResults &br, int pp, const LaunchShape &shape, cudaStream_t stream)
 {
-    k_begin<<<1, 32, 0, stream>>>(q, pp);
-    k_regen<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, br, pp);
-    k_extend<<<shape.grid, shape.block, 0, stream>>>(s, ps, q, pp);
-    k_shade<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, pp);
-    k_connect<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+    for (int k = 0; k < K_NUM; k++)
+        launch_kernel((KernelId)k, s, dparams, ps, q, br, pp, shape, stream);
 }
 
 void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
@@ -1077,11 +1228,20 @@ void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, 
     case K_EXTEND:
         k_extend<<<shape.grid, shape.block, 0, stream>>>(s, ps, q, pp);
         break;
+    case K_PARTITION:
+        k_partition<<<shape.grid, shape.block, 0, stream>>>(ps, q, pp);
+        break;
+    case K_WALK:
+        k_walk<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        break;
     case K_SHADE:
         k_shade<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, pp);
         break;
-    case K_CONNECT:
-        k_connect<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+    case K_SHADOW:
+        k_shadow<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        break;
+    case K_EMITTER:
+        k_emitter<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
         break;
     default:
         break;

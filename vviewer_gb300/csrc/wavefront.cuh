@@ -69,12 +69,15 @@ enum CounterIndex {
     C_SHADOW = 12,
     C_NEE = 13,
     C_PATHS = 14,
+    C_WALK = 15,
     C_COUNT = 16
 };
 
 struct Queues {
     uint32_t *ext[2];
+    uint32_t *ext_key;  // per extension-queue entry: shade bin (0 Lambert, 1 PBR, 2 miss) | 4 = emitter walk
     uint32_t *shade_l, *shade_p, *shade_m;
+    uint32_t *walk;     // paths whose pending emitter ray needs the full candidate walk
     uint32_t *conn;
     uint32_t *regen[2];
     uint32_t *counters; // CounterIndex
@@ -103,10 +106,20 @@ void launch_reduce(const RenderParams &hparams, const BatchResults &br, float4 *
 void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cudaStream_t stream);
 void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, float4 *hits_tuv, uint32_t *hits_ids,
                           uint32_t *err, cudaStream_t stream);
-constexpr int kKernelsPerIteration = 5;
-
-// One wavefront kernel, launched on its own (profiling mode).
-enum KernelId { K_BEGIN = 0, K_REGEN = 1, K_EXTEND = 2, K_SHADE = 3, K_CONNECT = 4, K_NUM = 5 };
+// One wavefront kernel, launched on its own (profiling mode); an iteration
+// launches all of them in this order.
+enum KernelId {
+    K_BEGIN = 0,
+    K_REGEN = 1,
+    K_EXTEND = 2,
+    K_PARTITION = 3,
+    K_WALK = 4,
+    K_SHADE = 5,
+    K_SHADOW = 6,
+    K_EMITTER = 7,
+    K_NUM = 8
+};
+constexpr int kKernelsPerIteration = K_NUM;
 void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
                    const BatchResults &br, int pingpong, const LaunchShape &shape, cudaStream_t stream);
 
@@ -115,10 +128,14 @@ void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, 
 // (nominal branch), plus the three shading vertices and their indices read by
 // shade. BVH nodes, triangles and textures are excluded.
 constexpr double kBytesRegen = 4 + 3 * 4 + 3 * sizeof(float4) + 3 * sizeof(float4) + 4 + 9 * sizeof(float4) + 5 * 4 + 4;
-constexpr double kBytesExtend = 4 + 2 * sizeof(float4) + sizeof(float4) + 4 + 4;
+constexpr double kBytesExtend = 4 + 4 /* flags */ + 2 * sizeof(float4) + sizeof(float4) + 4 + 4 /* key */;
+constexpr double kBytesPartition = 4 + 4 + 4;
+constexpr double kBytesWalk = 4 + 4 + 4 + 4 * sizeof(float4) /* o d nee_b rad */ + sizeof(float4) + 4;
 constexpr double kBytesShade = 4 + (4 + 4 + 4 + 4) + 5 * sizeof(float4) /* beta rad o d hit */ + 3 * 4 +
                                3 * sizeof(ShadeVertex) /* vertices */ + (4 + 4 + 4) + 4 * sizeof(float4) /* writes */ +
-                               5 * sizeof(float4) /* alb nrm sh_dir sh_c nee_b */ + 2 * 4;
-constexpr double kBytesConnect = 4 + 4 + 4 + 6 * sizeof(float4) /* o rad sh_dir sh_c d nee_b */ + sizeof(float4) + 4;
+                               5 * sizeof(float4) /* alb nrm sh_dir sh_c nee_b */ + sizeof(float4) /* nee_b read */ +
+                               2 * 4;
+constexpr double kBytesShadow = 4 + 4 + 4 + 4 * sizeof(float4) /* o sh_dir rad sh_c */ + sizeof(float4) + 4;
+constexpr double kBytesEmitter = 4 + 4 + 4 + 4 * sizeof(float4) /* o d nee_b rad */ + sizeof(float4) + 4;
 
 }  // namespace vvpt
