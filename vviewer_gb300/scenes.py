@@ -254,6 +254,85 @@ def displaced_sphere(freq: int, radius: float, amplitude: float, noise_scale: fl
     return indexed_mesh("displaced_sphere", pos, T, uv, nrm)
 
 
+def random_scene(seed: int, min_tris: int = 10_000, max_tris: int = 2_000_000, max_lights: int = 4) -> Engine:
+    """One scene of the batched/serving workloads: the Cornell room with
+    10k-2M triangles of displaced spheres (log-uniform count), a Lambert /
+    metallic-roughness mix, 0-4 extra mesh lights (the ceiling light stays) and
+    a homogeneous medium of density U[0, 0.3] (none below 0.01)."""
+    engine = Engine()
+    scene = _cornell_room(engine, seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    target = float(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris))))
+    n_spheres = int(rng.integers(1, 9))
+    freq = max(2, int(round(math.sqrt(target / (20.0 * n_spheres)))))
+    centers = []
+    for k in range(n_spheres):
+        r = float(rng.uniform(0.06, 0.12))
+        for _ in range(200):
+            c = rng.uniform([0.15, 0.1, 0.15], [0.85, 0.85, 0.85])
+            if all(np.linalg.norm(c - c2) > r + r2 + 0.02 for c2, r2 in centers):
+                break
+        centers.append((c, r))
+        mesh = engine.add_mesh(displaced_sphere(freq, 1.0, 0.04 / r, 4.0, rng))
+        if rng.random() < 0.5:
+            mat = engine.create_material(MaterialLambert, f"sphere_mat{k}")
+            mat.albedo = [*rng.uniform(0.1, 0.9, size=3).tolist(), 1.0]
+        else:
+            mat = engine.create_material(MaterialPBRStandard, f"sphere_mat{k}")
+            mat.albedo = [*rng.uniform(0.1, 0.9, size=3).tolist(), 1.0]
+            mat.roughness = float(rng.uniform(0.05, 1.0))
+            mat.metallic = float(rng.random() < 0.3)
+        so = scene.add_scene_object(f"sphere{k}", Transform(tuple(c), (r, r, r)))
+        so.mesh = mesh
+        so.material = mat
+    n_lights = int(rng.integers(0, max_lights + 1))
+    lq = mesh_from_triangles("light_quad", quad((-0.5, 0, -0.5), (0.5, 0, -0.5), (0.5, 0, 0.5), (-0.5, 0, 0.5)), QUAD_UV)
+    lmesh = engine.add_mesh(lq) if n_lights else None
+    for k in range(n_lights):
+        m = engine.create_material(MaterialLambert, f"extra_light{k}")
+        m.albedo = [0.8, 0.8, 0.8, 1.0]
+        m.emissive = [*rng.uniform(0.5, 1.0, size=3).tolist(), float(rng.uniform(2.0, 10.0))]
+        s = float(rng.uniform(0.08, 0.2))
+        # on the back wall, facing the room (+z)
+        p = (float(rng.uniform(0.2, 0.8)), float(rng.uniform(0.3, 0.8)), 0.002)
+        so = scene.add_scene_object(f"extra_light{k}", Transform(p, (s, s, s), (radians(90.0), 0.0, 0.0)))
+        so.mesh = lmesh
+        so.material = m
+    density = float(rng.uniform(0.0, 0.3))
+    if density >= 0.01:
+        medium = engine.create_material(MaterialVolume, "room_medium")
+        medium.sigma_a = [0.2 * density] * 3 + [0.0]
+        medium.sigma_s = [0.8 * density] * 3 + [0.0]
+        medium.g = 0.0
+        boundary_mat = engine.create_material(MaterialPBRStandard, "medium_boundary")
+        boundary_mat.albedo = [1.0, 1.0, 1.0, 0.0]
+        boundary_mat.set_transparent(True)
+        b = scene.add_scene_object("medium_boundary", Transform((0.5, 0.5, 0.5), (1.002, 1.002, 1.002)))
+        b.mesh = engine.add_mesh(unit_box())
+        b.material = boundary_mat
+        b.volume_back = medium
+    scene.background_color = [0.05, 0.05, 0.05]
+    return engine
+
+
+RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+SPPS = [16, 64, 256]
+
+
+def job_mix(seed: int, n_jobs: int, n_scenes: int) -> list[tuple[int, RenderInfo]]:
+    """(scene index, render info) per job: scene drawn from a pool of n_scenes,
+    resolution from {256^2, 512^2, 1024^2, 1920x1080}, spp from {16, 64, 256}."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    jobs = []
+    for j in range(n_jobs):
+        w, h = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
+        spp = SPPS[int(rng.integers(0, len(SPPS)))]
+        jobs.append((int(rng.integers(0, n_scenes)),
+                     RenderInfo(samples=spp, depth=8, batch_size=4, width=w, height=h, filename=f"job{j}",
+                                write_files=False)))
+    return jobs
+
+
 def cornell_medium(seed: int = 1, width: int = 1920, height: int = 1080, samples: int = 256, depth: int = 12,
                    batch_size: int = 4, freq: int = 79, spheres: int = 8) -> tuple[Engine, RenderInfo]:
     engine = Engine()
