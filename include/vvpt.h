@@ -273,6 +273,32 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx,
                                  const vvpt_scene_data *scene_data,
                                  const vvpt_render_info *info,
                                  vvpt_outputs *outputs);
+/* Render that makes no device allocations (no counterpart in the reference).
+ *
+ * For callers that cannot let a library call cudaMalloc: engines that manage
+ * a fixed device-memory pool and forbid allocations they did not make,
+ * processes under a hard memory cap, or frame loops that must not take the
+ * implicit device synchronisation of the allocator. Same result as
+ * vvpt_render (bit for bit). All scratch (parameters, counters, ray queues,
+ * path state for up to 65,536 paths in flight, per-batch sums) comes from one
+ * 64 MiB array the library defines at file scope, which every GPU that loads
+ * the library holds until the process exits. Limit: the request must fit it:
+ * width * height * (samples / batch_size) <= 999,413 work items (48 bytes
+ * each, beside 18.3 MiB of path state), e.g. 256 x 256 at 15 batches;
+ * larger requests fail with
+ * VVPT_ERR_INVALID_ARG before any GPU work. Outputs must be device buffers
+ * (outputs->on_device = 1). The scene must already be resident
+ * (vvpt_scene_upload allocates; this call does not).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. All calls in the process share the
+ * array: calls that overlap on the GPU (two contexts on one device, or two
+ * threads) race and corrupt each other's results, so serialise them. */
+VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx,
+                                         vvpt_scene *scene,
+                                         const vvpt_scene_data *scene_data,
+                                         const vvpt_render_info *info,
+                                         vvpt_outputs *outputs);
+
 /* Fraction of the current/last render done, readable from any thread
  * (RendererPathTracing::renderProgress). */
 VVPT_API vvpt_status vvpt_progress(vvpt_ctx *ctx, float *out_progress);

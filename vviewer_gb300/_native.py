@@ -146,6 +146,8 @@ _SIGNATURES = {
     "vvpt_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "vvpt_last_kernel_profile": (C.c_int, [C.c_void_p, C.POINTER(KernelProfile)]),
     "vvpt_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vvpt_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SceneData), C.POINTER(RenderInfo),
+                                      C.POINTER(Outputs)]),
 }
 
 _lib = None

@@ -1019,3 +1019,205 @@ VVPT_API vvpt_status vvpt_trace_closest(vvpt_ctx *ctx, vvpt_scene *scene, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Render without device allocations.
+//
+// Some callers cannot let a library call cudaMalloc: an engine that owns a
+// fixed device-memory pool and forbids allocations behind its back, a process
+// under a hard memory cap, or code that must not hit the allocator's implicit
+// device synchronisation in the middle of a frame. vvpt_render_noalloc renders
+// with every piece of its scratch (render parameters, counters, ray queues,
+// path state and per-batch sums) carved out of one fixed device array that the
+// library defines at file scope. The array is part of the module, so every GPU
+// that loads this library holds it until the process exits.
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 64ull << 20; // 64 MiB
+constexpr uint32_t kNoAllocMaxSlots = 65536;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The array's address on each device, looked up once per device with that
+// device current. On the host, `g_noalloc_scratch` is only a stand-in symbol,
+// never a device address: kernels receive the looked-up pointer.
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[64] = {};
+
+vvpt_status noalloc_scratch(vvpt_ctx *ctx, unsigned char **out)
+{
+    if (ctx->device < 0 || ctx->device >= 64)
+        return fail(ctx, VVPT_ERR_UNSUPPORTED, "device index beyond 63");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[ctx->device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return cuda_fail(ctx, e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(scratch)");
+        g_noalloc_ptr[ctx->device] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[ctx->device];
+    return VVPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_scene_data *sd,
+                                         const vvpt_render_info *info, vvpt_outputs *out)
+{
+    if (!ctx || !scene || !sd || !info || !out)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "null argument");
+    if (!out->on_device)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "vvpt_render_noalloc writes device buffers only (outputs.on_device = 1)");
+    if (info->width == 0 || info->height == 0 || info->batch_size == 0)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "width, height and batch_size must be positive");
+    const uint64_t npix64 = (uint64_t)info->width * info->height;
+    const uint32_t batches = info->samples / info->batch_size;
+    const uint64_t items64 = npix64 * batches;
+    const uint64_t slots64 = std::max<uint64_t>(32, std::min<uint64_t>(items64, kNoAllocMaxSlots));
+    auto aligned = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
+    const uint64_t f4 = slots64 * sizeof(float4), u4 = slots64 * sizeof(uint32_t);
+    const uint64_t need = aligned(sizeof(RenderParams)) + aligned(C_COUNT * sizeof(uint32_t)) + 14 * aligned(f4) +
+                          7 * aligned(u4) + 10 * aligned(u4) + 3 * aligned(items64 * sizeof(float4));
+    if (need > kNoAllocScratchBytes)
+        return fail(ctx, VVPT_ERR_INVALID_ARG,
+                    "render needs " + std::to_string(need) + " bytes of scratch; vvpt_render_noalloc has " +
+                        std::to_string(kNoAllocScratchBytes) + " (width * height * samples / batch_size too large)");
+
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    ctx->progress.store(0.0f);
+    unsigned char *scratch = nullptr;
+    vvpt_status st = noalloc_scratch(ctx, &scratch);
+    if (st != VVPT_OK)
+        return st;
+    cudaStream_t stream = vv_stream(ctx);
+
+    RenderParams hp{};
+    for (int c = 0; c < 4; c++) {
+        hp.view_inv[c] = make_float4(sd->view_inverse[c * 4 + 0], sd->view_inverse[c * 4 + 1],
+                                     sd->view_inverse[c * 4 + 2], sd->view_inverse[c * 4 + 3]);
+        hp.proj_inv[c] = make_float4(sd->projection_inverse[c * 4 + 0], sd->projection_inverse[c * 4 + 1],
+                                     sd->projection_inverse[c * 4 + 2], sd->projection_inverse[c * 4 + 3]);
+    }
+    hp.background = make_float3(sd->background[0], sd->background[1], sd->background[2]);
+    hp.env_type = sd->background[3];
+    hp.lens_radius = sd->exposure[2];
+    hp.focal_distance = sd->exposure[3];
+    hp.env_intensity = sd->exposure[1];
+    hp.zfar = sd->volumes[2];
+    hp.zfar_trunc = (float)(uint32_t)std::max(0.0f, sd->volumes[2]);
+    hp.cam_volume = (int32_t)sd->volumes[0];
+    if (hp.cam_volume != -1 && (hp.cam_volume < 0 || (uint32_t)hp.cam_volume >= scene->num_materials))
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "camera volume material index out of range");
+    hp.width = info->width;
+    hp.height = info->height;
+    hp.batch_size = info->batch_size;
+    hp.batches = batches;
+    hp.depth = std::min(info->depth, 255u);
+    hp.total_samples = info->batch_size * batches;
+    hp.num_lights = scene->view.num_lights;
+    hp.total_items = (uint32_t)items64;
+    hp.want_m2 = out->radiance_m2 ? 1u : 0u;
+
+    float4 *d_out[4] = {reinterpret_cast<float4 *>(out->radiance), reinterpret_cast<float4 *>(out->albedo),
+                        reinterpret_cast<float4 *>(out->normal), reinterpret_cast<float4 *>(out->radiance_m2)};
+    if (batches == 0 || hp.depth == 0) {
+        for (int k = 0; k < 4; k++)
+            if (d_out[k])
+                VV_CUDA(cudaMemsetAsync(d_out[k], 0, npix64 * sizeof(float4), stream), "clear outputs");
+        VV_CUDA(cudaStreamSynchronize(stream), "render");
+        ctx->progress.store(1.0f);
+        return VVPT_OK;
+    }
+
+    // carve the scratch array; everything below is rewritten by this call
+    // before it is read (the counters and slot queue by k_init_slots, path
+    // state by k_regen, every per-batch sum once per work item)
+    unsigned char *base = scratch;
+    auto take = [&](uint64_t b) {
+        unsigned char *p = base;
+        base += aligned(b);
+        return p;
+    };
+    RenderParams *dparams = reinterpret_cast<RenderParams *>(take(sizeof(RenderParams)));
+    Queues q;
+    q.counters = reinterpret_cast<uint32_t *>(take(C_COUNT * sizeof(uint32_t)));
+    PathState ps;
+    float4 **f4s[14] = {&ps.o, &ps.d, &ps.beta, &ps.rad, &ps.alb, &ps.nrm, &ps.cum_rad,
+                        &ps.cum_alb, &ps.cum_nrm, &ps.hit, &ps.sh_dir, &ps.sh_c, &ps.nee_b, nullptr};
+    for (float4 **p : f4s) {
+        float4 *m = reinterpret_cast<float4 *>(take(f4));
+        if (p)
+            *p = m;
+    }
+    uint32_t **u4s[7] = {&ps.hit_inst, &ps.rng, &ps.flags, &ps.vol, &ps.item, &ps.sample, nullptr};
+    for (uint32_t **p : u4s) {
+        uint32_t *m = reinterpret_cast<uint32_t *>(take(u4));
+        if (p)
+            *p = m;
+    }
+    uint32_t **qs[10] = {&q.ext[0], &q.ext[1], &q.shade_l, &q.shade_p, &q.shade_m,
+                         &q.conn,   &q.ext_key, &q.walk,  &q.regen[0], &q.regen[1]};
+    for (uint32_t **p : qs)
+        *p = reinterpret_cast<uint32_t *>(take(u4));
+    BatchResults br;
+    br.rad = reinterpret_cast<float4 *>(take(items64 * sizeof(float4)));
+    br.alb = reinterpret_cast<float4 *>(take(items64 * sizeof(float4)));
+    br.nrm = reinterpret_cast<float4 *>(take(items64 * sizeof(float4)));
+
+    VV_CUDA(cudaMemcpyAsync(dparams, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream), "upload params");
+    LaunchShape shape;
+    shape.block = 256;
+    shape.grid = std::max(1, ctx->num_sms * 4);
+    const uint32_t slots = (uint32_t)slots64;
+    launch_init_slots(q, ps, slots, stream);
+    VV_CUDA(cudaGetLastError(), "launch init");
+    const uint64_t max_iters =
+        (uint64_t)hp.batch_size * (hp.depth + 1) * ((hp.total_items + slots - 1) / slots + 1) + 64;
+    // kernels are launched one by one (no graph objects); the pinned counter
+    // buffer was allocated when the context was created
+    vvpt_render_stats stats{};
+    stats.kernel_launches = 1;
+    uint64_t it = 0;
+    for (;;) {
+        for (int k = 0; k < 8; k++) {
+            for (int kk = 0; kk < K_NUM; kk++)
+                launch_kernel((KernelId)kk, scene->view, dparams, ps, q, br, (int)(it & 1), shape, stream);
+            it++;
+        }
+        stats.kernel_launches += 8 * K_NUM;
+        VV_CUDA(cudaGetLastError(), "launch iteration");
+        VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                stream),
+                "read counters");
+        VV_CUDA(cudaStreamSynchronize(stream), "render");
+        const uint32_t *c = ctx->counters_pinned;
+        if (c[C_ERR])
+            return fail(ctx, VVPT_ERR_DEVICE, "device status word set: " + std::to_string(c[C_ERR]));
+        ctx->progress.store((float)std::min<uint32_t>(c[C_NEXT_ITEM] - std::min(c[C_NEXT_ITEM], c[C_ACTIVE]),
+                                                     hp.total_items) /
+                            (float)hp.total_items);
+        if (c[C_NEXT_ITEM] >= hp.total_items && c[C_ACTIVE] == 0)
+            break;
+        if (it > max_iters + 16)
+            return fail(ctx, VVPT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+    }
+    stats.iterations = it;
+    stats.segments = ctx->counters_pinned[C_SEGMENTS];
+    stats.shadow_rays = ctx->counters_pinned[C_SHADOW];
+    stats.emitter_rays = ctx->counters_pinned[C_NEE];
+    stats.paths = ctx->counters_pinned[C_PATHS];
+    launch_reduce(hp, br, d_out[0], d_out[1], d_out[2], d_out[3], stream);
+    stats.kernel_launches += 1;
+    VV_CUDA(cudaGetLastError(), "launch reduce");
+    VV_CUDA(cudaStreamSynchronize(stream), "render finish");
+    ctx->stats = stats;
+    ctx->progress.store(1.0f);
+    return VVPT_OK;
+}
+
+}  // extern "C"
