@@ -283,8 +283,8 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx,
  * path state for up to 65,536 paths in flight, per-batch sums) comes from one
  * 64 MiB array the library defines at file scope, which every GPU that loads
  * the library holds until the process exits. Limit: the request must fit it:
- * width * height * (samples / batch_size) <= 999,413 work items (48 bytes
- * each, beside 18.3 MiB of path state), e.g. 256 x 256 at 15 batches;
+ * width * height * (samples / batch_size) <= 993,936 work items (48 bytes
+ * each, beside 18.5 MiB of path state), e.g. 256 x 256 at 15 batches;
  * larger requests fail with
  * VVPT_ERR_INVALID_ARG before any GPU work. Outputs must be device buffers
  * (outputs->on_device = 1). The scene must already be resident
@@ -358,6 +358,83 @@ typedef struct vvpt_tuning {
 } vvpt_tuning;
 VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *tuning);
 VVPT_API vvpt_status vvpt_get_tuning(vvpt_ctx *ctx, vvpt_tuning *out_tuning);
+
+/* ---- Jobs: batched and served renders ------------------------------------
+ *
+ * No counterpart in the reference, whose render() is synchronous and
+ * non-reentrant (VulkanRendererPathTracing.cpp:121-226). A submitted job is
+ * the same request as vvpt_render; the context's engine thread runs all
+ * admitted jobs together, with the work items of every job in one hand-out
+ * sequence and one queue per wavefront stage, so small jobs fill the GPU
+ * beside large ones. A job's images are bit-identical to vvpt_render of the
+ * same request (its RNG streams depend only on pixel and batch). Admission is
+ * first come first served, bounded by the device budget.
+ *
+ * Thread-safe: submit, poll, wait and release may be called from any thread.
+ * The scene must stay resident until its jobs have finished
+ * (vvpt_scene_release returns VVPT_ERR_NOT_READY while they run). Output
+ * buffers must stay valid until the job is done; host outputs are written
+ * by the engine's completion thread. */
+typedef uint64_t vvpt_job;
+
+typedef enum vvpt_job_state {
+    VVPT_JOB_QUEUED = 0,  /* submitted, waiting for admission */
+    VVPT_JOB_RUNNING = 1, /* admitted: its work items are being traced */
+    VVPT_JOB_DONE = 2,    /* outputs written */
+    VVPT_JOB_FAILED = 3   /* see status */
+} vvpt_job_state;
+
+typedef struct vvpt_job_info {
+    uint32_t state;       /* vvpt_job_state */
+    int32_t status;       /* vvpt_status of a failed job, else VVPT_OK */
+    double submit_ms;     /* host steady clock, ms since the context was created */
+    double start_ms;      /* admission */
+    double end_ms;        /* outputs written */
+    uint64_t paths;       /* width * height * (samples / batch_size) * batch_size */
+    uint64_t device_bytes; /* engine memory the job holds while admitted */
+} vvpt_job_info;
+
+/* Queues one render. `outputs` is copied; its buffers (host or device) are
+ * written when the job completes. Fails with VVPT_ERR_BUDGET_EXCEEDED if the
+ * job alone could never fit the budget. */
+VVPT_API vvpt_status vvpt_submit(vvpt_ctx *ctx,
+                                 vvpt_scene *scene,
+                                 const vvpt_scene_data *scene_data,
+                                 const vvpt_render_info *info,
+                                 const vvpt_outputs *outputs,
+                                 vvpt_job *out_job);
+/* Non-blocking state of a job. */
+VVPT_API vvpt_status vvpt_poll(vvpt_ctx *ctx, vvpt_job job, vvpt_job_info *out_info);
+/* Blocks until the job is done (VVPT_OK), failed (its status) or
+ * `timeout_ms` passed (VVPT_ERR_TIMEOUT; the job keeps running). A negative
+ * timeout waits without limit. */
+VVPT_API vvpt_status vvpt_wait(vvpt_ctx *ctx, vvpt_job job, double timeout_ms);
+/* Forgets a finished job's record (VVPT_ERR_NOT_READY while it runs). */
+VVPT_API vvpt_status vvpt_job_release(vvpt_ctx *ctx, vvpt_job job);
+/* Device-memory budget of the engine in bytes (path state, queues, per-job
+ * batch sums and output staging); 0 = no limit but the device's memory.
+ * Applies to admissions after the call. */
+VVPT_API vvpt_status vvpt_set_budget(vvpt_ctx *ctx, uint64_t bytes);
+/* Engine occupancy: its fixed pool (path slots, queues, job table), the
+ * memory admitted jobs hold, and job counts by state (records not yet
+ * released). Starts the engine if it is not running. */
+typedef struct vvpt_engine_stats {
+    uint64_t fixed_bytes;
+    uint64_t job_bytes;
+    uint32_t queued;
+    uint32_t running;
+    uint32_t finished;
+    uint32_t slots;
+} vvpt_engine_stats;
+VVPT_API vvpt_status vvpt_engine_stats_get(vvpt_ctx *ctx, vvpt_engine_stats *out_stats);
+/* Renders n requests together through the engine and waits for all of them;
+ * returns the first failure. Each output equals vvpt_render's. */
+VVPT_API vvpt_status vvpt_render_batch(vvpt_ctx *ctx,
+                                       uint32_t n,
+                                       vvpt_scene *const *scenes,
+                                       const vvpt_scene_data *scene_data,
+                                       const vvpt_render_info *infos,
+                                       const vvpt_outputs *outputs);
 
 #ifdef __cplusplus
 }

@@ -257,6 +257,7 @@ struct Scene {
     const vvpt_light_data *ldata = nullptr;
     std::vector<Tex> tex;
     int env = -1;
+    float cull_o = 0.0f, cull_r = 0.0f;
 };
 
 // ------------------------------------------------------------------ closest hit
@@ -344,11 +345,15 @@ bool wtest(const WRay &r, const Tri &tr, float tmin, float tmax, float &t, float
 }
 
 // Culling margins: a node is kept unless its entry lies clearly beyond the
-// best hit (relative slack 1e-5), so rounding in the slab and triangle
-// distances never drops a candidate, in particular equal-t ties on coplanar
-// geometry that the (instance, primitive) order must see.
-inline float cull_far(float best_t) { return best_t * (1.0f + 1e-5f) + 1e-30f; }
-inline float cull_near(float tmin) { return tmin - std::fabs(tmin) * 1e-5f; }
+// best hit, so rounding in the slab and triangle distances never drops a
+// candidate, in particular equal-t ties on coplanar geometry that the
+// (instance, primitive) order must see. Relative slack 1e-5, plus an absolute
+// one per ray for hits near the origin, where the triangle's t carries an
+// error of about epsilon times the object-space coordinates over |d|:
+// 1e-5 * (cull_o * |o| + cull_r) / |d| (max-norms; cull_o, cull_r bound the
+// object-space coordinate growth over the TLAS instances).
+inline float cull_far(float best_t, float slack) { return best_t * (1.0f + 1e-5f) + slack + 1e-30f; }
+inline float cull_near(float tmin, float slack) { return tmin - std::fabs(tmin) * 1e-5f - slack; }
 
 // box test widened generously: culling only needs to be conservative
 inline bool box_hit(const Node &n, V3 o, V3 inv, float tmin, float tmax)
@@ -371,7 +376,7 @@ inline bool box_hit(const Node &n, V3 o, V3 inv, float tmin, float tmax)
     return true;
 }
 
-void trace_mesh(const Scene &s, uint32_t inst_id, V3 o, V3 d, float tmin, const Hit &after, Hit &best)
+void trace_mesh(const Scene &s, uint32_t inst_id, V3 o, V3 d, float tmin, float slack, const Hit &after, Hit &best)
 {
     const Inst &in = s.inst[inst_id];
     const Mesh &m = s.meshes[in.mesh];
@@ -382,13 +387,13 @@ void trace_mesh(const Scene &s, uint32_t inst_id, V3 o, V3 d, float tmin, const 
     V3 od = xvector(in.w2o, d);
     V3 inv = {1.0f / od.x, 1.0f / od.y, 1.0f / od.z};
     WRay wr = wsetup(oo, od);
-    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t));
+    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t), slack);
     int stack[128];
     int sp = 0;
     stack[sp++] = 0;
     while (sp) {
         const Node &n = m.bvh.nodes[stack[--sp]];
-        if (!box_hit(n, oo, inv, box_tmin, cull_far(best.t)))
+        if (!box_hit(n, oo, inv, box_tmin, cull_far(best.t, slack)))
             continue;
         if (n.left < 0) {
             for (int k = n.first; k < n.first + n.count; k++) {
@@ -422,14 +427,17 @@ Hit trace_after(const Scene &s, V3 o, V3 d, float tmin, float tmax, const Hit &a
     int stack[128];
     int sp = 0;
     stack[sp++] = 0;
-    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t));
+    const float om = std::max(std::max(std::fabs(o.x), std::fabs(o.y)), std::fabs(o.z));
+    const float dm = std::max(std::max(std::fabs(d.x), std::fabs(d.y)), std::fabs(d.z));
+    const float slack = dm > 0.0f ? 1e-5f * (s.cull_o * om + s.cull_r) / dm : 0.0f;
+    float box_tmin = cull_near(after.inst == NOHIT ? tmin : std::max(tmin, after.t), slack);
     while (sp) {
         const Node &n = s.tlas.nodes[stack[--sp]];
-        if (!box_hit(n, o, inv, box_tmin, cull_far(best.t)))
+        if (!box_hit(n, o, inv, box_tmin, cull_far(best.t, slack)))
             continue;
         if (n.left < 0) {
             for (int k = n.first; k < n.first + n.count; k++)
-                trace_mesh(s, s.tlas_ids[s.tlas.order[k]], o, d, tmin, after, best);
+                trace_mesh(s, s.tlas_ids[s.tlas.order[k]], o, d, tmin, slack, after, best);
         } else {
             if (sp + 2 > 128)
                 continue;
@@ -1519,6 +1527,16 @@ bool build_scene(const vvpt_scene_desc *desc, Scene &s)
                     b[3 + a] = std::max(b[3 + a], comp(q, a) + pad);
                 }
             }
+            // culling bound: |o_obj| <= |W|(|o| + |t|), |d_obj| >= |d| / |M|
+            double nm = 0.0, nw = 0.0, tt = 0.0, pm = 0.0;
+            for (int r = 0; r < 3; r++) {
+                nm = std::max(nm, (double)std::fabs(in.o2w.m[r][0]) + std::fabs(in.o2w.m[r][1]) + std::fabs(in.o2w.m[r][2]));
+                nw = std::max(nw, (double)std::fabs(in.w2o.m[r][0]) + std::fabs(in.w2o.m[r][1]) + std::fabs(in.w2o.m[r][2]));
+                tt = std::max(tt, (double)std::fabs(in.o2w.m[r][3]));
+                pm = std::max(pm, (double)std::max(std::fabs(m.lo[r]), std::fabs(m.hi[r])));
+            }
+            s.cull_o = std::max(s.cull_o, (float)(nm * nw));
+            s.cull_r = std::max(s.cull_r, (float)(nm * (nw * tt + pm)));
             tboxes.push_back(b);
             s.tlas_ids.push_back(i);
         }

@@ -1,0 +1,67 @@
+// Test harness: the device traversal of vviewer_gb300/csrc/traverse.cuh
+// compiled for the host, over the scene arrays that vvpt_scene_upload would
+// upload (pack_scene). The rounding intrinsics map to plain IEEE float /
+// double operations, which round to nearest like the device's _rn forms
+// (compile with -ffp-contract=off so no multiply-add is fused). Used only by
+// the tests to check the traversal's bookkeeping (stack, instance entry and
+// return, culling order) against the oracle without a GPU; it is not a
+// rendering path.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
+static inline double __dmul_rn(double a, double b) { return a * b; }
+static inline double __dsub_rn(double a, double b) { return a - b; }
+static inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+static inline unsigned __float_as_uint(float f) { unsigned i; std::memcpy(&i, &f, 4); return i; }
+static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+template <class T>
+static inline T __ldg(const T *p) { return *p; }
+
+#include "scene_pack.h"
+#include "traverse.cuh"
+
+using namespace vvpt;
+
+extern "C" int host_trace_closest(const vvpt_scene_desc *desc, const vvpt_ray *rays, uint32_t n, vvpt_hit *hits,
+                                  uint32_t *err_bits, char *msg, int msg_len)
+{
+    PackedScene pk;
+    std::string err;
+    vvpt_status st = pack_scene(desc, pk, err, 1);
+    if (st != VVPT_OK) {
+        std::strncpy(msg, err.c_str(), msg_len - 1);
+        msg[msg_len - 1] = 0;
+        return (int)st;
+    }
+    SceneView v{};
+    v.nodes = pk.nodes.data();
+    v.tris = pk.tris.data();
+    v.verts = pk.verts.data();
+    v.indices = pk.indices.data();
+    v.instances = pk.instances.data();
+    v.tlas_order = pk.tlas_order.data();
+    v.tlas_root = pk.tlas_root;
+    v.num_instances = desc->num_instances;
+    v.cull_o = pk.cull_o;
+    v.cull_r = pk.cull_r;
+    uint32_t e = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const vvpt_ray &r = rays[i];
+        Hit h = trace_closest(v, f3(r.origin[0], r.origin[1], r.origin[2]),
+                              f3(r.direction[0], r.direction[1], r.direction[2]), r.tmin, r.tmax, e);
+        hits[i].t = h.t;
+        hits[i].u = h.u;
+        hits[i].v = h.v;
+        hits[i].instance = h.inst;
+        hits[i].primitive = h.prim;
+    }
+    *err_bits = e;
+    return 0;
+}

@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 import reference_scenes as R
+from raygen import HIT_SCENES, make_near_rays, make_rays
 from oracle import oracle
 from vviewer_gb300 import _native as N
 from vviewer_gb300 import scenes
@@ -26,58 +27,12 @@ from vviewer_gb300.scene import EnvironmentType, Engine, MaterialLambert, Transf
 pytestmark = pytest.mark.gpu
 
 
-def world_triangles(fs):
-    """World-space vertices of every TLAS triangle: (T x 3 x 3)."""
-    out = []
-    for inst in fs.instances:
-        if not inst.flags & 1:
-            continue
-        m = fs.meshes[inst.mesh_index]
-        M = np.array(list(inst.model), dtype=np.float64).reshape(4, 4).T
-        p = m.vertices["position"][m.indices.astype(np.int64)].astype(np.float64)
-        w = p @ M[:3, :3].T + M[:3, 3]
-        out.append(w)
-    return np.concatenate(out)
-
-
-def make_rays(fs, n, seed, lo, hi):
-    rng = np.random.default_rng(seed)
-    tris = world_triangles(fs)
-    k = n // 2
-    # random rays
-    o1 = rng.uniform(lo, hi, (k, 3))
-    d1 = rng.normal(size=(k, 3))
-    # rays aimed at triangle interiors, edges and vertices (watertightness, ties)
-    pick = tris[rng.integers(0, len(tris), n - k)]
-    bc = rng.dirichlet([1, 1, 1], n - k)
-    kind = rng.integers(0, 3, n - k)
-    bc[kind == 1, 2] = 0.0  # edge v0-v1
-    bc[kind == 2] = [1.0, 0.0, 0.0]  # vertex
-    bc /= bc.sum(1, keepdims=True)
-    target = (pick * bc[:, :, None]).sum(1)
-    o2 = rng.uniform(lo, hi, (n - k, 3))
-    d2 = target - o2
-    o = np.concatenate([o1, o2])
-    d = np.concatenate([d1, d2])
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    tmin = np.where(rng.random(n) < 0.5, 0.0, 1e-3)
-    rays = np.concatenate([o, tmin[:, None], d, np.full((n, 1), 1e4)], 1).astype(np.float32)
-    return rays
-
-
 def assert_hits_equal(hg, ho):
     for f in ("instance", "primitive", "t", "u", "v"):
         eq = hg[f] == ho[f]
         assert eq.all(), f"{f}: {np.count_nonzero(~eq)} of {len(eq)} differ, first {np.nonzero(~eq)[0][:5]}"
 
 
-HIT_SCENES = {
-    "cornell": (lambda: scenes.cornell_box(1)[0], (-0.2, 1.2)),
-    "two_balls_mesh_light": (lambda: R.mesh_light()[0], (-3.0, 4.0)),
-    "volume_cube": (lambda: R.volume(9)[0], (-3.0, 4.0)),
-    "shared_components": (lambda: R.shared_components()[0], (-160.0, 160.0)),
-    "displaced_spheres": (lambda: scenes.cornell_medium(3, freq=12, spheres=8)[0], (-0.2, 1.2)),
-}
 
 
 @pytest.mark.parametrize("name", list(HIT_SCENES))
@@ -86,6 +41,7 @@ def test_closest_hit_bit_exact(ctx, name):
     fs = build().scene.build()
     g = ctx.upload(fs)
     rays = make_rays(fs, 200_000 if name != "shared_components" else 50_000, 7, lo, hi)
+    rays = np.concatenate([rays, make_near_rays(fs, 50_000, 11)])
     hg = g.trace_closest(rays)
     ho = oracle.trace_closest(fs, rays)
     assert (hg["instance"] != 0xFFFFFFFF).mean() > 0.3

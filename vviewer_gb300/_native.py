@@ -13,6 +13,9 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvvpt.so"
 
 VVPT_OK = 0
+TIMEOUT = 4
+BUDGET_EXCEEDED = 3
+NOT_READY = 6
 STATUS_NAMES = {
     0: "VVPT_OK", 1: "VVPT_ERR_INVALID_ARG", 2: "VVPT_ERR_OOM", 3: "VVPT_ERR_BUDGET_EXCEEDED",
     4: "VVPT_ERR_TIMEOUT", 5: "VVPT_ERR_DEVICE", 6: "VVPT_ERR_NOT_READY", 7: "VVPT_ERR_EMPTY_SCENE",
@@ -129,6 +132,18 @@ RENDER_PROFILE_KERNELS = 2
 
 
 # every symbol include/vvpt.h declares, with its ctypes signature
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("status", C.c_int32), ("submit_ms", C.c_double), ("start_ms", C.c_double),
+                ("end_ms", C.c_double), ("paths", C.c_uint64), ("device_bytes", C.c_uint64)]
+
+
+class EngineStats(C.Structure):
+    _fields_ = [("fixed_bytes", C.c_uint64), ("job_bytes", C.c_uint64), ("queued", C.c_uint32),
+                ("running", C.c_uint32), ("finished", C.c_uint32), ("slots", C.c_uint32)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
 _SIGNATURES = {
     "vvpt_version": (C.c_char_p, []),
     "vvpt_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
@@ -148,6 +163,15 @@ _SIGNATURES = {
     "vvpt_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vvpt_render_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SceneData), C.POINTER(RenderInfo),
                                       C.POINTER(Outputs)]),
+    "vvpt_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SceneData), C.POINTER(RenderInfo),
+                              C.POINTER(Outputs), C.POINTER(C.c_uint64)]),
+    "vvpt_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(JobInfo)]),
+    "vvpt_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
+    "vvpt_job_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vvpt_set_budget": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vvpt_engine_stats_get": (C.c_int, [C.c_void_p, C.POINTER(EngineStats)]),
+    "vvpt_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(SceneData),
+                                    C.POINTER(RenderInfo), C.POINTER(Outputs)]),
 }
 
 _lib = None

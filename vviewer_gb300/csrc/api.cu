@@ -13,146 +13,126 @@
 #include <vector>
 
 #include "../../include/vvpt.h"
-#include "bvh_build.h"
+#include "internal.h"
+#include "scene_pack.h"
 #include "scene_gpu.h"
+#include "traverse.cuh"
 #include "wavefront.cuh"
 
 using namespace vvpt;
 
+namespace vvpt {
+
+vvpt_status make_render_params(vvpt_ctx *ctx, const vvpt_scene *scene, const vvpt_scene_data *sd,
+                               const vvpt_render_info *info, RenderParams &hp)
+{
+    if (info->width == 0 || info->height == 0 || info->batch_size == 0)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "width, height and batch_size must be positive");
+    if ((uint64_t)info->width * info->height > (1ull << 28))
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "resolution too large");
+    const uint32_t batches = info->samples / info->batch_size; // integer truncation, as the reference
+    hp = RenderParams{};
+    for (int c = 0; c < 4; c++) {
+        hp.view_inv[c] = make_float4(sd->view_inverse[c * 4 + 0], sd->view_inverse[c * 4 + 1],
+                                     sd->view_inverse[c * 4 + 2], sd->view_inverse[c * 4 + 3]);
+        hp.proj_inv[c] = make_float4(sd->projection_inverse[c * 4 + 0], sd->projection_inverse[c * 4 + 1],
+                                     sd->projection_inverse[c * 4 + 2], sd->projection_inverse[c * 4 + 3]);
+    }
+    hp.background = make_float3(sd->background[0], sd->background[1], sd->background[2]);
+    hp.env_type = sd->background[3];
+    hp.lens_radius = sd->exposure[2];
+    hp.focal_distance = sd->exposure[3];
+    hp.env_intensity = sd->exposure[1];
+    hp.zfar = sd->volumes[2];
+    hp.zfar_trunc = (float)(uint32_t)std::max(0.0f, sd->volumes[2]);
+    hp.cam_volume = (int32_t)sd->volumes[0];
+    if (hp.cam_volume != -1 && (hp.cam_volume < 0 || (uint32_t)hp.cam_volume >= scene->num_materials))
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "camera volume material index out of range");
+    hp.width = info->width;
+    hp.height = info->height;
+    hp.batch_size = info->batch_size;
+    hp.batches = batches;
+    hp.depth = std::min(info->depth, 255u);
+    hp.total_samples = info->batch_size * batches;
+    hp.num_lights = scene->view.num_lights;
+    const uint64_t total_items64 = (uint64_t)info->width * info->height * batches;
+    if (total_items64 >= 0xFFFFFFF0ull)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "width * height * batches exceeds 2^32");
+    hp.total_items = (uint32_t)total_items64;
+    hp.want_m2 = (info->flags & VVPT_RENDER_WANT_BATCH_M2) ? 1u : 0u;
+    return VVPT_OK;
+}
+
+// 14 float4 arrays (one spare) and 7 uint32 arrays per slot
+size_t path_state_bytes(size_t slots)
+{
+    return 14 * aligned256(slots * sizeof(float4)) + 7 * aligned256(slots * sizeof(uint32_t));
+}
+
+size_t queue_bytes(size_t slots)
+{
+    return 10 * aligned256(slots * sizeof(uint32_t)) + aligned256(C_COUNT * sizeof(uint32_t));
+}
+
+PathState carve_path_state(char *base, size_t n)
+{
+    const size_t f4 = aligned256(n * sizeof(float4)), u4 = aligned256(n * sizeof(uint32_t));
+    auto take = [&](size_t b) {
+        char *p = base;
+        base += b;
+        return p;
+    };
+    PathState ps;
+    ps.o = (float4 *)take(f4);
+    ps.d = (float4 *)take(f4);
+    ps.beta = (float4 *)take(f4);
+    ps.rad = (float4 *)take(f4);
+    ps.alb = (float4 *)take(f4);
+    ps.nrm = (float4 *)take(f4);
+    ps.cum_rad = (float4 *)take(f4);
+    ps.cum_alb = (float4 *)take(f4);
+    ps.cum_nrm = (float4 *)take(f4);
+    ps.hit = (float4 *)take(f4);
+    ps.sh_dir = (float4 *)take(f4);
+    ps.sh_c = (float4 *)take(f4);
+    ps.nee_b = (float4 *)take(f4);
+    take(f4); // spare
+    ps.hit_inst = (uint32_t *)take(u4);
+    ps.rng = (uint32_t *)take(u4);
+    ps.flags = (uint32_t *)take(u4);
+    ps.vol = (uint32_t *)take(u4);
+    ps.item = (uint32_t *)take(u4);
+    ps.sample = (uint32_t *)take(u4);
+    ps.job = (uint32_t *)take(u4);
+    return ps;
+}
+
+Queues carve_queues(char *base, size_t n)
+{
+    const size_t u4 = aligned256(n * sizeof(uint32_t));
+    auto take = [&](size_t b) {
+        char *p = base;
+        base += b;
+        return p;
+    };
+    Queues q;
+    q.ext[0] = (uint32_t *)take(u4);
+    q.ext[1] = (uint32_t *)take(u4);
+    q.shade_l = (uint32_t *)take(u4);
+    q.shade_p = (uint32_t *)take(u4);
+    q.shade_m = (uint32_t *)take(u4);
+    q.conn = (uint32_t *)take(u4);
+    q.ext_key = (uint32_t *)take(u4);
+    q.walk = (uint32_t *)take(u4);
+    q.regen[0] = (uint32_t *)take(u4);
+    q.regen[1] = (uint32_t *)take(u4);
+    q.counters = (uint32_t *)take(aligned256(C_COUNT * sizeof(uint32_t)));
+    return q;
+}
+
+}  // namespace vvpt
+
 namespace {
-
-struct DevBuf {
-    void *ptr = nullptr;
-    size_t bytes = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (ptr)
-            cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-    }
-    cudaError_t alloc(size_t n)
-    {
-        release();
-        if (n == 0)
-            n = 16;
-        cudaError_t e = cudaMalloc(&ptr, n);
-        if (e == cudaSuccess)
-            bytes = n;
-        else
-            ptr = nullptr;
-        return e;
-    }
-    // grow-only reuse
-    cudaError_t reserve(size_t n)
-    {
-        if (ptr && bytes >= n)
-            return cudaSuccess;
-        return alloc(n);
-    }
-    template <class T>
-    T *as() const
-    {
-        return reinterpret_cast<T *>(ptr);
-    }
-};
-
-struct StatusError {
-    vvpt_status code;
-    std::string msg;
-};
-
-}  // namespace
-
-struct vvpt_scene {
-    DevBuf nodes, tris, verts, indices, instances, tlas_order, materials, lights, textures, texels;
-    SceneView view{};
-    uint64_t bytes = 0;
-    uint32_t num_materials = 0;
-};
-
-struct vvpt_ctx {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    std::string last_error;
-    std::atomic<float> progress{0.0f};
-    vvpt_render_stats stats{};
-    vvpt_tuning tuning{};
-    // render buffers (grow-only, reused across renders)
-    DevBuf state, queues, results, params, outputs;
-    uint32_t *counters_pinned = nullptr;
-    DevBuf rays, hits_tuv, hits_ids, err_word;
-    cudaStream_t user_stream = nullptr;
-    vvpt_kernel_profile profile{};
-};
-
-namespace {
-
-inline cudaStream_t vv_stream(const vvpt_ctx *ctx) { return ctx->user_stream ? ctx->user_stream : ctx->stream; }
-
-vvpt_status fail(vvpt_ctx *ctx, vvpt_status code, const std::string &msg)
-{
-    if (ctx)
-        ctx->last_error = msg;
-    return code;
-}
-
-vvpt_status cuda_fail(vvpt_ctx *ctx, cudaError_t e, const char *what)
-{
-    cudaGetLastError();
-    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-    return fail(ctx, e == cudaErrorMemoryAllocation ? VVPT_ERR_OOM : VVPT_ERR_DEVICE, m);
-}
-
-#define VV_CUDA(call, what)                       \
-    do {                                          \
-        cudaError_t _e = (call);                  \
-        if (_e != cudaSuccess)                    \
-            return cuda_fail(ctx, _e, what);      \
-    } while (0)
-
-// column-major 4x4 -> rows of the 3x4 affine part
-void affine_rows(const float m[16], float4 rows[3])
-{
-    for (int r = 0; r < 3; r++)
-        rows[r] = make_float4(m[0 * 4 + r], m[1 * 4 + r], m[2 * 4 + r], m[3 * 4 + r]);
-}
-
-// inverse of the 3x4 affine part in double, rounded to float rows
-bool affine_inverse_rows(const float m[16], float4 rows[3])
-{
-    double a[3][3], t[3];
-    for (int r = 0; r < 3; r++) {
-        for (int c = 0; c < 3; c++)
-            a[r][c] = m[c * 4 + r];
-        t[r] = m[3 * 4 + r];
-    }
-    double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
-                 a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
-    if (!(std::fabs(det) > 0.0))
-        return false;
-    double inv[3][3];
-    inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
-    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
-    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
-    inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
-    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
-    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
-    inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
-    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
-    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
-    for (int r = 0; r < 3; r++) {
-        double tt = -(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]);
-        rows[r] = make_float4((float)inv[r][0], (float)inv[r][1], (float)inv[r][2], (float)tt);
-    }
-    return true;
-}
 
 template <class T>
 vvpt_status upload(vvpt_ctx *ctx, DevBuf &buf, const std::vector<T> &v, uint64_t &bytes)
@@ -165,10 +145,47 @@ vvpt_status upload(vvpt_ctx *ctx, DevBuf &buf, const std::vector<T> &v, uint64_t
     return VVPT_OK;
 }
 
-struct MeshBuild {
-    BVHBuildResult bvh;
-    Box3 root{};
+// Device block of a one-job table (single renders): the job, its one
+// hand-out range and the table's counters in one struct, filled on the host
+// and copied with one memcpy.
+struct SingleJobBlock {
+    JobView job;
+    unsigned long long range_begin;
+    unsigned long long next_item;
+    unsigned long long total_items;
+    uint32_t range_job;
+    uint32_t num_ranges;
+    uint32_t idle_count;
+    uint32_t item_done;
 };
+
+JobTable single_job_table(SingleJobBlock *d, uint32_t *idle)
+{
+    JobTable jt;
+    jt.jobs = &d->job;
+    jt.range_begin = &d->range_begin;
+    jt.range_job = &d->range_job;
+    jt.item_done = &d->item_done;
+    jt.next_item = &d->next_item;
+    jt.total_items = &d->total_items;
+    jt.num_ranges = &d->num_ranges;
+    jt.idle = idle;
+    jt.idle_count = &d->idle_count;
+    return jt;
+}
+
+SingleJobBlock single_job_host(const SceneView &view, const RenderParams &hp, const BatchResults &br)
+{
+    SingleJobBlock h{};
+    h.job.scene = view;
+    h.job.params = hp;
+    h.job.results = br;
+    h.range_begin = 0;
+    h.range_job = 0;
+    h.total_items = hp.total_items;
+    h.num_ranges = 1;
+    return h;
+}
 
 }  // namespace
 
@@ -197,7 +214,8 @@ VVPT_API vvpt_status vvpt_create(int device, vvpt_ctx **out_ctx)
         delete ctx;
         return VVPT_ERR_DEVICE;
     }
-    if (cudaMallocHost(&ctx->counters_pinned, C_COUNT * sizeof(uint32_t)) != cudaSuccess) {
+    // counters plus room for per-job done counts read alongside them
+    if (cudaMallocHost(&ctx->counters_pinned, (C_COUNT + 4096) * sizeof(uint32_t)) != cudaSuccess) {
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return VVPT_ERR_OOM;
@@ -210,6 +228,7 @@ VVPT_API vvpt_status vvpt_destroy(vvpt_ctx *ctx)
 {
     if (!ctx)
         return VVPT_ERR_INVALID_ARG;
+    engine_shutdown(ctx);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(vv_stream(ctx));
     if (ctx->counters_pinned)
@@ -253,321 +272,35 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
 
-    // ---- validation (indices the shaders would dereference)
-    if ((desc->num_meshes && !desc->meshes) || (desc->num_instances && !desc->instances) ||
-        (desc->num_materials && !desc->materials) || (desc->num_lights && !desc->lights) ||
-        (desc->num_light_data && !desc->light_data) || (desc->num_textures && !desc->textures))
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "array pointer is null while its count is not zero");
-    for (uint32_t m = 0; m < desc->num_meshes; m++) {
-        const vvpt_mesh_desc &md = desc->meshes[m];
-        if ((md.num_vertices && !md.vertices) || (md.num_triangles && !md.indices))
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "mesh " + std::to_string(m) + ": null vertex or index array");
-        for (uint64_t i = 0; i < 3ull * md.num_triangles; i++)
-            if (md.indices[i] >= md.num_vertices)
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "mesh " + std::to_string(m) + ": index out of range");
-    }
-    auto check_tex = [&](uint32_t t) { return t < desc->num_textures; };
-    bool has_transparent = false;
-    for (uint32_t i = 0; i < desc->num_materials; i++) {
-        const vvpt_material &mt = desc->materials[i];
-        for (int k = 0; k < 4; k++) {
-            if (k != 2 && !check_tex(mt.textures2[k]) && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME)
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "material " + std::to_string(i) + ": texture index out of range");
-            if (!check_tex(mt.textures1[k]) && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME &&
-                !((uint32_t)mt.uv_tiling[2] == VVPT_MATERIAL_LAMBERT && (k == 1 || k == 2)))
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "material " + std::to_string(i) + ": texture index out of range");
-        }
-        if (mt.metallic_roughness_ao[3] > 0.0f && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME)
-            has_transparent = true;
-    }
-    for (uint32_t i = 0; i < desc->num_instances; i++) {
-        const vvpt_instance &in = desc->instances[i];
-        if (!(in.flags & VVPT_INSTANCE_IN_TLAS))
-            continue;
-        if (in.mesh_index >= desc->num_meshes)
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": mesh index out of range");
-        if (in.material_index >= desc->num_materials)
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": material index out of range");
-        uint32_t mtype = (uint32_t)desc->materials[in.material_index].uv_tiling[2];
-        if (mtype != VVPT_MATERIAL_PBR_STANDARD && mtype != VVPT_MATERIAL_LAMBERT)
-            return fail(ctx, VVPT_ERR_INVALID_ARG,
-                        "instance " + std::to_string(i) + ": surface material must be PBR standard or Lambert");
-        for (int k = 1; k <= 2; k++) {
-            float v = in.id[k];
-            if (v != -1.0f && !(v >= 0.0f && (uint32_t)v < desc->num_materials))
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": volume index out of range");
-        }
-    }
-    for (uint32_t i = 0; i < desc->num_lights; i++) {
-        const vvpt_light_instance &L = desc->lights[i];
-        if (L.info[3] <= 1 && L.info[0] >= desc->num_light_data)
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "light " + std::to_string(i) + ": light data index out of range");
-        if (L.info[3] == 2) {
-            if (L.info[1] >= desc->num_instances)
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": instance out of range");
-            const vvpt_instance &in = desc->instances[L.info[1]];
-            if (in.mesh_index >= desc->num_meshes || in.material_index >= desc->num_materials ||
-                desc->meshes[in.mesh_index].num_triangles == 0)
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": instance has no mesh");
-        }
-        if (L.info[3] > 2)
-            return fail(ctx, VVPT_ERR_UNSUPPORTED, "light " + std::to_string(i) + ": unsupported light type");
-    }
-    for (uint32_t t = 0; t < desc->num_textures; t++) {
-        const vvpt_texture_desc &td = desc->textures[t];
-        if (!td.data || td.width == 0 || td.height == 0 || td.format > VVPT_TEXTURE_RGBA32F)
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "texture " + std::to_string(t) + ": bad description");
-    }
-
+    PackedScene pk;
+    std::string err;
+    vvpt_status st = pack_scene(desc, pk, err);
+    if (st != VVPT_OK)
+        return fail(ctx, st, err);
     auto scene = new vvpt_scene();
     std::unique_ptr<vvpt_scene> guard(scene);
 
-    // ---- BLAS per mesh (largest first, meshes built in parallel)
-    const uint32_t nm = desc->num_meshes;
-    std::vector<MeshBuild> builds(nm);
-    std::vector<uint32_t> order(nm);
-    for (uint32_t i = 0; i < nm; i++)
-        order[i] = i;
-    std::sort(order.begin(), order.end(),
-              [&](uint32_t a, uint32_t b) { return desc->meshes[a].num_triangles > desc->meshes[b].num_triangles; });
-    std::atomic<uint32_t> next{0};
-    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    auto worker = [&]() {
-        for (;;) {
-            uint32_t k = next.fetch_add(1);
-            if (k >= nm)
-                break;
-            uint32_t m = order[k];
-            const vvpt_mesh_desc &md = desc->meshes[m];
-            std::vector<Box3> boxes(md.num_triangles);
-            for (uint32_t t = 0; t < md.num_triangles; t++) {
-                Box3 &b = boxes[t];
-                for (int a = 0; a < 3; a++) {
-                    b.lo[a] = INFINITY;
-                    b.hi[a] = -INFINITY;
-                }
-                for (int c = 0; c < 3; c++) {
-                    const float *p = md.vertices[md.indices[3 * t + c]].position;
-                    for (int a = 0; a < 3; a++) {
-                        b.lo[a] = std::min(b.lo[a], p[a]);
-                        b.hi[a] = std::max(b.hi[a], p[a]);
-                    }
-                }
-            }
-            BVHBuildOptions opt;
-            opt.threads = (k == 0 && md.num_triangles > 100000) ? (int)hw : 1;
-            builds[m].bvh = build_bvh2(boxes, opt);
-            Box3 r;
-            for (int a = 0; a < 3; a++) {
-                r.lo[a] = INFINITY;
-                r.hi[a] = -INFINITY;
-            }
-            for (const Box3 &b : boxes)
-                for (int a = 0; a < 3; a++) {
-                    r.lo[a] = std::min(r.lo[a], b.lo[a]);
-                    r.hi[a] = std::max(r.hi[a], b.hi[a]);
-                }
-            builds[m].root = r;
-        }
-    };
-    {
-        std::vector<std::thread> th;
-        unsigned nth = std::min<unsigned>(hw, std::max<uint32_t>(nm, 1));
-        for (unsigned i = 0; i < nth; i++)
-            th.emplace_back(worker);
-        for (auto &t : th)
-            t.join();
-    }
-
-    std::vector<MeshInfo> minfo(nm);
-    std::vector<BVHNode> nodes;
-    std::vector<TriVerts> tris;
-    std::vector<ShadeVertex> verts;
-    std::vector<uint32_t> indices;
-    size_t total_nodes = 0, total_tris = 0, total_verts = 0;
-    for (uint32_t m = 0; m < nm; m++) {
-        total_nodes += builds[m].bvh.nodes.size();
-        total_tris += desc->meshes[m].num_triangles;
-        total_verts += desc->meshes[m].num_vertices;
-    }
-    nodes.reserve(total_nodes + 2 * desc->num_instances + 2);
-    tris.reserve(total_tris);
-    verts.reserve(total_verts);
-    indices.reserve(3 * total_tris);
-    for (uint32_t m = 0; m < nm; m++) {
-        const vvpt_mesh_desc &md = desc->meshes[m];
-        MeshInfo &mi = minfo[m];
-        mi.node_offset = (uint32_t)nodes.size();
-        mi.tri_offset = (uint32_t)tris.size();
-        mi.vertex_offset = (uint32_t)verts.size();
-        mi.index_offset = (uint32_t)indices.size();
-        mi.num_triangles = md.num_triangles;
-        mi.num_nodes = (uint32_t)builds[m].bvh.nodes.size();
-        nodes.insert(nodes.end(), builds[m].bvh.nodes.begin(), builds[m].bvh.nodes.end());
-        for (uint32_t k = 0; k < md.num_triangles; k++) {
-            uint32_t prim = builds[m].bvh.order[k];
-            TriVerts tv;
-            const float *p0 = md.vertices[md.indices[3 * prim + 0]].position;
-            const float *p1 = md.vertices[md.indices[3 * prim + 1]].position;
-            const float *p2 = md.vertices[md.indices[3 * prim + 2]].position;
-            float pid;
-            std::memcpy(&pid, &prim, 4);
-            tv.v0 = make_float4(p0[0], p0[1], p0[2], pid);
-            tv.v1 = make_float4(p1[0], p1[1], p1[2], 0.0f);
-            tv.v2 = make_float4(p2[0], p2[1], p2[2], 0.0f);
-            tris.push_back(tv);
-        }
-        for (uint32_t v = 0; v < md.num_vertices; v++) {
-            const vvpt_vertex &x = md.vertices[v];
-            ShadeVertex sv;
-            sv.pos_u = make_float4(x.position[0], x.position[1], x.position[2], x.uv[0]);
-            sv.nrm_v = make_float4(x.normal[0], x.normal[1], x.normal[2], x.uv[1]);
-            sv.tan_ = make_float4(x.tangent[0], x.tangent[1], x.tangent[2], 0.0f);
-            verts.push_back(sv);
-        }
-        indices.insert(indices.end(), md.indices, md.indices + 3ull * md.num_triangles);
-    }
-
-    // ---- instances + TLAS
-    const uint32_t ni = desc->num_instances;
-    std::vector<DevInstance> dinst(ni);
-    std::vector<Box3> tlas_boxes;
-    std::vector<uint32_t> tlas_ids;
-    for (uint32_t i = 0; i < ni; i++) {
-        const vvpt_instance &in = desc->instances[i];
-        DevInstance &d = dinst[i];
-        std::memset(&d, 0, sizeof(d));
-        affine_rows(in.model, d.o2w);
-        if (!affine_inverse_rows(in.model, d.w2o)) {
-            if (in.flags & VVPT_INSTANCE_IN_TLAS)
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": singular model matrix");
-        }
-        d.material = in.material_index < desc->num_materials ? in.material_index : 0;
-        d.front_volume = (int32_t)in.id[1];
-        d.back_volume = (int32_t)in.id[2];
-        if (in.mesh_index < nm) {
-            const MeshInfo &mi = minfo[in.mesh_index];
-            d.node_offset = mi.node_offset;
-            d.tri_offset = mi.tri_offset;
-            d.vertex_offset = mi.vertex_offset;
-            d.index_offset = mi.index_offset;
-            d.num_triangles = mi.num_triangles;
-        }
-        if ((in.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh_index < nm && minfo[in.mesh_index].num_triangles > 0) {
-            const Box3 &r = builds[in.mesh_index].root;
-            Box3 w;
-            for (int a = 0; a < 3; a++) {
-                w.lo[a] = INFINITY;
-                w.hi[a] = -INFINITY;
-            }
-            for (int c = 0; c < 8; c++) {
-                double p[3] = {(c & 1) ? r.hi[0] : r.lo[0], (c & 2) ? r.hi[1] : r.lo[1], (c & 4) ? r.hi[2] : r.lo[2]};
-                const float4 *rows = d.o2w;
-                double q[3] = {rows[0].x * p[0] + rows[0].y * p[1] + rows[0].z * p[2] + rows[0].w,
-                               rows[1].x * p[0] + rows[1].y * p[1] + rows[1].z * p[2] + rows[1].w,
-                               rows[2].x * p[0] + rows[2].y * p[1] + rows[2].z * p[2] + rows[2].w};
-                for (int a = 0; a < 3; a++) {
-                    // widen by a few ulps: the box must contain every
-                    // object-space hit mapped back to world space
-                    double pad = 1e-5 * (std::fabs(q[a]) + 1.0);
-                    w.lo[a] = std::min(w.lo[a], (float)(q[a] - pad));
-                    w.hi[a] = std::max(w.hi[a], (float)(q[a] + pad));
-                }
-            }
-            tlas_boxes.push_back(w);
-            tlas_ids.push_back(i);
-        }
-    }
-    BVHBuildResult tlas = build_bvh2(tlas_boxes);
-    const uint32_t tlas_root = (uint32_t)nodes.size();
-    nodes.insert(nodes.end(), tlas.nodes.begin(), tlas.nodes.end());
-    std::vector<uint32_t> tlas_order(tlas.order.size());
-    for (size_t k = 0; k < tlas.order.size(); k++)
-        tlas_order[k] = tlas_ids[tlas.order[k]];
-    if (tlas.depth > 30 || [&] {
-            int md = 0;
-            for (auto &b : builds)
-                md = std::max(md, b.bvh.depth);
-            return md > 62;
-        }())
-        return fail(ctx, VVPT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
-
-    // ---- materials, lights, textures
-    std::vector<DevMaterial> mats(desc->num_materials);
-    static_assert(sizeof(DevMaterial) == sizeof(vvpt_material), "material layout");
-    if (desc->num_materials)
-        std::memcpy(mats.data(), desc->materials, sizeof(vvpt_material) * desc->num_materials);
-    std::vector<DevLightInstance> lights(desc->num_lights);
-    for (uint32_t i = 0; i < desc->num_lights; i++) {
-        const vvpt_light_instance &L = desc->lights[i];
-        DevLightInstance &d = lights[i];
-        std::memset(&d, 0, sizeof(d));
-        std::memcpy(d.info, L.info, sizeof(d.info));
-        d.position = make_float4(L.position[0], L.position[1], L.position[2], L.position[3]);
-        d.position1 = make_float4(L.position1[0], L.position1[1], L.position1[2], L.position1[3]);
-        d.position2 = make_float4(L.position2[0], L.position2[1], L.position2[2], L.position2[3]);
-        if (L.info[3] <= 1) {
-            const vvpt_light_data &ld = desc->light_data[L.info[0]];
-            d.color = make_float4(ld.color[0], ld.color[1], ld.color[2], ld.color[3]);
-        } else {
-            // transpose(inverse(M)) for the sampled normal (lightSampling.glsl:80)
-            float m[16] = {L.position[0], L.position1[0], L.position2[0], 0.0f, L.position[1], L.position1[1],
-                           L.position2[1], 0.0f, L.position[2], L.position1[2], L.position2[2], 0.0f,
-                           L.position[3], L.position1[3], L.position2[3], 1.0f};
-            float4 inv[3];
-            if (!affine_inverse_rows(m, inv))
-                return fail(ctx, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": singular transform");
-            d.nrm0 = make_float4(inv[0].x, inv[1].x, inv[2].x, 0.0f);
-            d.nrm1 = make_float4(inv[0].y, inv[1].y, inv[2].y, 0.0f);
-            d.nrm2 = make_float4(inv[0].z, inv[1].z, inv[2].z, 0.0f);
-        }
-    }
-    std::vector<DevTexture> texs;
-    std::vector<uint8_t> texels;
-    auto add_texture = [&](const vvpt_texture_desc &td) {
-        DevTexture t{};
-        t.width = td.width;
-        t.height = td.height;
-        t.format = td.format;
-        size_t texel_bytes = td.format == VVPT_TEXTURE_RGBA32F ? 16 : 4;
-        size_t off = (texels.size() + 15) & ~size_t(15);
-        texels.resize(off + texel_bytes * td.width * td.height);
-        std::memcpy(texels.data() + off, td.data, texel_bytes * td.width * td.height);
-        t.offset = off;
-        texs.push_back(t);
-    };
-    for (uint32_t t = 0; t < desc->num_textures; t++)
-        add_texture(desc->textures[t]);
-    int env_index = -1;
-    if (desc->environment) {
-        if (!desc->environment->data || desc->environment->format != VVPT_TEXTURE_RGBA32F)
-            return fail(ctx, VVPT_ERR_INVALID_ARG, "environment must be an RGBA32F equirectangular image");
-        env_index = (int)texs.size();
-        add_texture(*desc->environment);
-    }
-
     // ---- upload
-    vvpt_status st;
     uint64_t bytes = 0;
-    if ((st = upload(ctx, scene->nodes, nodes, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->nodes, pk.nodes, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->tris, tris, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->tris, pk.tris, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->verts, verts, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->verts, pk.verts, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->indices, indices, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->indices, pk.indices, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->instances, dinst, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->instances, pk.instances, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->tlas_order, tlas_order, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->tlas_order, pk.tlas_order, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->materials, mats, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->materials, pk.materials, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->lights, lights, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->lights, pk.lights, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->textures, texs, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->textures, pk.textures, bytes)) != VVPT_OK)
         return st;
-    if ((st = upload(ctx, scene->texels, texels, bytes)) != VVPT_OK)
+    if ((st = upload(ctx, scene->texels, pk.texels, bytes)) != VVPT_OK)
         return st;
     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "scene upload");
 
@@ -578,17 +311,19 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     v.indices = scene->indices.as<uint32_t>();
     v.instances = scene->instances.as<DevInstance>();
     v.tlas_order = scene->tlas_order.as<uint32_t>();
-    v.tlas_root = tlas_root;
-    v.num_instances = ni;
+    v.tlas_root = pk.tlas_root;
+    v.num_instances = desc->num_instances;
     v.materials = scene->materials.as<DevMaterial>();
     v.num_materials = desc->num_materials;
     v.lights = scene->lights.as<DevLightInstance>();
     v.num_lights = desc->num_lights;
     v.textures = scene->textures.as<DevTexture>();
-    v.num_textures = (uint32_t)texs.size();
+    v.num_textures = (uint32_t)pk.textures.size();
     v.texels = scene->texels.as<uint8_t>();
-    v.env_texture = env_index;
-    v.has_transparent = has_transparent ? 1u : 0u;
+    v.env_texture = pk.env_texture;
+    v.has_transparent = pk.has_transparent ? 1u : 0u;
+    v.cull_o = pk.cull_o;
+    v.cull_r = pk.cull_r;
     scene->bytes = bytes;
     scene->num_materials = desc->num_materials;
     *out_scene = guard.release();
@@ -599,6 +334,8 @@ VVPT_API vvpt_status vvpt_scene_release(vvpt_ctx *ctx, vvpt_scene *scene)
 {
     if (!ctx || !scene)
         return VVPT_ERR_INVALID_ARG;
+    if (scene->jobs_in_flight.load() != 0)
+        return fail(ctx, VVPT_ERR_NOT_READY, "scene still used by submitted jobs");
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(vv_stream(ctx));
@@ -654,47 +391,15 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
 {
     if (!ctx || !scene || !sd || !info || !out)
         return fail(ctx, VVPT_ERR_INVALID_ARG, "null argument");
-    if (info->width == 0 || info->height == 0 || info->batch_size == 0)
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "width, height and batch_size must be positive");
-    if ((uint64_t)info->width * info->height > (1ull << 28))
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "resolution too large");
+    RenderParams hp;
+    vvpt_status pst0 = make_render_params(ctx, scene, sd, info, hp);
+    if (pst0 != VVPT_OK)
+        return pst0;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     ctx->progress.store(0.0f);
-    auto t_start = std::chrono::steady_clock::now();
-
-    const uint32_t W = info->width, H = info->height;
-    const uint32_t npix = W * H;
-    const uint32_t batches = info->samples / info->batch_size; // integer truncation, as the reference
-    RenderParams hp{};
-    for (int c = 0; c < 4; c++) {
-        hp.view_inv[c] = make_float4(sd->view_inverse[c * 4 + 0], sd->view_inverse[c * 4 + 1],
-                                     sd->view_inverse[c * 4 + 2], sd->view_inverse[c * 4 + 3]);
-        hp.proj_inv[c] = make_float4(sd->projection_inverse[c * 4 + 0], sd->projection_inverse[c * 4 + 1],
-                                     sd->projection_inverse[c * 4 + 2], sd->projection_inverse[c * 4 + 3]);
-    }
-    hp.background = make_float3(sd->background[0], sd->background[1], sd->background[2]);
-    hp.env_type = sd->background[3];
-    hp.lens_radius = sd->exposure[2];
-    hp.focal_distance = sd->exposure[3];
-    hp.env_intensity = sd->exposure[1];
-    hp.zfar = sd->volumes[2];
-    hp.zfar_trunc = (float)(uint32_t)std::max(0.0f, sd->volumes[2]);
-    hp.cam_volume = (int32_t)sd->volumes[0];
-    if (hp.cam_volume != -1 && (hp.cam_volume < 0 || (uint32_t)hp.cam_volume >= scene->num_materials))
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "camera volume material index out of range");
-    hp.width = W;
-    hp.height = H;
-    hp.batch_size = info->batch_size;
-    hp.batches = batches;
-    hp.depth = std::min(info->depth, 255u);
-    hp.total_samples = info->batch_size * batches;
-    hp.num_lights = scene->view.num_lights;
-    uint64_t total_items64 = (uint64_t)npix * batches;
-    if (total_items64 >= 0xFFFFFFF0ull)
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "width * height * batches exceeds 2^32");
-    hp.total_items = (uint32_t)total_items64;
-    hp.want_m2 = (info->flags & VVPT_RENDER_WANT_BATCH_M2) ? 1u : 0u;
+    const uint32_t npix = hp.width * hp.height;
+    const uint32_t batches = hp.batches;
 
     vvpt_render_stats stats{};
     // ---- output buffers
@@ -720,54 +425,18 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         uint32_t slots = ctx->tuning.slots ? ctx->tuning.slots : (1u << 20);
         slots = std::max<uint32_t>(32u, std::min<uint32_t>(slots, hp.total_items));
         const size_t n = slots;
-        const size_t f4 = n * sizeof(float4), u4 = n * sizeof(uint32_t);
-        auto aligned = [](size_t b) { return (b + 255) & ~size_t(255); };
+        const size_t u4 = n * sizeof(uint32_t);
+        auto aligned = [](size_t b) { return aligned256(b); };
         char *base = nullptr;
         auto take = [&](size_t b) {
             char *p = base;
             base += aligned(b);
             return p;
         };
-        VV_CUDA(ctx->state.reserve(14 * aligned(f4) + 7 * aligned(u4)), "cudaMalloc path state");
-        base = ctx->state.as<char>();
-        PathState ps;
-        ps.o = (float4 *)take(f4);
-        ps.d = (float4 *)take(f4);
-        ps.beta = (float4 *)take(f4);
-        ps.rad = (float4 *)take(f4);
-        ps.alb = (float4 *)take(f4);
-        ps.nrm = (float4 *)take(f4);
-        ps.cum_rad = (float4 *)take(f4);
-        ps.cum_alb = (float4 *)take(f4);
-        ps.cum_nrm = (float4 *)take(f4);
-        ps.hit = (float4 *)take(f4);
-        ps.sh_dir = (float4 *)take(f4);
-        ps.sh_c = (float4 *)take(f4);
-        ps.nee_b = (float4 *)take(f4);
-        take(f4); // spare
-        ps.hit_inst = (uint32_t *)take(u4);
-        ps.rng = (uint32_t *)take(u4);
-        ps.flags = (uint32_t *)take(u4);
-        ps.vol = (uint32_t *)take(u4);
-        ps.item = (uint32_t *)take(u4);
-        ps.sample = (uint32_t *)take(u4);
-        take(u4);
-
-        size_t qneed = 10 * aligned(u4) + aligned(C_COUNT * sizeof(uint32_t));
-        VV_CUDA(ctx->queues.reserve(qneed), "cudaMalloc queues");
-        base = ctx->queues.as<char>();
-        Queues q;
-        q.ext[0] = (uint32_t *)take(u4);
-        q.ext[1] = (uint32_t *)take(u4);
-        q.shade_l = (uint32_t *)take(u4);
-        q.shade_p = (uint32_t *)take(u4);
-        q.shade_m = (uint32_t *)take(u4);
-        q.conn = (uint32_t *)take(u4);
-        q.ext_key = (uint32_t *)take(u4);
-        q.walk = (uint32_t *)take(u4);
-        q.regen[0] = (uint32_t *)take(u4);
-        q.regen[1] = (uint32_t *)take(u4);
-        q.counters = (uint32_t *)take(C_COUNT * sizeof(uint32_t));
+        VV_CUDA(ctx->state.reserve(path_state_bytes(n)), "cudaMalloc path state");
+        const PathState ps = carve_path_state(ctx->state.as<char>(), n);
+        VV_CUDA(ctx->queues.reserve(queue_bytes(n)), "cudaMalloc queues");
+        const Queues q = carve_queues(ctx->queues.as<char>(), n);
 
         const size_t rb = (size_t)hp.total_items * sizeof(float4);
         size_t rneed = 3 * aligned(rb);
@@ -778,9 +447,13 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         br.alb = (float4 *)take(rb);
         br.nrm = (float4 *)take(rb);
 
-        VV_CUDA(ctx->params.reserve(sizeof(RenderParams)), "cudaMalloc params");
-        RenderParams *dparams = ctx->params.as<RenderParams>();
-        VV_CUDA(cudaMemcpyAsync(dparams, &hp, sizeof(hp), cudaMemcpyHostToDevice, vv_stream(ctx)), "upload params");
+        VV_CUDA(ctx->params.reserve(aligned(sizeof(SingleJobBlock)) + u4), "cudaMalloc job table");
+        base = ctx->params.as<char>();
+        SingleJobBlock *djob = (SingleJobBlock *)take(sizeof(SingleJobBlock));
+        const JobTable jt = single_job_table(djob, (uint32_t *)take(u4));
+        const SingleJobBlock hjob = single_job_host(scene->view, hp, br);
+        VV_CUDA(cudaMemcpyAsync(djob, &hjob, sizeof(hjob), cudaMemcpyHostToDevice, vv_stream(ctx)), "upload job");
+        uint32_t *d_item_done = &djob->item_done;
 
         LaunchShape shape;
         shape.block = ctx->tuning.threads_per_block ? (int)ctx->tuning.threads_per_block : 256;
@@ -800,7 +473,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
             }
         } tev_guard{tev};
         VV_CUDA(cudaEventRecord(tev[0], vv_stream(ctx)), "event");
-        launch_init_slots(q, ps, slots, vv_stream(ctx));
+        launch_init_slots(q, ps, jt, slots, vv_stream(ctx));
         stats.kernel_launches += 1;
         VV_CUDA(cudaGetLastError(), "launch init");
         const uint64_t max_iters =
@@ -838,7 +511,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                                      : (k == K_SHADOW || k == K_EMITTER) ? c[C_CONN]
                                                       : 1;
                     cudaEventRecord(ka, vv_stream(ctx));
-                    launch_kernel((KernelId)k, scene->view, dparams, ps, q, br, pp, shape, vv_stream(ctx));
+                    launch_kernel((KernelId)k, jt, ps, q, pp, shape, vv_stream(ctx));
                     cudaEventRecord(kb, vv_stream(ctx));
                     VV_CUDA(cudaEventSynchronize(kb), "profile kernel");
                     float ms = 0.0f;
@@ -850,12 +523,15 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                 }
                 VV_CUDA(cudaMemcpy(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost),
                         "read counters");
+                VV_CUDA(cudaMemcpy(ctx->counters_pinned + C_COUNT, d_item_done, sizeof(uint32_t),
+                                   cudaMemcpyDeviceToHost),
+                        "read done count");
                 const uint32_t *c = ctx->counters_pinned;
                 if (c[C_ERR]) {
                     pst = fail(ctx, VVPT_ERR_DEVICE, "device status word set: " + std::to_string(c[C_ERR]));
                     break;
                 }
-                if (c[C_NEXT_ITEM] >= hp.total_items && c[C_ACTIVE] == 0)
+                if (c[C_COUNT] >= hp.total_items)
                     break;
                 if (it > max_iters) {
                     pst = fail(ctx, VVPT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
@@ -875,7 +551,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         cudaGraphExec_t exec;
         VV_CUDA(cudaStreamBeginCapture(vv_stream(ctx), cudaStreamCaptureModeThreadLocal), "begin capture");
         for (int it = 0; it < Ke; it++)
-            launch_iteration(scene->view, dparams, ps, q, br, it & 1, shape, vv_stream(ctx));
+            launch_iteration(jt, ps, q, it & 1, shape, vv_stream(ctx));
         cudaError_t ce = cudaStreamEndCapture(vv_stream(ctx), &graph);
         if (ce != cudaSuccess)
             return cuda_fail(ctx, ce, "end capture");
@@ -903,6 +579,9 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
             VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, vv_stream(ctx)),
                     "read counters");
+            VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned + C_COUNT, d_item_done, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, vv_stream(ctx)),
+                    "read done count");
             VV_CUDA(cudaEventRecord(ev[launched & 1], vv_stream(ctx)), "event");
             int check = launched & 1;
             VV_CUDA(cudaGraphLaunch(exec, vv_stream(ctx)), "graph launch");
@@ -910,18 +589,14 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
             iters += Ke;
             VV_CUDA(cudaEventSynchronize(ev[check]), "wait counters");
             const uint32_t *c = ctx->counters_pinned;
-            float prog = hp.total_items ? (float)std::min<uint32_t>(c[C_NEXT_ITEM] - std::min(c[C_NEXT_ITEM], c[C_ACTIVE]),
-                                                                   hp.total_items) /
-                                              (float)hp.total_items
-                                        : 1.0f;
-            ctx->progress.store(prog);
+            ctx->progress.store((float)std::min<uint32_t>(c[C_COUNT], hp.total_items) / (float)hp.total_items);
             if (c[C_ERR]) {
                 loop_status = fail(ctx, VVPT_ERR_DEVICE,
                                    "device status word set (traversal stack overflow or loop cap): " +
                                        std::to_string(c[C_ERR]));
                 break;
             }
-            if (c[C_NEXT_ITEM] >= hp.total_items && c[C_ACTIVE] == 0)
+            if (c[C_COUNT] >= hp.total_items)
                 done = true;
             else if (iters > max_iters + 4 * (uint64_t)Ke) {
                 loop_status = fail(ctx, VVPT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
@@ -963,7 +638,6 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                         "download outputs");
     }
     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "render finish");
-    (void)t_start;
     ctx->stats = stats;
     ctx->progress.store(1.0f);
     return VVPT_OK;
@@ -1080,8 +754,9 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     const uint64_t slots64 = std::max<uint64_t>(32, std::min<uint64_t>(items64, kNoAllocMaxSlots));
     auto aligned = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
     const uint64_t f4 = slots64 * sizeof(float4), u4 = slots64 * sizeof(uint32_t);
-    const uint64_t need = aligned(sizeof(RenderParams)) + aligned(C_COUNT * sizeof(uint32_t)) + 14 * aligned(f4) +
-                          7 * aligned(u4) + 10 * aligned(u4) + 3 * aligned(items64 * sizeof(float4));
+    const uint64_t need = aligned(sizeof(SingleJobBlock)) + aligned(C_COUNT * sizeof(uint32_t)) + 14 * aligned(f4) +
+                          7 * aligned(u4) + aligned(u4) /* idle slots */ + 10 * aligned(u4) +
+                          3 * aligned(items64 * sizeof(float4));
     if (need > kNoAllocScratchBytes)
         return fail(ctx, VVPT_ERR_INVALID_ARG,
                     "render needs " + std::to_string(need) + " bytes of scratch; vvpt_render_noalloc has " +
@@ -1143,7 +818,7 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
         base += aligned(b);
         return p;
     };
-    RenderParams *dparams = reinterpret_cast<RenderParams *>(take(sizeof(RenderParams)));
+    SingleJobBlock *djob = reinterpret_cast<SingleJobBlock *>(take(sizeof(SingleJobBlock)));
     Queues q;
     q.counters = reinterpret_cast<uint32_t *>(take(C_COUNT * sizeof(uint32_t)));
     PathState ps;
@@ -1154,12 +829,10 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
         if (p)
             *p = m;
     }
-    uint32_t **u4s[7] = {&ps.hit_inst, &ps.rng, &ps.flags, &ps.vol, &ps.item, &ps.sample, nullptr};
-    for (uint32_t **p : u4s) {
-        uint32_t *m = reinterpret_cast<uint32_t *>(take(u4));
-        if (p)
-            *p = m;
-    }
+    uint32_t **u4s[7] = {&ps.hit_inst, &ps.rng, &ps.flags, &ps.vol, &ps.item, &ps.sample, &ps.job};
+    for (uint32_t **p : u4s)
+        *p = reinterpret_cast<uint32_t *>(take(u4));
+    const JobTable jt = single_job_table(djob, reinterpret_cast<uint32_t *>(take(u4)));
     uint32_t **qs[10] = {&q.ext[0], &q.ext[1], &q.shade_l, &q.shade_p, &q.shade_m,
                          &q.conn,   &q.ext_key, &q.walk,  &q.regen[0], &q.regen[1]};
     for (uint32_t **p : qs)
@@ -1169,12 +842,13 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     br.alb = reinterpret_cast<float4 *>(take(items64 * sizeof(float4)));
     br.nrm = reinterpret_cast<float4 *>(take(items64 * sizeof(float4)));
 
-    VV_CUDA(cudaMemcpyAsync(dparams, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream), "upload params");
+    const SingleJobBlock hjob = single_job_host(scene->view, hp, br);
+    VV_CUDA(cudaMemcpyAsync(djob, &hjob, sizeof(hjob), cudaMemcpyHostToDevice, stream), "upload job");
     LaunchShape shape;
     shape.block = 256;
     shape.grid = std::max(1, ctx->num_sms * 4);
     const uint32_t slots = (uint32_t)slots64;
-    launch_init_slots(q, ps, slots, stream);
+    launch_init_slots(q, ps, jt, slots, stream);
     VV_CUDA(cudaGetLastError(), "launch init");
     const uint64_t max_iters =
         (uint64_t)hp.batch_size * (hp.depth + 1) * ((hp.total_items + slots - 1) / slots + 1) + 64;
@@ -1186,7 +860,7 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     for (;;) {
         for (int k = 0; k < 8; k++) {
             for (int kk = 0; kk < K_NUM; kk++)
-                launch_kernel((KernelId)kk, scene->view, dparams, ps, q, br, (int)(it & 1), shape, stream);
+                launch_kernel((KernelId)kk, jt, ps, q, (int)(it & 1), shape, stream);
             it++;
         }
         stats.kernel_launches += 8 * K_NUM;
@@ -1194,14 +868,15 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
         VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 stream),
                 "read counters");
+        VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned + C_COUNT, &djob->item_done, sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, stream),
+                "read done count");
         VV_CUDA(cudaStreamSynchronize(stream), "render");
         const uint32_t *c = ctx->counters_pinned;
         if (c[C_ERR])
             return fail(ctx, VVPT_ERR_DEVICE, "device status word set: " + std::to_string(c[C_ERR]));
-        ctx->progress.store((float)std::min<uint32_t>(c[C_NEXT_ITEM] - std::min(c[C_NEXT_ITEM], c[C_ACTIVE]),
-                                                     hp.total_items) /
-                            (float)hp.total_items);
-        if (c[C_NEXT_ITEM] >= hp.total_items && c[C_ACTIVE] == 0)
+        ctx->progress.store((float)std::min<uint32_t>(c[C_COUNT], hp.total_items) / (float)hp.total_items);
+        if (c[C_COUNT] >= hp.total_items)
             break;
         if (it > max_iters + 16)
             return fail(ctx, VVPT_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");

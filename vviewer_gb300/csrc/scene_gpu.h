@@ -4,14 +4,13 @@
 #pragma once
 #include <stdint.h>
 
-#ifndef __CUDACC__
-struct alignas(16) float4 { float x, y, z, w; };
-struct alignas(16) int4 { int x, y, z, w; };
-#else
-#include <cuda_runtime.h>
-#endif
+#include <vector_types.h>
 
 namespace vvpt {
+
+// Entries of the single traversal stack (TLAS and BLAS levels together). The
+// scene builder rejects BVHs whose worst-case depth would not fit.
+constexpr int kTraversalStack = 128;
 
 // Binary BVH node, 64 bytes: both children's boxes plus child links, so one
 // node visit is four 128-bit loads. lxy = (l.lo.x, l.hi.x, l.lo.y, l.hi.y),
@@ -131,6 +130,10 @@ struct SceneView {
     const uint8_t *texels;
     int32_t env_texture;       // texture index of the equirect environment, -1 none
     uint32_t has_transparent;  // any material with the transparent flag set
+    // culling-margin bound: over the TLAS instances, the object-space
+    // coordinate magnitude a triangle test sees per unit of world-space ray
+    // direction is at most cull_o * |origin| + cull_r (max-norms)
+    float cull_o, cull_r;
 };
 
 }  // namespace vvpt

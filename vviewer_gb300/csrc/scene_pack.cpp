@@ -1,0 +1,397 @@
+// Host-side scene preparation (scene_pack.h). Validation follows the indices
+// the reference's shaders dereference: MaterialData texture slots
+// (shaders/include/structs.glsl:41-52), InstanceData material / volume ids
+// (src/lib/vengine/core/Instances.hpp:17-35), LightInstance data and
+// instance links (src/lib/vengine/vulkan/VulkanInstances.cpp:66-109).
+#include "scene_pack.h"
+
+#include <vector_functions.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+#include "bvh_build.h"
+
+namespace vvpt {
+
+namespace {
+
+vvpt_status fail(std::string &err, vvpt_status code, const std::string &msg)
+{
+    err = msg;
+    return code;
+}
+
+struct MeshBuild {
+    BVHBuildResult bvh;
+    Box3 root{};
+};
+
+}  // namespace
+
+// column-major 4x4 -> rows of the 3x4 affine part
+void affine_rows(const float m[16], float4 rows[3])
+{
+    for (int r = 0; r < 3; r++)
+        rows[r] = make_float4(m[0 * 4 + r], m[1 * 4 + r], m[2 * 4 + r], m[3 * 4 + r]);
+}
+
+// inverse of the 3x4 affine part in double, rounded to float rows
+bool affine_inverse_rows(const float m[16], float4 rows[3])
+{
+    double a[3][3], t[3];
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++)
+            a[r][c] = m[c * 4 + r];
+        t[r] = m[3 * 4 + r];
+    }
+    double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                 a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    if (!(std::fabs(det) > 0.0))
+        return false;
+    double inv[3][3];
+    inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    for (int r = 0; r < 3; r++) {
+        double tt = -(inv[r][0] * t[0] + inv[r][1] * t[1] + inv[r][2] * t[2]);
+        rows[r] = make_float4((float)inv[r][0], (float)inv[r][1], (float)inv[r][2], (float)tt);
+    }
+    return true;
+}
+
+vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads)
+{
+    out = PackedScene();
+    // ---- validation (indices the shaders would dereference)
+    if ((desc->num_meshes && !desc->meshes) || (desc->num_instances && !desc->instances) ||
+        (desc->num_materials && !desc->materials) || (desc->num_lights && !desc->lights) ||
+        (desc->num_light_data && !desc->light_data) || (desc->num_textures && !desc->textures))
+        return fail(err, VVPT_ERR_INVALID_ARG, "array pointer is null while its count is not zero");
+    for (uint32_t m = 0; m < desc->num_meshes; m++) {
+        const vvpt_mesh_desc &md = desc->meshes[m];
+        if ((md.num_vertices && !md.vertices) || (md.num_triangles && !md.indices))
+            return fail(err, VVPT_ERR_INVALID_ARG, "mesh " + std::to_string(m) + ": null vertex or index array");
+        for (uint64_t i = 0; i < 3ull * md.num_triangles; i++)
+            if (md.indices[i] >= md.num_vertices)
+                return fail(err, VVPT_ERR_INVALID_ARG, "mesh " + std::to_string(m) + ": index out of range");
+    }
+    auto check_tex = [&](uint32_t t) { return t < desc->num_textures; };
+    bool &has_transparent = out.has_transparent;
+    has_transparent = false;
+    for (uint32_t i = 0; i < desc->num_materials; i++) {
+        const vvpt_material &mt = desc->materials[i];
+        for (int k = 0; k < 4; k++) {
+            if (k != 2 && !check_tex(mt.textures2[k]) && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME)
+                return fail(err, VVPT_ERR_INVALID_ARG, "material " + std::to_string(i) + ": texture index out of range");
+            if (!check_tex(mt.textures1[k]) && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME &&
+                !((uint32_t)mt.uv_tiling[2] == VVPT_MATERIAL_LAMBERT && (k == 1 || k == 2)))
+                return fail(err, VVPT_ERR_INVALID_ARG, "material " + std::to_string(i) + ": texture index out of range");
+        }
+        if (mt.metallic_roughness_ao[3] > 0.0f && (uint32_t)mt.uv_tiling[2] != VVPT_MATERIAL_VOLUME)
+            has_transparent = true;
+    }
+    for (uint32_t i = 0; i < desc->num_instances; i++) {
+        const vvpt_instance &in = desc->instances[i];
+        if (!(in.flags & VVPT_INSTANCE_IN_TLAS))
+            continue;
+        if (in.mesh_index >= desc->num_meshes)
+            return fail(err, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": mesh index out of range");
+        if (in.material_index >= desc->num_materials)
+            return fail(err, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": material index out of range");
+        uint32_t mtype = (uint32_t)desc->materials[in.material_index].uv_tiling[2];
+        if (mtype != VVPT_MATERIAL_PBR_STANDARD && mtype != VVPT_MATERIAL_LAMBERT)
+            return fail(err, VVPT_ERR_INVALID_ARG,
+                        "instance " + std::to_string(i) + ": surface material must be PBR standard or Lambert");
+        for (int k = 1; k <= 2; k++) {
+            float v = in.id[k];
+            if (v != -1.0f && !(v >= 0.0f && (uint32_t)v < desc->num_materials))
+                return fail(err, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": volume index out of range");
+        }
+    }
+    for (uint32_t i = 0; i < desc->num_lights; i++) {
+        const vvpt_light_instance &L = desc->lights[i];
+        if (L.info[3] <= 1 && L.info[0] >= desc->num_light_data)
+            return fail(err, VVPT_ERR_INVALID_ARG, "light " + std::to_string(i) + ": light data index out of range");
+        if (L.info[3] == 2) {
+            if (L.info[1] >= desc->num_instances)
+                return fail(err, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": instance out of range");
+            const vvpt_instance &in = desc->instances[L.info[1]];
+            if (in.mesh_index >= desc->num_meshes || in.material_index >= desc->num_materials ||
+                desc->meshes[in.mesh_index].num_triangles == 0)
+                return fail(err, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": instance has no mesh");
+        }
+        if (L.info[3] > 2)
+            return fail(err, VVPT_ERR_UNSUPPORTED, "light " + std::to_string(i) + ": unsupported light type");
+    }
+    for (uint32_t t = 0; t < desc->num_textures; t++) {
+        const vvpt_texture_desc &td = desc->textures[t];
+        if (!td.data || td.width == 0 || td.height == 0 || td.format > VVPT_TEXTURE_RGBA32F)
+            return fail(err, VVPT_ERR_INVALID_ARG, "texture " + std::to_string(t) + ": bad description");
+    }
+
+    // ---- BLAS per mesh (largest first, meshes built in parallel)
+    const uint32_t nm = desc->num_meshes;
+    std::vector<MeshBuild> builds(nm);
+    std::vector<uint32_t> order(nm);
+    for (uint32_t i = 0; i < nm; i++)
+        order[i] = i;
+    std::sort(order.begin(), order.end(),
+              [&](uint32_t a, uint32_t b) { return desc->meshes[a].num_triangles > desc->meshes[b].num_triangles; });
+    std::atomic<uint32_t> next{0};
+    const unsigned hw = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
+    auto worker = [&]() {
+        for (;;) {
+            uint32_t k = next.fetch_add(1);
+            if (k >= nm)
+                break;
+            uint32_t m = order[k];
+            const vvpt_mesh_desc &md = desc->meshes[m];
+            std::vector<Box3> boxes(md.num_triangles);
+            for (uint32_t t = 0; t < md.num_triangles; t++) {
+                Box3 &b = boxes[t];
+                for (int a = 0; a < 3; a++) {
+                    b.lo[a] = INFINITY;
+                    b.hi[a] = -INFINITY;
+                }
+                for (int c = 0; c < 3; c++) {
+                    const float *p = md.vertices[md.indices[3 * t + c]].position;
+                    for (int a = 0; a < 3; a++) {
+                        b.lo[a] = std::min(b.lo[a], p[a]);
+                        b.hi[a] = std::max(b.hi[a], p[a]);
+                    }
+                }
+            }
+            BVHBuildOptions opt;
+            opt.threads = (k == 0 && md.num_triangles > 100000) ? (int)hw : 1;
+            builds[m].bvh = build_bvh2(boxes, opt);
+            Box3 r;
+            for (int a = 0; a < 3; a++) {
+                r.lo[a] = INFINITY;
+                r.hi[a] = -INFINITY;
+            }
+            for (const Box3 &b : boxes)
+                for (int a = 0; a < 3; a++) {
+                    r.lo[a] = std::min(r.lo[a], b.lo[a]);
+                    r.hi[a] = std::max(r.hi[a], b.hi[a]);
+                }
+            builds[m].root = r;
+        }
+    };
+    {
+        std::vector<std::thread> th;
+        unsigned nth = std::min<unsigned>(hw, std::max<uint32_t>(nm, 1));
+        for (unsigned i = 0; i < nth; i++)
+            th.emplace_back(worker);
+        for (auto &t : th)
+            t.join();
+    }
+
+    std::vector<MeshInfo> minfo(nm);
+    std::vector<BVHNode> &nodes = out.nodes;
+    std::vector<TriVerts> &tris = out.tris;
+    std::vector<ShadeVertex> &verts = out.verts;
+    std::vector<uint32_t> &indices = out.indices;
+    size_t total_nodes = 0, total_tris = 0, total_verts = 0;
+    for (uint32_t m = 0; m < nm; m++) {
+        total_nodes += builds[m].bvh.nodes.size();
+        total_tris += desc->meshes[m].num_triangles;
+        total_verts += desc->meshes[m].num_vertices;
+    }
+    nodes.reserve(total_nodes + 2 * desc->num_instances + 2);
+    tris.reserve(total_tris);
+    verts.reserve(total_verts);
+    indices.reserve(3 * total_tris);
+    for (uint32_t m = 0; m < nm; m++) {
+        const vvpt_mesh_desc &md = desc->meshes[m];
+        MeshInfo &mi = minfo[m];
+        mi.node_offset = (uint32_t)nodes.size();
+        mi.tri_offset = (uint32_t)tris.size();
+        mi.vertex_offset = (uint32_t)verts.size();
+        mi.index_offset = (uint32_t)indices.size();
+        mi.num_triangles = md.num_triangles;
+        mi.num_nodes = (uint32_t)builds[m].bvh.nodes.size();
+        nodes.insert(nodes.end(), builds[m].bvh.nodes.begin(), builds[m].bvh.nodes.end());
+        for (uint32_t k = 0; k < md.num_triangles; k++) {
+            uint32_t prim = builds[m].bvh.order[k];
+            TriVerts tv;
+            const float *p0 = md.vertices[md.indices[3 * prim + 0]].position;
+            const float *p1 = md.vertices[md.indices[3 * prim + 1]].position;
+            const float *p2 = md.vertices[md.indices[3 * prim + 2]].position;
+            float pid;
+            std::memcpy(&pid, &prim, 4);
+            tv.v0 = make_float4(p0[0], p0[1], p0[2], pid);
+            tv.v1 = make_float4(p1[0], p1[1], p1[2], 0.0f);
+            tv.v2 = make_float4(p2[0], p2[1], p2[2], 0.0f);
+            tris.push_back(tv);
+        }
+        for (uint32_t v = 0; v < md.num_vertices; v++) {
+            const vvpt_vertex &x = md.vertices[v];
+            ShadeVertex sv;
+            sv.pos_u = make_float4(x.position[0], x.position[1], x.position[2], x.uv[0]);
+            sv.nrm_v = make_float4(x.normal[0], x.normal[1], x.normal[2], x.uv[1]);
+            sv.tan_ = make_float4(x.tangent[0], x.tangent[1], x.tangent[2], 0.0f);
+            verts.push_back(sv);
+        }
+        indices.insert(indices.end(), md.indices, md.indices + 3ull * md.num_triangles);
+    }
+
+    // ---- instances + TLAS
+    const uint32_t ni = desc->num_instances;
+    std::vector<DevInstance> &dinst = out.instances;
+    dinst.assign(ni, DevInstance{});
+    std::vector<Box3> tlas_boxes;
+    std::vector<uint32_t> tlas_ids;
+    for (uint32_t i = 0; i < ni; i++) {
+        const vvpt_instance &in = desc->instances[i];
+        DevInstance &d = dinst[i];
+        std::memset(&d, 0, sizeof(d));
+        affine_rows(in.model, d.o2w);
+        if (!affine_inverse_rows(in.model, d.w2o)) {
+            if (in.flags & VVPT_INSTANCE_IN_TLAS)
+                return fail(err, VVPT_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": singular model matrix");
+        }
+        d.material = in.material_index < desc->num_materials ? in.material_index : 0;
+        d.front_volume = (int32_t)in.id[1];
+        d.back_volume = (int32_t)in.id[2];
+        if (in.mesh_index < nm) {
+            const MeshInfo &mi = minfo[in.mesh_index];
+            d.node_offset = mi.node_offset;
+            d.tri_offset = mi.tri_offset;
+            d.vertex_offset = mi.vertex_offset;
+            d.index_offset = mi.index_offset;
+            d.num_triangles = mi.num_triangles;
+        }
+        if ((in.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh_index < nm && minfo[in.mesh_index].num_triangles > 0) {
+            const Box3 &r = builds[in.mesh_index].root;
+            Box3 w;
+            for (int a = 0; a < 3; a++) {
+                w.lo[a] = INFINITY;
+                w.hi[a] = -INFINITY;
+            }
+            for (int c = 0; c < 8; c++) {
+                double p[3] = {(c & 1) ? r.hi[0] : r.lo[0], (c & 2) ? r.hi[1] : r.lo[1], (c & 4) ? r.hi[2] : r.lo[2]};
+                const float4 *rows = d.o2w;
+                double q[3] = {rows[0].x * p[0] + rows[0].y * p[1] + rows[0].z * p[2] + rows[0].w,
+                               rows[1].x * p[0] + rows[1].y * p[1] + rows[1].z * p[2] + rows[1].w,
+                               rows[2].x * p[0] + rows[2].y * p[1] + rows[2].z * p[2] + rows[2].w};
+                for (int a = 0; a < 3; a++) {
+                    // widen by a few ulps: the box must contain every
+                    // object-space hit mapped back to world space
+                    double pad = 1e-5 * (std::fabs(q[a]) + 1.0);
+                    w.lo[a] = std::min(w.lo[a], (float)(q[a] - pad));
+                    w.hi[a] = std::max(w.hi[a], (float)(q[a] + pad));
+                }
+            }
+            // culling-margin bound (traverse.cuh cull_slack), max-norms:
+            // |o_obj| <= |A^-1| (|o| + |b|), |d_obj| >= |d| / |A|
+            auto row_norm = [](const float4 *m) {
+                double n = 0.0;
+                for (int k = 0; k < 3; k++)
+                    n = std::max(n, (double)std::fabs(m[k].x) + std::fabs(m[k].y) + std::fabs(m[k].z));
+                return n;
+            };
+            const double na = row_norm(d.o2w), ninv = row_norm(d.w2o);
+            const double bt = std::max({std::fabs((double)d.o2w[0].w), std::fabs((double)d.o2w[1].w),
+                                        std::fabs((double)d.o2w[2].w)});
+            double pm = 0.0;
+            for (int a = 0; a < 3; a++)
+                pm = std::max({pm, (double)std::fabs(r.lo[a]), (double)std::fabs(r.hi[a])});
+            out.cull_o = std::max(out.cull_o, (float)(na * ninv));
+            out.cull_r = std::max(out.cull_r, (float)(na * (ninv * bt + pm)));
+            tlas_boxes.push_back(w);
+            tlas_ids.push_back(i);
+        }
+    }
+    // one instance per TLAS leaf: entering an instance costs a BLAS traversal
+    BVHBuildOptions tlas_opt;
+    tlas_opt.max_leaf = 1;
+    BVHBuildResult tlas = build_bvh2(tlas_boxes, tlas_opt);
+    out.tlas_root = (uint32_t)nodes.size();
+    nodes.insert(nodes.end(), tlas.nodes.begin(), tlas.nodes.end());
+    std::vector<uint32_t> &tlas_order = out.tlas_order;
+    tlas_order.resize(tlas.order.size());
+    for (size_t k = 0; k < tlas.order.size(); k++)
+        tlas_order[k] = tlas_ids[tlas.order[k]];
+    {
+        // the traversal stack holds at most two entries per TLAS level, the
+        // instance return marker and one entry per BLAS level
+        int md = 0;
+        for (auto &b : builds)
+            md = std::max(md, b.bvh.depth);
+        out.tlas_depth = tlas.depth;
+        out.max_blas_depth = md;
+        if (2 * tlas.depth + md + 2 > kTraversalStack)
+            return fail(err, VVPT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+    }
+
+    // ---- materials, lights, textures
+    std::vector<DevMaterial> &mats = out.materials;
+    mats.resize(desc->num_materials);
+    static_assert(sizeof(DevMaterial) == sizeof(vvpt_material), "material layout");
+    if (desc->num_materials)
+        std::memcpy(mats.data(), desc->materials, sizeof(vvpt_material) * desc->num_materials);
+    std::vector<DevLightInstance> &lights = out.lights;
+    lights.resize(desc->num_lights);
+    for (uint32_t i = 0; i < desc->num_lights; i++) {
+        const vvpt_light_instance &L = desc->lights[i];
+        DevLightInstance &d = lights[i];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.info, L.info, sizeof(d.info));
+        d.position = make_float4(L.position[0], L.position[1], L.position[2], L.position[3]);
+        d.position1 = make_float4(L.position1[0], L.position1[1], L.position1[2], L.position1[3]);
+        d.position2 = make_float4(L.position2[0], L.position2[1], L.position2[2], L.position2[3]);
+        if (L.info[3] <= 1) {
+            const vvpt_light_data &ld = desc->light_data[L.info[0]];
+            d.color = make_float4(ld.color[0], ld.color[1], ld.color[2], ld.color[3]);
+        } else {
+            // transpose(inverse(M)) for the sampled normal (lightSampling.glsl:80)
+            float m[16] = {L.position[0], L.position1[0], L.position2[0], 0.0f, L.position[1], L.position1[1],
+                           L.position2[1], 0.0f, L.position[2], L.position1[2], L.position2[2], 0.0f,
+                           L.position[3], L.position1[3], L.position2[3], 1.0f};
+            float4 inv[3];
+            if (!affine_inverse_rows(m, inv))
+                return fail(err, VVPT_ERR_INVALID_ARG, "mesh light " + std::to_string(i) + ": singular transform");
+            d.nrm0 = make_float4(inv[0].x, inv[1].x, inv[2].x, 0.0f);
+            d.nrm1 = make_float4(inv[0].y, inv[1].y, inv[2].y, 0.0f);
+            d.nrm2 = make_float4(inv[0].z, inv[1].z, inv[2].z, 0.0f);
+        }
+    }
+    std::vector<DevTexture> &texs = out.textures;
+    std::vector<uint8_t> &texels = out.texels;
+    auto add_texture = [&](const vvpt_texture_desc &td) {
+        DevTexture t{};
+        t.width = td.width;
+        t.height = td.height;
+        t.format = td.format;
+        size_t texel_bytes = td.format == VVPT_TEXTURE_RGBA32F ? 16 : 4;
+        size_t off = (texels.size() + 15) & ~size_t(15);
+        texels.resize(off + texel_bytes * td.width * td.height);
+        std::memcpy(texels.data() + off, td.data, texel_bytes * td.width * td.height);
+        t.offset = off;
+        texs.push_back(t);
+    };
+    for (uint32_t t = 0; t < desc->num_textures; t++)
+        add_texture(desc->textures[t]);
+    int &env_index = out.env_texture;
+    env_index = -1;
+    if (desc->environment) {
+        if (!desc->environment->data || desc->environment->format != VVPT_TEXTURE_RGBA32F)
+            return fail(err, VVPT_ERR_INVALID_ARG, "environment must be an RGBA32F equirectangular image");
+        env_index = (int)texs.size();
+        add_texture(*desc->environment);
+    }
+
+    return VVPT_OK;
+}
+
+}  // namespace vvpt

@@ -1,0 +1,45 @@
+// Host-side scene preparation: validates a vvpt_scene_desc and packs it into
+// the device layout of scene_gpu.h (BLAS per mesh, TLAS over the instances,
+// leaf-ordered triangles, shading vertices, materials, lights, texel pool).
+// The arrays are uploaded as they are by vvpt_scene_upload; nothing here
+// touches the GPU, so the packed scene can also be inspected on the host.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/vvpt.h"
+#include "scene_gpu.h"
+
+namespace vvpt {
+
+struct PackedScene {
+    std::vector<BVHNode> nodes;       // every BLAS, then the TLAS
+    std::vector<TriVerts> tris;       // leaf order per BLAS
+    std::vector<ShadeVertex> verts;
+    std::vector<uint32_t> indices;    // original triangle order
+    std::vector<DevInstance> instances;
+    std::vector<uint32_t> tlas_order; // TLAS leaf order -> instance slot
+    uint32_t tlas_root = 0;
+    std::vector<DevMaterial> materials;
+    std::vector<DevLightInstance> lights;
+    std::vector<DevTexture> textures;
+    std::vector<uint8_t> texels;
+    int32_t env_texture = -1;
+    bool has_transparent = false;
+    float cull_o = 0.0f, cull_r = 0.0f; // SceneView culling-margin bound
+    int tlas_depth = 0;
+    int max_blas_depth = 0;
+};
+
+// Returns VVPT_OK or an error status with `err` set. `threads` = 0 uses every
+// hardware thread for the BLAS builds.
+vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads = 0);
+
+// Row form of the 3x4 affine part of a column-major 4x4 matrix, and of its
+// inverse (computed in double, rounded to float). False when singular.
+void affine_rows(const float m[16], float4 rows[3]);
+bool affine_inverse_rows(const float m[16], float4 rows[3]);
+
+}  // namespace vvpt

@@ -19,8 +19,6 @@
 namespace vvpt {
 
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
-constexpr int kTlasStack = 32;
-constexpr int kBlasStack = 64;
 // device status word bits
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrLoopCap = 2u;
@@ -151,12 +149,27 @@ __device__ __forceinline__ void box2(const BVHNode &n, const float3 &o, const fl
 
 // Culling bounds with slack. A node is skipped when its entry distance lies
 // beyond the current best hit. The slab distances and the triangle test's t
-// carry independent rounding errors of a few ulps, so for a triangle on a
-// node's face (coplanar geometry, axis-aligned walls) the computed entry can
-// exceed the computed hit t; a relative margin of 1e-5 keeps such nodes (and
-// equal-t ties, which the (instance, primitive) order resolves) in the search.
-__device__ __forceinline__ float cull_far(float best_t) { return best_t * (1.0f + 1e-5f) + 1e-30f; }
-__device__ __forceinline__ float cull_near(float tmin) { return tmin - fabsf(tmin) * 1e-5f; }
+// carry independent rounding errors, so for a triangle on a node's face
+// (coplanar geometry, axis-aligned walls) the computed entry can exceed the
+// computed hit t. Two margins keep such nodes (and equal-t ties, which the
+// (instance, primitive) order resolves) in the search: 1e-5 relative to t, and
+// an absolute one for hits close to the ray origin, where the triangle's t is
+// a difference of coordinates far larger than t itself and its error is about
+// machine epsilon times those coordinates over |d| (cull_slack).
+__device__ __forceinline__ float cull_far(float best_t, float slack)
+{
+    return best_t * (1.0f + 1e-5f) + slack + 1e-30f;
+}
+__device__ __forceinline__ float cull_near(float tmin, float slack) { return tmin - fabsf(tmin) * 1e-5f - slack; }
+// Absolute culling margin of one ray: 1e-5 (about 160 ulps) times the largest
+// object-space coordinate magnitude a triangle test of this scene can see,
+// bounded per instance on the host (SceneView::cull_o, cull_r), over |d|.
+__device__ __forceinline__ float cull_slack(const SceneView &s, const float3 &o, const float3 &d)
+{
+    const float om = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    const float dm = fmaxf(fmaxf(fabsf(d.x), fabsf(d.y)), fabsf(d.z));
+    return dm > 0.0f ? 1e-5f * (s.cull_o * om + s.cull_r) / dm : 0.0f;
+}
 
 __device__ __forceinline__ BVHNode load_node(const BVHNode *nodes, int idx)
 {
@@ -194,94 +207,16 @@ __device__ __forceinline__ float3 wt_xform_vector(const float4 *rows, const floa
     return r;
 }
 
-// Walks one BLAS in object space, updating `best`. Returns false on stack overflow.
-__device__ __forceinline__ bool traverse_blas(const SceneView &s, const DevInstance &inst, uint32_t inst_id,
-                                              const float3 &o, const float3 &d, float tmin, const Hit &after, Hit &best)
-{
-    const float3 invd = safe_inv(d);
-    const WatertightRay wr = wt_setup(o, d);
-    const BVHNode *nodes = s.nodes + inst.node_offset;
-    const TriVerts *tris = s.tris + inst.tri_offset;
-    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t));
-    int stack[kBlasStack];
-    int sp = 0;
-    int node = 0;
-    for (;;) {
-        BVHNode n = load_node(nodes, node);
-        float tl, tr;
-        box2(n, o, invd, box_tmin, cull_far(best.t), tl, tr);
-        int next = -1;
-        // leaves are intersected right away; internal children are descended
-        // nearest first
-        int push[2];
-        float pusht[2];
-        int np = 0;
-        const bool hl = tl <= cull_far(best.t) && n.c.x >= 0;
-        const bool hr = tr <= cull_far(best.t) && n.c.y >= 0;
-        if (hl) {
-            if (n.c.z > 0) {
-                for (int k = n.c.x; k < n.c.x + n.c.z; k++) {
-                    const float4 *tp = reinterpret_cast<const float4 *>(tris + k);
-                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-                    float t, u, v;
-                    uint32_t prim = __float_as_uint(p0.w);
-                    if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
-                        is_after(t, inst_id, prim, after)) {
-                        best.t = t;
-                        best.u = u;
-                        best.v = v;
-                        best.inst = inst_id;
-                        best.prim = prim;
-                    }
-                }
-            } else {
-                push[np] = n.c.x;
-                pusht[np++] = tl;
-            }
-        }
-        if (hr) {
-            if (n.c.w > 0) {
-                for (int k = n.c.y; k < n.c.y + n.c.w; k++) {
-                    const float4 *tp = reinterpret_cast<const float4 *>(tris + k);
-                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-                    float t, u, v;
-                    uint32_t prim = __float_as_uint(p0.w);
-                    if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
-                        is_after(t, inst_id, prim, after)) {
-                        best.t = t;
-                        best.u = u;
-                        best.v = v;
-                        best.inst = inst_id;
-                        best.prim = prim;
-                    }
-                }
-            } else {
-                push[np] = n.c.y;
-                pusht[np++] = tr;
-            }
-        }
-        if (np == 2) {
-            int nearc = pusht[0] <= pusht[1] ? push[0] : push[1];
-            int farc = pusht[0] <= pusht[1] ? push[1] : push[0];
-            if (sp >= kBlasStack)
-                return false;
-            stack[sp++] = farc;
-            next = nearc;
-        } else if (np == 1) {
-            next = push[0];
-        }
-        if (next < 0) {
-            if (sp == 0)
-                break;
-            next = stack[--sp];
-        }
-        node = next;
-    }
-    return true;
-}
-
 // Closest hit over all TLAS instances among candidates strictly after
-// `after`. `err` receives status bits.
+// `after`, as one flat loop over a single stack. Every loop step is one of:
+// a triangle test, a node visit (both children's boxes), or a stack
+// transition (enter an instance: transform the ray into its object space and
+// push a return marker; pop the marker: back to the world-space ray). Keeping
+// the two levels in one loop keeps a warp's lanes in step: a lane inside an
+// instance never holds lanes that are still in the TLAS, as nested per-level
+// loops would. `err` receives status bits.
+constexpr int kTagNode = 0, kTagLeaf = 1, kTagInst = 2, kTagReturn = 3;
+
 __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
                                            const Hit &after, uint32_t &err)
 {
@@ -290,62 +225,113 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     best.u = best.v = 0.0f;
     best.inst = kNoHit;
     best.prim = kNoHit;
-    const float3 invd = safe_inv(d);
-    const BVHNode *nodes = s.nodes + s.tlas_root;
-    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t));
-    int stack[kTlasStack];
+    const float slack = cull_slack(s, o, d);
+    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t), slack);
+    const float3 winvd = safe_inv(d);
+    // current level: the TLAS (world ray) or one instance's BLAS (object ray)
+    float3 co = o, cinvd = winvd;
+    WatertightRay wr = wt_setup(o, d);
+    uint32_t inst_id = kNoHit;
+    uint32_t node_base = s.tlas_root, tri_base = 0;
+    bool in_blas = false;
+    int node = 0;                 // inner node to visit (local index), -1 none
+    int leaf_first = 0, leaf_count = 0; // triangles still to test (local indices)
+    int2 stack[kTraversalStack];
     int sp = 0;
-    int node = 0;
+    auto push = [&](int value, int tag, int count) {
+        if (sp < kTraversalStack)
+            stack[sp++] = make_int2(value, (tag << 28) | count);
+        else
+            err |= kErrStackOverflow;
+    };
     for (;;) {
-        BVHNode n = load_node(nodes, node);
-        float tl, tr;
-        box2(n, o, invd, box_tmin, cull_far(best.t), tl, tr);
-        int push[2];
-        float pusht[2];
-        int np = 0;
-        const bool hl = tl <= cull_far(best.t) && n.c.x >= 0;
-        const bool hr = tr <= cull_far(best.t) && n.c.y >= 0;
+        if (leaf_count > 0) {
+            const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
+            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            const uint32_t prim = __float_as_uint(p0.w);
+            float t, u, v;
+            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
+                is_after(t, inst_id, prim, after)) {
+                best.t = t;
+                best.u = u;
+                best.v = v;
+                best.inst = inst_id;
+                best.prim = prim;
+            }
+            leaf_first++;
+            leaf_count--;
+            continue;
+        }
+        if (node >= 0) {
+            const BVHNode n = load_node(s.nodes, (int)node_base + node);
+            float tl, tr;
+            const float far_t = cull_far(best.t, slack);
+            box2(n, co, cinvd, box_tmin, far_t, tl, tr);
+            const bool hl = tl <= far_t && n.c.x >= 0;
+            const bool hr = tr <= far_t && n.c.y >= 0;
+            // near child first
+            const bool swap = hl && hr && tr < tl;
+            int next = -1;
 #pragma unroll
-        for (int side = 0; side < 2; side++) {
-            const bool h = side == 0 ? hl : hr;
-            const int idx = side == 0 ? n.c.x : n.c.y;
-            const int cnt = side == 0 ? n.c.z : n.c.w;
-            if (!h)
-                continue;
-            if (cnt > 0) {
-                for (int k = idx; k < idx + cnt; k++) {
-                    uint32_t id = __ldg(s.tlas_order + k);
-                    const DevInstance &inst = s.instances[id];
-                    float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
-                    float3 oo = wt_xform_point(rows, o);
-                    float3 od = wt_xform_vector(rows, d);
-                    if (!traverse_blas(s, inst, id, oo, od, tmin, after, best))
-                        err |= kErrStackOverflow;
+            for (int k = 0; k < 2; k++) {
+                const bool right = (k == 0) == swap;
+                const bool h = right ? hr : hl;
+                if (!h)
+                    continue;
+                const int idx = right ? n.c.y : n.c.x;
+                const int cnt = right ? n.c.w : n.c.z;
+                if (cnt == 0) {
+                    if (next < 0)
+                        next = idx;
+                    else
+                        push(idx, kTagNode, 0);
+                } else if (in_blas) {
+                    if (leaf_count == 0) {
+                        leaf_first = idx;
+                        leaf_count = cnt;
+                    } else {
+                        push(idx, kTagLeaf, cnt);
+                    }
+                } else {
+                    push(idx, kTagInst, cnt);
                 }
-            } else {
-                push[np] = idx;
-                pusht[np++] = side == 0 ? tl : tr;
             }
+            node = next;
+            continue;
         }
-        int next = -1;
-        if (np == 2) {
-            int nearc = pusht[0] <= pusht[1] ? push[0] : push[1];
-            int farc = pusht[0] <= pusht[1] ? push[1] : push[0];
-            if (sp >= kTlasStack) {
-                err |= kErrStackOverflow;
-                break;
-            }
-            stack[sp++] = farc;
-            next = nearc;
-        } else if (np == 1) {
-            next = push[0];
+        if (sp == 0)
+            break;
+        const int2 e = stack[--sp];
+        const int tag = (int)((unsigned)e.y >> 28);
+        const int cnt = e.y & 0x0FFFFFFF;
+        if (tag == kTagNode) {
+            node = e.x;
+        } else if (tag == kTagLeaf) {
+            leaf_first = e.x;
+            leaf_count = cnt;
+        } else if (tag == kTagInst) {
+            if (cnt > 1)
+                push(e.x + 1, kTagInst, cnt - 1);
+            inst_id = __ldg(s.tlas_order + e.x);
+            const DevInstance &inst = s.instances[inst_id];
+            const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
+            co = wt_xform_point(rows, o);
+            const float3 cd = wt_xform_vector(rows, d);
+            cinvd = safe_inv(cd);
+            wr = wt_setup(co, cd);
+            node_base = inst.node_offset;
+            tri_base = inst.tri_offset;
+            in_blas = true;
+            push(0, kTagReturn, 0);
+            node = 0;
+        } else {
+            // back to the TLAS
+            co = o;
+            cinvd = winvd;
+            node_base = s.tlas_root;
+            in_blas = false;
+            inst_id = kNoHit;
         }
-        if (next < 0) {
-            if (sp == 0)
-                break;
-            next = stack[--sp];
-        }
-        node = next;
     }
     return best;
 }

@@ -238,18 +238,57 @@ __device__ __forceinline__ float3 medium_transmittance(const SceneView &s, uint3
 // ---------------------------------------------------------------------------
 // Kernels
 
-__global__ void k_init_slots(Queues q, PathState ps, uint32_t slots)
+__global__ void k_init_slots(Queues q, PathState ps, JobTable jt, uint32_t slots)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
         q.regen[0][i] = i;
         ps.flags[i] = 0u;
         ps.item[i] = 0xFFFFFFFFu;
+        ps.job[i] = 0u;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int c = 0; c < C_COUNT; c++)
             q.counters[c] = 0u;
         q.counters[C_REGEN0] = slots;
+        *jt.next_item = 0ull;
+        *jt.idle_count = 0u;
     }
+}
+
+// New work for idle slots (see launch_admit). One block: the counters it
+// resets are read by all of its threads first.
+__global__ void k_admit(Queues q, JobTable jt, unsigned long long total_items, uint32_t num_ranges)
+{
+    const uint32_t n = *jt.idle_count;
+    const uint32_t base = q.counters[C_REGEN0];
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        q.regen[0][base + i] = jt.idle[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // hand-out attempts past the old end claimed nothing
+        const unsigned long long old_total = *jt.total_items;
+        if (*jt.next_item > old_total)
+            *jt.next_item = old_total;
+        *jt.total_items = total_items;
+        *jt.num_ranges = num_ranges;
+        q.counters[C_REGEN0] = base + n;
+        *jt.idle_count = 0u;
+    }
+}
+
+// Hand-out range holding global work item g (the last range beginning at or
+// before g).
+__device__ __forceinline__ uint32_t find_range(const JobTable &jt, uint32_t num_ranges, unsigned long long g)
+{
+    uint32_t lo = 0, hi = num_ranges;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jt.range_begin[mid] <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
 __global__ void k_begin(Queues q, int pp)
@@ -267,17 +306,18 @@ __global__ void k_begin(Queues q, int pp)
 
 // Finalizes finished samples, hands out work items, and generates camera
 // rays (raygen.rgen.glsl:24-99, 126-129).
-__global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
-                                               Queues q, BatchResults br, int pp)
+__global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues q, int pp)
 {
-    const RenderParams &p = *pp_;
     const uint32_t n = q.counters[C_REGEN0 + pp];
     const uint32_t *queue = q.regen[pp];
+    const unsigned long long total_items = *jt.total_items;
+    const uint32_t num_ranges = *jt.num_ranges;
     // per-slot body; returns true when the slot emits a camera ray
     auto body = [&](const uint32_t slot) -> bool {
         uint32_t flags = ps.flags[slot];
         uint32_t sample = ps.sample[slot];
         uint32_t item = ps.item[slot];
+        uint32_t job = ps.job[slot];
         float3 cr, ca, cn;
         if (flags & F_ITEM) {
             cr = f3(ps.cum_rad[slot]);
@@ -287,7 +327,7 @@ __global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *
             cr = ca = cn = f3(0.0f);
         }
         if (flags & F_DONE) {
-            const float total = (float)p.total_samples;
+            const float total = (float)jt.jobs[job].params.total_samples;
             cr += f3(ps.rad[slot]) / total;
             ca += f3(ps.alb[slot]) / total;
             cn += f3(ps.nrm[slot]) / total;
@@ -295,26 +335,34 @@ __global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *
             atomicAdd(&q.counters[C_PATHS], 1u);
         }
         bool fresh = false;
-        if ((flags & F_ITEM) && sample >= p.batch_size) {
+        if ((flags & F_ITEM) && sample >= jt.jobs[job].params.batch_size) {
+            const BatchResults br = jt.jobs[job].results;
             br.rad[item] = f4(cr, 1.0f);
             br.alb[item] = f4(ca, 1.0f);
             br.nrm[item] = f4(cn, 1.0f);
             flags &= ~F_ITEM;
             atomicSub(&q.counters[C_ACTIVE], 1u);
+            __threadfence();
+            atomicAdd(&jt.item_done[job], 1u);
         }
         if (!(flags & F_ITEM)) {
-            item = atomicAdd(&q.counters[C_NEXT_ITEM], 1u);
-            if (item >= p.total_items) {
+            const unsigned long long g = atomicAdd(jt.next_item, 1ull);
+            if (g >= total_items) {
                 ps.flags[slot] = 0u;
                 ps.item[slot] = 0xFFFFFFFFu;
+                jt.idle[atomicAdd(jt.idle_count, 1u)] = slot;
                 return false;
             }
+            const uint32_t r = find_range(jt, num_ranges, g);
+            job = jt.range_job[r];
+            item = (uint32_t)(g - jt.range_begin[r]);
             atomicAdd(&q.counters[C_ACTIVE], 1u);
             flags = F_ITEM;
             sample = 0;
             fresh = true;
             cr = ca = cn = f3(0.0f);
         }
+        const RenderParams &p = jt.jobs[job].params;
         const uint32_t npix = p.width * p.height;
         const uint32_t batch = item / npix;
         const uint32_t pix = item - batch * npix;
@@ -367,6 +415,7 @@ __global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *
         ps.vol[slot] = (uint32_t)p.cam_volume;
         ps.item[slot] = item;
         ps.sample[slot] = sample;
+        ps.job[slot] = job;
         return true;
     };
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -385,7 +434,7 @@ __global__ void __launch_bounds__(256) k_regen(SceneView s, const RenderParams *
 
 // Closest hit for every queued extension ray; hits are binned by material
 // model into the shade queues (material-sorted shading).
-__global__ void __launch_bounds__(256) k_extend(SceneView s, PathState ps, Queues q, int pp)
+__global__ void __launch_bounds__(256) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
@@ -395,6 +444,7 @@ __global__ void __launch_bounds__(256) k_extend(SceneView s, PathState ps, Queue
     // shade bin is written per queue entry and compacted by k_partition.
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = queue[i];
+        const SceneView &s = jt.jobs[ps.job[slot]].scene;
         const float3 o = f3(ps.o[slot]);
         const float3 d = f3(ps.d[slot]);
         const uint32_t flags = ps.flags[slot];
@@ -464,13 +514,15 @@ __device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams 
 // The pending emitter rays whose first candidate is transparent (or below the
 // extension ray's tmin): the full candidate walk, before shade adds this
 // iteration's contributions.
-__global__ void __launch_bounds__(256) k_walk(SceneView s, const RenderParams *__restrict__ pp_, PathState ps, Queues q)
+__global__ void __launch_bounds__(256) k_walk(JobTable jt, PathState ps, Queues q)
 {
-    const RenderParams &p = *pp_;
     const uint32_t n = q.counters[C_WALK];
     uint32_t err = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = q.walk[i];
+        const JobView &J = jt.jobs[ps.job[slot]];
+        const SceneView &s = J.scene;
+        const RenderParams &p = J.params;
         const uint32_t flags = ps.flags[slot];
         const float4 nb = ps.nee_b[slot];
         float3 emT, T, em;
@@ -524,10 +576,8 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 // One shading event per queued path: the body of rayPrimary*.rchit.glsl:45-175
 // (hits) or rayPrimary.rmiss.glsl:40-106 (misses), followed by Russian
 // roulette (russian_roulette.glsl:1-11).
-__global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *__restrict__ pp_, PathState ps, Queues q,
-                                               int pp)
+__global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues q, int pp)
 {
-    const RenderParams &p = *pp_;
     const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
     const uint32_t n = nl + np + nm;
     uint32_t err = 0, walks = 0;
@@ -542,6 +592,9 @@ __global__ void __launch_bounds__(256) k_shade(SceneView s, const RenderParams *
             slot = q.shade_p[i - nl];
         else
             slot = q.shade_m[i - nl - np];
+        const JobView &J = jt.jobs[ps.job[slot]];
+        const SceneView &s = J.scene;
+        const RenderParams &p = J.params;
 
         uint32_t flags = ps.flags[slot];
         uint32_t rng = ps.rng[slot];
@@ -1104,10 +1157,8 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 }
 
 // Shadow rays of the events shaded this iteration.
-__global__ void __launch_bounds__(256) k_shadow(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
-                                                Queues q)
+__global__ void __launch_bounds__(256) k_shadow(JobTable jt, PathState ps, Queues q)
 {
-    const RenderParams &p = *pp_;
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
     uint32_t nsh = 0;
@@ -1116,6 +1167,9 @@ __global__ void __launch_bounds__(256) k_shadow(SceneView s, const RenderParams 
         const uint32_t flags = ps.flags[slot];
         if (!(flags & F_SHADOW))
             continue;
+        const JobView &J = jt.jobs[ps.job[slot]];
+        const SceneView &s = J.scene;
+        const RenderParams &p = J.params;
         const float4 sd = ps.sh_dir[slot];
         const float3 T = shadow_transmittance(s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
                                               ps.vol[slot], err);
@@ -1132,10 +1186,8 @@ __global__ void __launch_bounds__(256) k_shadow(SceneView s, const RenderParams 
 
 // BSDF-direction emitter rays of paths that end at this event (their next
 // extension ray is never traced, so the emitter ray cannot ride on it).
-__global__ void __launch_bounds__(256) k_emitter(SceneView s, const RenderParams *__restrict__ pp_, PathState ps,
-                                                 Queues q)
+__global__ void __launch_bounds__(256) k_emitter(JobTable jt, PathState ps, Queues q)
 {
-    const RenderParams &p = *pp_;
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
     uint32_t nnee = 0;
@@ -1144,6 +1196,9 @@ __global__ void __launch_bounds__(256) k_emitter(SceneView s, const RenderParams
         const uint32_t flags = ps.flags[slot];
         if (!(flags & F_NEE))
             continue;
+        const JobView &J = jt.jobs[ps.job[slot]];
+        const SceneView &s = J.scene;
+        const RenderParams &p = J.params;
         const float4 nb = ps.nee_b[slot];
         float3 emT, T, em;
         float lpdf;
@@ -1202,46 +1257,52 @@ __global__ void k_trace_closest(SceneView s, const float4 *rays, uint32_t n, flo
 // ---------------------------------------------------------------------------
 // Host launchers
 
-void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cudaStream_t stream)
+void launch_init_slots(const Queues &q, const PathState &ps, const JobTable &jt, uint32_t slots, cudaStream_t stream)
 {
     int grid = (int)std::min<uint32_t>((slots + 255) / 256, 65535u);
-    k_init_slots<<<grid, 256, 0, stream>>>(q, ps, slots);
+    k_init_slots<<<grid, 256, 0, stream>>>(q, ps, jt, slots);
 }
 
-void launch_iteration(const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
-                      const BatchResults &br, int pp, const LaunchShape &shape, cudaStream_t stream)
+void launch_admit(const Queues &q, const JobTable &jt, unsigned long long total_items, uint32_t num_ranges,
+                  cudaStream_t stream)
+{
+    k_admit<<<1, 1024, 0, stream>>>(q, jt, total_items, num_ranges);
+}
+
+void launch_iteration(const JobTable &jt, const PathState &ps, const Queues &q, int pp, const LaunchShape &shape,
+                      cudaStream_t stream)
 {
     for (int k = 0; k < K_NUM; k++)
-        launch_kernel((KernelId)k, s, dparams, ps, q, br, pp, shape, stream);
+        launch_kernel((KernelId)k, jt, ps, q, pp, shape, stream);
 }
 
-void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
-                   const BatchResults &br, int pp, const LaunchShape &shape, cudaStream_t stream)
+void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Queues &q, int pp,
+                   const LaunchShape &shape, cudaStream_t stream)
 {
     switch (k) {
     case K_BEGIN:
         k_begin<<<1, 32, 0, stream>>>(q, pp);
         break;
     case K_REGEN:
-        k_regen<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, br, pp);
+        k_regen<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
         break;
     case K_EXTEND:
-        k_extend<<<shape.grid, shape.block, 0, stream>>>(s, ps, q, pp);
+        k_extend<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
         break;
     case K_PARTITION:
         k_partition<<<shape.grid, shape.block, 0, stream>>>(ps, q, pp);
         break;
     case K_WALK:
-        k_walk<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        k_walk<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
         break;
     case K_SHADE:
-        k_shade<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q, pp);
+        k_shade<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
         break;
     case K_SHADOW:
-        k_shadow<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        k_shadow<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
         break;
     case K_EMITTER:
-        k_emitter<<<shape.grid, shape.block, 0, stream>>>(s, dparams, ps, q);
+        k_emitter<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
         break;
     default:
         break;

@@ -49,8 +49,9 @@ struct PathState {
     uint32_t *rng;
     uint32_t *flags;
     uint32_t *vol;
-    uint32_t *item;
+    uint32_t *item;   // work item within its job: batch * width * height + pixel
     uint32_t *sample;
+    uint32_t *job;    // index into the job table
 };
 
 enum CounterIndex {
@@ -92,6 +93,30 @@ struct BatchResults {
     float4 *nrm;
 };
 
+// One render job: its scene, its parameters and its per-batch sums. The
+// table holds one per job slot; a slot is reused once its job has finished.
+struct JobView {
+    SceneView scene;
+    RenderParams params;
+    BatchResults results;
+};
+
+// Work items of all admitted jobs form one global sequence, handed out in
+// admission order: global item range_begin[r] + i is work item i of job slot
+// range_job[r] (ranges ascending). Fused per stage, every queue holds paths of
+// all live jobs; a path finds its job through ps.job.
+struct JobTable {
+    const JobView *jobs;                   // per job slot
+    const unsigned long long *range_begin; // per hand-out range, ascending
+    const uint32_t *range_job;
+    uint32_t *item_done;                   // per job slot: work items finished
+    unsigned long long *next_item;         // next global work item to hand out
+    unsigned long long *total_items;       // end of the last range
+    uint32_t *num_ranges;
+    uint32_t *idle;                        // slots that found no work
+    uint32_t *idle_count;
+};
+
 struct LaunchShape {
     int grid;
     int block;
@@ -99,11 +124,20 @@ struct LaunchShape {
 
 // Kernel launchers (wavefront.cu). Each reads its work count from `counters`,
 // so a sequence of them can be captured in a CUDA graph.
-void launch_iteration(const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
-                      const BatchResults &br, int pingpong, const LaunchShape &shape, cudaStream_t stream);
+void launch_iteration(const JobTable &jt, const PathState &ps, const Queues &q, int pingpong, const LaunchShape &shape,
+                      cudaStream_t stream);
 void launch_reduce(const RenderParams &hparams, const BatchResults &br, float4 *radiance, float4 *albedo,
                    float4 *normal, float4 *radiance_m2, cudaStream_t stream);
-void launch_init_slots(const Queues &q, const PathState &ps, uint32_t slots, cudaStream_t stream);
+// Resets counters, the job table counters and puts every slot on the first
+// regeneration queue (its flags cleared).
+void launch_init_slots(const Queues &q, const PathState &ps, const JobTable &jt, uint32_t slots, cudaStream_t stream);
+// Admits work: raises the global item count to `total_items` over
+// `num_ranges` hand-out ranges (after work items ran out, the hand-out counter
+// is brought back to the old total) and returns idle slots to the first
+// regeneration queue. Launched between graph replays, stream-ordered, after
+// the range arrays were written.
+void launch_admit(const Queues &q, const JobTable &jt, unsigned long long total_items, uint32_t num_ranges,
+                  cudaStream_t stream);
 void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, float4 *hits_tuv, uint32_t *hits_ids,
                           uint32_t *err, cudaStream_t stream);
 // One wavefront kernel, launched on its own (profiling mode); an iteration
@@ -120,8 +154,8 @@ enum KernelId {
     K_NUM = 8
 };
 constexpr int kKernelsPerIteration = K_NUM;
-void launch_kernel(KernelId k, const SceneView &s, const RenderParams *dparams, const PathState &ps, const Queues &q,
-                   const BatchResults &br, int pingpong, const LaunchShape &shape, cudaStream_t stream);
+void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Queues &q, int pingpong,
+                   const LaunchShape &shape, cudaStream_t stream);
 
 // Algorithmic bytes per work unit of each kernel: the path-state, queue and
 // hit-record loads and stores the kernel's code performs for one queue entry

@@ -94,6 +94,15 @@ class Context:
                  "total_ms": float(k.total_ms), "bytes_per_unit": float(k.bytes_per_unit)}
                 for k in p.kernels[:p.count]]
 
+    def set_budget(self, nbytes: int) -> None:
+        """Device-memory budget of the job engine (0: no limit)."""
+        self.check(self.lib.vvpt_set_budget(self.handle, int(nbytes)))
+
+    def engine_stats(self) -> N.EngineStats:
+        es = N.EngineStats()
+        self.check(self.lib.vvpt_engine_stats_get(self.handle, C.byref(es)))
+        return es
+
     def set_stream(self, cuda_stream: int | None) -> None:
         """Runs the context's work on a caller-owned CUDA stream (None: its own)."""
         self.check(self.lib.vvpt_set_stream(self.handle, cuda_stream or None))
@@ -108,8 +117,10 @@ class GpuScene:
         self.flat = flat
 
     def release(self) -> None:
+        """Frees the device copy; raises (VVPT_ERR_NOT_READY) while
+        submitted jobs still use the scene."""
         if self.handle:
-            self.ctx.lib.vvpt_scene_release(self.ctx.handle, self.handle)
+            self.ctx.check(self.ctx.lib.vvpt_scene_release(self.ctx.handle, self.handle))
             self.handle = None
 
     def __del__(self):
@@ -153,6 +164,31 @@ class GpuScene:
                                                 C.byref(o)))
         return RenderResult(rad, alb, nrm, m2, self.ctx.stats(), info.samples // info.batch_size)
 
+    def submit(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
+               outputs: dict | None = None) -> "Job":
+        """Queues a render on the context's job engine (vvpt_submit). Outputs go
+        to new host arrays, or to device pointers when `outputs` maps
+        radiance/albedo/normal/radiance_m2 to device addresses."""
+        flags = N.RENDER_WANT_BATCH_M2 if want_m2 else 0
+        ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
+        job = Job(self, info, want_m2)
+        if outputs is not None:
+            o = N.Outputs(outputs.get("radiance"), outputs.get("albedo"), outputs.get("normal"),
+                          outputs.get("radiance_m2"), 1)
+        else:
+            H, W = info.height, info.width
+            job.radiance = np.zeros((H, W, 4), dtype=np.float32)
+            job.albedo = np.zeros((H, W, 4), dtype=np.float32)
+            job.normal = np.zeros((H, W, 4), dtype=np.float32)
+            job.radiance_m2 = np.zeros((H, W, 4), dtype=np.float32) if want_m2 else None
+            o = N.Outputs(job.radiance.ctypes.data, job.albedo.ctypes.data, job.normal.ctypes.data,
+                          job.radiance_m2.ctypes.data if want_m2 else None, 0)
+        jid = C.c_uint64()
+        self.ctx.check(self.ctx.lib.vvpt_submit(self.ctx.handle, self.handle, C.byref(scene_data), C.byref(ri),
+                                                C.byref(o), C.byref(jid)))
+        job.id = int(jid.value)
+        return job
+
     def trace_closest(self, rays: np.ndarray) -> np.ndarray:
         """rays: N x 8 float32 (origin, tmin, direction, tmax) -> structured hits."""
         rays = np.ascontiguousarray(rays, dtype=np.float32)
@@ -161,6 +197,45 @@ class GpuScene:
         self.ctx.check(self.ctx.lib.vvpt_trace_closest(self.ctx.handle, self.handle, rays.ctypes.data, n,
                                                        hits.ctypes.data, 0))
         return hits
+
+
+class Job:
+    """A render submitted to the job engine; its host outputs (if any) are
+    filled when the job is done."""
+
+    def __init__(self, scene: GpuScene, info: RenderInfo, want_m2: bool):
+        self.scene = scene
+        self.ctx = scene.ctx
+        self.info = info
+        self.want_m2 = want_m2
+        self.id = 0
+        self.radiance = self.albedo = self.normal = self.radiance_m2 = None
+
+    def poll(self) -> N.JobInfo:
+        ji = N.JobInfo()
+        self.ctx.check(self.ctx.lib.vvpt_poll(self.ctx.handle, self.id, C.byref(ji)))
+        return ji
+
+    def done(self) -> bool:
+        return self.poll().state in (N.JOB_DONE, N.JOB_FAILED)
+
+    def wait(self, timeout_ms: float = -1.0) -> bool:
+        """True when done; False on timeout; raises if the job failed."""
+        st = self.ctx.lib.vvpt_wait(self.ctx.handle, self.id, float(timeout_ms))
+        if st == N.TIMEOUT:
+            return False
+        self.ctx.check(st)
+        return True
+
+    def result(self) -> RenderResult:
+        self.wait()
+        return RenderResult(self.radiance, self.albedo, self.normal, self.radiance_m2, None,
+                            self.info.samples // self.info.batch_size)
+
+    def release(self) -> None:
+        if self.id:
+            self.ctx.check(self.ctx.lib.vvpt_job_release(self.ctx.handle, self.id))
+            self.id = 0
 
 
 HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), ("instance", np.uint32),
