@@ -53,6 +53,13 @@ def workload(name: str):
                 "spp": info.samples, "depth": info.depth, "batch_size": info.batch_size,
                 "triangles": 998596, "medium": {"sigma_a": 0.05, "sigma_s": 0.2, "g": 0.0},
                 "materials": "Lambert walls, metallic/roughness spheres", "seed": 1}
+    elif name == "instanced_sky":
+        engine, info = scenes.instanced_sky_scene(seed=1)
+        desc = {"workload": "instanced_sky_4k", "width": info.width, "height": info.height, "spp": info.samples,
+                "depth": info.depth, "batch_size": info.batch_size, "instances": 512,
+                "instanced_triangles": 20736000, "unique_triangles": 324000, "mesh_lights": 32,
+                "sky": "4096x2048 procedural equirect, Gaussian sun peak 5e4", "lens_radius": 0.02,
+                "env_is": True, "seed": 1}
     elif name == "cornell":
         engine, info = scenes.cornell_box(seed=1)
         desc = {"workload": "cornell_256", "width": info.width, "height": info.height, "spp": info.samples,
@@ -250,8 +257,9 @@ def run_ours(args) -> None:
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     paths_per_step = W * H * (info.samples // info.batch_size) * info.batch_size
 
+    env_is = bool(desc.get("env_is", False))
     for _ in range(args.warmup):
-        gpu.render(sd, info, outputs=dev_ptrs)
+        gpu.render(sd, info, outputs=dev_ptrs, env_is=env_is)
     torch.cuda.synchronize()
 
     step_ms = []
@@ -264,7 +272,7 @@ def run_ours(args) -> None:
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            gpu.render(sd, info, outputs=dev_ptrs)
+            gpu.render(sd, info, outputs=dev_ptrs, env_is=env_is)
             e1.record(stream)
             torch.cuda.synchronize()
             barrier()
@@ -289,7 +297,7 @@ def run_ours(args) -> None:
         torch.cuda.synchronize()
         barrier()
         t = time.perf_counter()
-        gpu.render(sd_step, info, host_outputs=host_ptrs)
+        gpu.render(sd_step, info, host_outputs=host_ptrs, env_is=env_is)
         dt = time.perf_counter() - t
         if i >= args.warmup:
             e2e_s.append(dt)
@@ -306,7 +314,7 @@ def run_ours(args) -> None:
            "d2h_bytes_per_step": 3 * H * W * 16}
 
     # roofline of the dominant kernel from one profiled render of the same workload
-    gpu.render(sd, info, outputs=dev_ptrs, profile=True)
+    gpu.render(sd, info, outputs=dev_ptrs, profile=True, env_is=env_is)
     prof = [k for k in ctx.kernel_profile() if k["name"] != "k_begin"]
     total_prof = sum(k["total_ms"] for k in ctx.kernel_profile())
     dom = max(prof, key=lambda k: k["total_ms"])
@@ -340,13 +348,172 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+N_SCENES = 8
+
+
+def _job_scenes(ctx, n_scenes: int):
+    """The seeded scene pool of the batched and serving workloads, resident."""
+    from vviewer_gb300 import scenes
+    engines = [scenes.random_scene(100 + k) for k in range(n_scenes)]
+    gpus = [ctx.upload(e.scene.build()) for e in engines]
+    tris = [sum(int(np.prod(m.indices.shape)) // 3 for m in e.scene.build().meshes) for e in engines]
+    return engines, gpus, tris
+
+
+def run_batched(args) -> None:
+    """64 jobs from the seeded job mix (scenes of 10k-2M triangles, 256^2 to
+    1920x1080, 16/64/256 spp) rendered together through the job engine: one
+    step submits all 64 and waits for the last. value = total paths / wall
+    time with device outputs; e2e = the same with host outputs; the same jobs
+    one after another through vvpt_render give sequential_paths_per_s."""
+    import torch
+
+    from vviewer_gb300 import Context, scenes
+    ctx = Context(0)
+    engines, gpus, tris = _job_scenes(ctx, N_SCENES)
+    mix = scenes.job_mix(1, 64, N_SCENES)
+    sds = [engines[k].scene.scene_data(i.width, i.height) for k, i in mix]
+    paths = sum(i.width * i.height * (i.samples // i.batch_size) * i.batch_size for _, i in mix)
+    dev = [{k: torch.zeros((i.height, i.width, 4), dtype=torch.float32, device="cuda")
+            for k in ("radiance", "albedo", "normal")} for _, i in mix]
+    ptrs = [{k: v.data_ptr() for k, v in d.items()} for d in dev]
+
+    def step(host: bool):
+        jobs = []
+        for (k, info), sd, p in zip(mix, sds, ptrs):
+            jobs.append(gpus[k].submit(sd, info, outputs=None if host else p))
+        for j in jobs:
+            j.wait()
+        lat = []
+        for j in jobs:
+            ji = j.poll()
+            lat.append(ji.end_ms - ji.submit_ms)
+            j.release()
+        return lat
+
+    warm = scenes.job_mix(2, 4, N_SCENES)
+    for _ in range(max(args.warmup, 1)):
+        js = [gpus[k].submit(engines[k].scene.scene_data(64, 64),
+                             type(i)(samples=16, depth=8, batch_size=4, width=64, height=64, write_files=False))
+              for k, i in warm]
+        for j in js:
+            j.wait()
+            j.release()
+    torch.cuda.synchronize()
+    times, lats = [], []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            lats += step(False)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t)
+    clock = clocks.summary()
+    e2e_t = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        step(True)
+        e2e_t.append(time.perf_counter() - t)
+    line = {"metric": METRIC, "value": paths * args.steps / sum(times), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scenes)",
+            "config": {"workload": "batched_64_jobs", "jobs": 64, "scenes": N_SCENES, "scene_triangles": tris,
+                       "resolutions": "256^2 / 512^2 / 1024^2 / 1920x1080", "spp": "16 / 64 / 256",
+                       "depth": 8, "batch_size": 4, "paths_per_step": paths, "seed": 1,
+                       "l2": "per-job batch sums and path state far above L2"},
+            "e2e": {"value": paths * args.steps / sum(e2e_t), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": sum(3 * i.width * i.height * 16 for _, i in mix)},
+            "job_latency_ms": {"p50": float(np.percentile(lats, 50)), "max": float(np.max(lats))},
+            "clocks": clock}
+    if args.sequential:
+        t = time.perf_counter()
+        for (k, info), sd, p in zip(mix, sds, ptrs):
+            gpus[k].render(sd, info, outputs=p)
+        torch.cuda.synchronize()
+        line["sequential_paths_per_s"] = paths / (time.perf_counter() - t)
+    for g in gpus:
+        g.release()
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args) -> None:
+    """512 requests with Poisson arrivals (mean gap 50 ms, seeded) against the
+    resident scene pool of the batched workload; preview sizes (256^2 / 512^2,
+    8 / 16 / 32 spp). A submitter thread issues each request at its arrival
+    time; latency = submit to outputs on the host. value = aggregate paths/s
+    from the first arrival to the last completion."""
+    import threading
+
+    import torch
+
+    from vviewer_gb300 import Context, scenes
+    ctx = Context(0)
+    ctx.set_budget(150 * (1 << 30))
+    engines, gpus, tris = _job_scenes(ctx, N_SCENES)
+    reqs = scenes.serving_requests(1, args.requests, N_SCENES)
+    sds = [engines[k].scene.scene_data(i.width, i.height) for _, k, i in reqs]
+    paths = sum(i.width * i.height * (i.samples // i.batch_size) * i.batch_size for _, _, i in reqs)
+    for _ in range(max(args.warmup, 1)):
+        j = gpus[0].submit(sds[0], reqs[0][2])
+        j.wait()
+        j.release()
+    torch.cuda.synchronize()
+    jobs = [None] * len(reqs)
+
+    def submitter():
+        t0 = time.perf_counter()
+        for n, ((at, k, info), sd) in enumerate(zip(reqs, sds)):
+            delay = at / 1e3 - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            jobs[n] = gpus[k].submit(sd, info)
+
+    with ClockSampler(0) as clocks:
+        th = threading.Thread(target=submitter)
+        t = time.perf_counter()
+        th.start()
+        th.join()
+        for j in jobs:
+            j.wait()
+        wall = time.perf_counter() - t
+    clock = clocks.summary()
+    infos = [j.poll() for j in jobs]
+    lat = np.array([ji.end_ms - ji.submit_ms for ji in infos])
+    span_ms = max(ji.end_ms for ji in infos) - min(ji.submit_ms for ji in infos)
+    for j in jobs:
+        j.release()
+    line = {"metric": METRIC, "value": paths / (span_ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": args.warmup, "ms_per_step": span_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes, Poisson arrivals)",
+            "config": {"workload": "serving_512_requests", "requests": len(reqs), "mean_gap_ms": 50.0,
+                       "scenes": N_SCENES, "scene_triangles": tris, "resolutions": "256^2 / 512^2",
+                       "spp": "8 / 16 / 32", "depth": 8, "batch_size": 4, "paths": paths, "seed": 1,
+                       "budget_bytes": 150 * (1 << 30), "outputs": "host"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
+                           "mean": float(lat.mean())},
+            "offered_paths_per_s": paths / (reqs[-1][0] / 1e3), "wall_s": wall,
+            "e2e": {"value": paths / (span_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": sum(3 * i.width * i.height * 16 for _, _, i in reqs)},
+            "clocks": clock}
+    for g in gpus:
+        g.release()
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cornell_medium", "cornell"], default="cornell_medium")
+    ap.add_argument("--workload", choices=["cornell_medium", "cornell", "instanced_sky", "batched64", "serving512"],
+                    default="cornell_medium")
+    ap.add_argument("--sequential", action="store_true", help="batched64: also time the jobs one by one")
+    ap.add_argument("--requests", type=int, default=512, help="serving512: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
@@ -354,6 +521,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched64":
+        run_batched(args)
+    elif args.workload == "serving512":
+        run_serving(args)
     else:
         run_ours(args)
 

@@ -208,7 +208,17 @@ enum {
     VVPT_RENDER_WANT_BATCH_M2 = 1u,
     /* launch the wavefront kernels one by one with CUDA events around each
      * (no graphs) and record per-kernel times: see vvpt_last_kernel_profile */
-    VVPT_RENDER_PROFILE_KERNELS = 2u
+    VVPT_RENDER_PROFILE_KERNELS = 2u,
+    /* Estimator addition with no counterpart in the reference (which never
+     * light-samples the environment, lightSampling.glsl:101-106): with an
+     * environment image and background mode 1 or 2, the environment joins
+     * the uniform light pick as one more light, importance sampled by
+     * texel luminance, and escapes of sampled directions take the BSDF side
+     * of the power-heuristic MIS weight. The environment sample of a path's
+     * last event contributes nothing (the reference never adds environment
+     * light from the last event either), so the expected image is the
+     * reference estimator's; the variance under bright skies is far lower. */
+    VVPT_RENDER_ENV_IS = 4u
 };
 
 /* Output images, RGBA32F row-major W*H*4 floats each, A = 1 (the three

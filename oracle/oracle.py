@@ -40,14 +40,16 @@ def load():
     return _lib
 
 
-def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threads: int = 0, fp64: bool = False):
+def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threads: int = 0, fp64: bool = False,
+           env_is: bool = False):
     """Renders with the oracle. Returns dict of H x W x 4 float32 arrays
     (radiance, albedo, normal, radiance_m2); pixels not in `pixels` stay 0."""
     from vviewer_gb300 import _native as N
 
     lib = load()
     desc = flat_scene.desc()
-    ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, 0)
+    ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height,
+                      N.RENDER_ENV_IS if env_is else 0)
     H, W = info.height, info.width
     out = {k: np.zeros((H, W, 4), dtype=np.float32) for k in ("radiance", "albedo", "normal", "radiance_m2")}
     px = None

@@ -258,6 +258,11 @@ struct Scene {
     std::vector<Tex> tex;
     int env = -1;
     float cull_o = 0.0f, cull_r = 0.0f;
+    // environment importance sampling (VVPT_RENDER_ENV_IS): piecewise
+    // constant over the equirect texels
+    std::vector<float> envFunc, envCond, envMarg;
+    uint32_t envW = 0, envH = 0;
+    float envInt = 0.0f;
 };
 
 // ------------------------------------------------------------------ closest hit
@@ -521,6 +526,126 @@ V3 env_sample(const Scene &s, V3 dir)
     return rgb(texture(s, (uint32_t)s.env, u, w, true));
 }
 
+// Environment sampling tables: function = texel luminance maximised over the
+// 3x3 neighbourhood (columns wrap, rows clamp) times the cosine of the row
+// centre's latitude; per-row and marginal CDFs summed in double.
+void build_env_tables(Scene &s, const float *rgba, uint32_t w, uint32_t h)
+{
+    s.envW = w;
+    s.envH = h;
+    std::vector<double> lum((size_t)w * h), f((size_t)w * h);
+    for (size_t i = 0; i < lum.size(); i++) {
+        double y = 0.2126 * rgba[4 * i] + 0.7152 * rgba[4 * i + 1] + 0.0722 * rgba[4 * i + 2];
+        lum[i] = (y > 0.0 && std::isfinite(y)) ? y : 0.0;
+    }
+    for (uint32_t r = 0; r < h; r++) {
+        double lat = (((double)r + 0.5) / (double)h - 0.5) / (double)0.3183f;
+        lat = std::min(std::max(lat, -0.5 * M_PI), 0.5 * M_PI);
+        double cl = std::max(0.0, std::cos(lat));
+        for (uint32_t c = 0; c < w; c++) {
+            double mx = 0.0;
+            for (int a = -1; a <= 1; a++) {
+                long rr = std::min<long>(std::max<long>((long)r + a, 0), (long)h - 1);
+                for (int b = -1; b <= 1; b++)
+                    mx = std::max(mx, lum[(size_t)rr * w + (c + w + b) % w]);
+            }
+            f[(size_t)r * w + c] = mx * cl;
+        }
+    }
+    s.envFunc.resize((size_t)w * h);
+    s.envCond.resize((size_t)h * (w + 1));
+    s.envMarg.resize(h + 1);
+    std::vector<double> rowInt(h);
+    for (uint32_t r = 0; r < h; r++) {
+        double sum = 0.0;
+        for (uint32_t c = 0; c < w; c++)
+            sum += f[(size_t)r * w + c];
+        rowInt[r] = sum / (double)w;
+        double run = 0.0;
+        float *cdf = &s.envCond[(size_t)r * (w + 1)];
+        cdf[0] = 0.0f;
+        for (uint32_t c = 0; c < w; c++) {
+            run += f[(size_t)r * w + c];
+            cdf[c + 1] = sum > 0.0 ? (float)(run / sum) : (float)((double)(c + 1) / (double)w);
+            s.envFunc[(size_t)r * w + c] = (float)f[(size_t)r * w + c];
+        }
+        cdf[w] = 1.0f;
+    }
+    double total = 0.0;
+    for (uint32_t r = 0; r < h; r++)
+        total += rowInt[r];
+    double run = 0.0;
+    s.envMarg[0] = 0.0f;
+    for (uint32_t r = 0; r < h; r++) {
+        run += rowInt[r];
+        s.envMarg[r + 1] = total > 0.0 ? (float)(run / total) : (float)((double)(r + 1) / (double)h);
+    }
+    s.envMarg[h] = 1.0f;
+    s.envInt = (float)(total / (double)h);
+}
+
+// density in solid angle of envSampleDir producing `dir` (lookup mapping of
+// env_sample: du dv = 0.1591 * 0.3183 * dw / cos(latitude))
+float envPdf(const Scene &s, V3 dir)
+{
+    if (s.envInt <= 0.0f)
+        return 0.0f;
+    V3 v = normalize(dir);
+    float y = std::min(std::max(v.y, -1.0f), 1.0f);
+    float u = std::atan2(v.z, v.x) * 0.1591f + 0.5f;
+    float w = std::asin(y) * 0.3183f + 0.5f;
+    float x = u + 0.25f;
+    u = x - std::floor(x);
+    float cl = std::sqrt(std::max(0.0f, 1.0f - y * y));
+    if (cl < 1e-6f)
+        return 0.0f;
+    uint32_t col = std::min((uint32_t)(u * (float)s.envW), s.envW - 1);
+    uint32_t row = std::min((uint32_t)(w * (float)s.envH), s.envH - 1);
+    return s.envFunc[(size_t)row * s.envW + col] / s.envInt * (0.1591f * 0.3183f) / cl;
+}
+
+// last index in [0, n) whose CDF value is <= x
+uint32_t cdfIndex(const float *cdf, uint32_t n, float x)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) / 2;
+        if (cdf[mid] <= x)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// PBRT-style 2D piecewise-constant sample: row from the marginal, column
+// from that row's conditional, continuous offsets inside the cells.
+V3 envSampleDir(const Scene &s, float uRow, float uCol, float &pdf)
+{
+    pdf = 0.0f;
+    uint32_t r = cdfIndex(s.envMarg.data(), s.envH, uRow);
+    float m0 = s.envMarg[r], m1 = s.envMarg[r + 1];
+    float dv = m1 > m0 ? (uRow - m0) / (m1 - m0) : 0.0f;
+    const float *cdf = &s.envCond[(size_t)r * (s.envW + 1)];
+    uint32_t c = cdfIndex(cdf, s.envW, uCol);
+    float c0 = cdf[c], c1 = cdf[c + 1];
+    float du = c1 > c0 ? (uCol - c0) / (c1 - c0) : 0.0f;
+    float u = ((float)c + du) / (float)s.envW;
+    float w = ((float)r + dv) / (float)s.envH;
+    float x = u - 0.25f;
+    if (x < 0.0f)
+        x += 1.0f;
+    float lon = (x - 0.5f) / 0.1591f;
+    if (std::fabs(lon) > PI)
+        return v3(0.0f, 1.0f, 0.0f);
+    float lat = std::min(std::max((w - 0.5f) / 0.3183f, -0.5f * PI), 0.5f * PI);
+    float cl = std::cos(lat);
+    if (cl < 1e-6f)
+        return v3(0.0f, 1.0f, 0.0f);
+    pdf = s.envFunc[(size_t)r * s.envW + c] / s.envInt * (0.1591f * 0.3183f) / cl;
+    return v3(cl * std::cos(lon), std::sin(lat), cl * std::sin(lon));
+}
+
 // ------------------------------------------------------------------ shader math (GLSL includes)
 
 // sampling.glsl:3-40
@@ -773,6 +898,7 @@ struct Params {
     float envType, lensRadius, focalDistance, envIntensity, zfar;
     int camVolume;
     uint32_t W, H, batchSize, batches, depth, totalSamples, totalLights;
+    uint32_t envLight = 0; // the environment is one more light of the pick
 };
 
 // RayPayloadPrimary, shaders/pt/structs_pt.glsl:4-30
@@ -785,6 +911,8 @@ struct Payload {
     float vtmin;
     uint32_t volumeMaterialIndex;
     uint32_t rngState;
+    bool sampled = false;   // direction drawn by BSDF/phase sampling (env MIS)
+    float samplePdf = 0.0f;
 };
 inline float rand1D(Payload &p) { return uintToFloat(xorshift(p.rngState)); }
 
@@ -950,22 +1078,40 @@ V3 shadow(const Ctx &c, const Payload &pl, V3 originPosition, V3 dir, float tmax
 }
 
 // sampleLight, lightSampling.glsl:1-147
-LSR sampleLight(const Ctx &c, Payload &pl, V3 originPosition)
+// allowEnv: with the environment as a light (VVPT_RENDER_ENV_IS), whether
+// picking it contributes (not at a path's last event).
+LSR sampleLight(const Ctx &c, Payload &pl, V3 originPosition, bool allowEnv)
 {
     LSR lsr;
     lsr.isDeltaLight = true;
     lsr.radiance = v3s(0.0f);
     lsr.pdf = 1.0f;
     lsr.direction = v3s(0.0f);
-    uint32_t totalLights = c.p.totalLights;
+    uint32_t totalLights = c.p.totalLights + c.p.envLight;
     if (totalLights == 0)
         return lsr;
     float pdf = 1.0f / (float)totalLights;
     uint32_t randomLight = (uint32_t)(rand1D(pl) * (float)totalLights);
     if (randomLight >= totalLights)
         randomLight = totalLights - 1;
-    const vvpt_light_instance &L = c.s.lights[randomLight];
     float tmax = 10000.0f;
+    if (randomLight == c.p.totalLights) {
+        lsr.isDeltaLight = false;
+        if (!allowEnv)
+            return lsr;
+        float uRow = rand1D(pl);
+        float uCol = rand1D(pl);
+        float epdf;
+        lsr.direction = envSampleDir(c.s, uRow, uCol, epdf);
+        tmax = c.p.zfar;
+        if (epdf > 0.0f) {
+            lsr.radiance = env_sample(c.s, lsr.direction) * ((int)c.p.envType == 1 ? c.p.envIntensity : 1.0f);
+            lsr.pdf = pdf * epdf;
+            lsr.radiance = lsr.radiance * shadow(c, pl, originPosition, lsr.direction, tmax);
+        }
+        return lsr;
+    }
+    const vvpt_light_instance &L = c.s.lights[randomLight];
     V3 lpos = v3(L.position[0], L.position[1], L.position[2]);
     if (L.info[3] == 0) {
         const vvpt_light_data &ld = c.s.ldata[L.info[0]];
@@ -1118,7 +1264,7 @@ void nextEventEstimation(const Ctx &c, Payload &pl, float sampleDirectionPDF)
                 V3 objOrigin = xpoint(in.w2o, origin); // gl_ObjectRayOriginEXT, rayNEE.rahit.glsl:122
                 float dd = length(objOrigin - wp);
                 float lightDirectPdf = sampledPointPdf * (dd * dd) / dp;
-                pdf = lightDirectPdf * (1.0f / (float)c.p.totalLights);
+                pdf = lightDirectPdf * (1.0f / (float)(c.p.totalLights + c.p.envLight));
             } else {
                 pdf = 0.0f;
                 emissive = v3s(0.0f);
@@ -1204,7 +1350,9 @@ bool processVolumeHit(const Ctx &c, Payload &pl, uint32_t vol, float vtstart, fl
     pl.beta = pl.beta * F;
     if (sampledMedium) {
         V3 scatteringPosition = pl.origin + (vtstart + hit_distance) * dirn;
-        LSR lsr = sampleLight(c, pl, scatteringPosition);
+        bool lastEvent = pl.recursionDepth + 1 >= c.p.depth;
+        LSR lsr = sampleLight(c, pl, scatteringPosition,
+                              !lastEvent && !((int)c.p.envType == 2 && pl.surfaceDepth == 0));
         if (!isBlack(lsr.radiance)) {
             float p = HenyeyGreenstein(dot(wo, lsr.direction), g);
             V3 Fp = v3s(p);
@@ -1223,6 +1371,8 @@ bool processVolumeHit(const Ctx &c, Payload &pl, uint32_t vol, float vtstart, fl
         float spdf = HG_Sample(wo, sdir, r0, r1, g);
         pl.origin = scatteringPosition;
         pl.direction = sdir;
+        pl.sampled = true;
+        pl.samplePdf = spdf;
         nextEventEstimation(c, pl, spdf);
     }
     return sampledMedium;
@@ -1281,7 +1431,7 @@ void closestHit(const Ctx &c, Payload &pl, const Hit &h, V3 rayDir)
         }
         pl.surfaceDepth += 1;
         V3 wo = worldToLocal(hi.frame, -rayDir);
-        LSR lsr = sampleLight(c, pl, hi.worldPosition);
+        LSR lsr = sampleLight(c, pl, hi.worldPosition, pl.recursionDepth + 1 < c.p.depth);
         if (!isBlack(lsr.radiance)) {
             V3 wi = worldToLocal(hi.frame, lsr.direction);
             V3 F;
@@ -1328,6 +1478,8 @@ void closestHit(const Ctx &c, Payload &pl, const Hit &h, V3 rayDir)
             pl.beta = pl.beta * v3(std::min(std::max(q.x, 0.0f), 1.0f), std::min(std::max(q.y, 0.0f), 1.0f),
                                    std::min(std::max(q.z, 0.0f), 1.0f));
         }
+        pl.sampled = true;
+        pl.samplePdf = sampleDirectionPDF;
         nextEventEstimation(c, pl, sampleDirectionPDF);
     }
     russianRoulette(pl);
@@ -1344,6 +1496,11 @@ void miss(const Ctx &c, Payload &pl, V3 rayDir)
     if (!sampledMedium) {
         pl.stop = true;
         int mode = (int)c.p.envType;
+        // environment light-sampled: BSDF side of the MIS weight for an
+        // escape along a sampled direction
+        float wenv = 1.0f;
+        if (c.p.envLight && pl.sampled)
+            wenv = PowerHeuristic(pl.samplePdf, envPdf(c.s, rayDir) / (float)(c.p.totalLights + 1));
         if (mode == 0) {
             V3 bg = c.p.background;
             if (pl.surfaceDepth == 0) {
@@ -1357,14 +1514,14 @@ void miss(const Ctx &c, Payload &pl, V3 rayDir)
                 pl.albedo = bg;
                 pl.normal = v3s(0.0f);
             }
-            pl.radiance = pl.radiance + bg * pl.beta;
+            pl.radiance = pl.radiance + bg * pl.beta * wenv;
         } else if (mode == 2) {
             if (pl.surfaceDepth == 0) {
                 pl.albedo = c.p.background;
                 pl.normal = v3s(0.0f);
                 pl.radiance = pl.radiance + c.p.background * pl.beta;
             } else {
-                pl.radiance = pl.radiance + env_sample(c.s, rayDir) * pl.beta;
+                pl.radiance = pl.radiance + env_sample(c.s, rayDir) * pl.beta * wenv;
             }
         }
         return;
@@ -1416,6 +1573,7 @@ void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, A
         pl.origin = origin;
         pl.direction = direction;
         pl.surfaceDepth = 0;
+        pl.sampled = false;
         pl.insideVolume = insideVolume;
         pl.volumeMaterialIndex = (uint32_t)p.camVolume;
         V3 beta = v3s(1.0f), radiance = v3s(0.0f), albedo = v3s(0.0f), normal = v3s(0.0f);
@@ -1556,6 +1714,9 @@ bool build_scene(const vvpt_scene_desc *desc, Scene &s)
         s.env = (int)s.tex.size();
         s.tex.push_back({desc->environment->width, desc->environment->height, desc->environment->format,
                          (const uint8_t *)desc->environment->data});
+        if (desc->environment->format == VVPT_TEXTURE_RGBA32F)
+            build_env_tables(s, (const float *)desc->environment->data, desc->environment->width,
+                             desc->environment->height);
     }
     return true;
 }
@@ -1580,6 +1741,12 @@ void make_params(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const v
     p.totalLights = desc->num_lights;
 }
 
+void set_env_light(const Scene &s, const vvpt_render_info *ri, Params &p)
+{
+    int mode = (int)p.envType;
+    p.envLight = ((ri->flags & VVPT_RENDER_ENV_IS) && s.envInt > 0.0f && (mode == 1 || mode == 2)) ? 1u : 0u;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1598,6 +1765,7 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
         return 2;
     Params p;
     make_params(desc, sd, ri, p);
+    set_env_light(s, ri, p);
     const Ctx c{s, p};
     const uint32_t npix = pixels ? num_pixels : p.W * p.H;
     if (threads <= 0)

@@ -23,6 +23,9 @@ static inline unsigned __float_as_uint(float f) { unsigned i; std::memcpy(&i, &f
 static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 template <class T>
 static inline T __ldg(const T *p) { return *p; }
+// one lane per "warp": the speculative-traversal vote sees only this ray
+static inline unsigned __activemask() { return 1u; }
+static inline int __all_sync(unsigned, int pred) { return pred; }
 
 #include "scene_pack.h"
 #include "traverse.cuh"

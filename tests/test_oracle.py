@@ -117,3 +117,41 @@ def test_oracle_edge_cases():
     info.depth, info.samples, info.batch_size = 8, 3, 4  # batches = 3 / 4 = 0
     z = oracle.render(fs, sd, info)
     assert (z["radiance"][..., :3] == 0).all()
+
+
+def _mean_and_var(out, batches):
+    """Per-channel image estimate and the variance of that estimate from the
+    per-batch sums (radiance = sum of batch sums, radiance_m2 = sum of squares)."""
+    r = out["radiance"][..., :3].astype(np.float64)
+    m2 = out["radiance_m2"][..., :3].astype(np.float64)
+    var_batch = np.maximum(m2 / batches - (r / batches) ** 2, 0.0) * batches / (batches - 1)
+    return r, var_batch * batches
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_env_importance_sampling_keeps_the_expectation(mode):
+    """VVPT_RENDER_ENV_IS is an estimator addition (the reference never
+    light-samples the environment). Under a broad sun both estimators are
+    well behaved: per pixel the two images agree within their Monte Carlo
+    error. Under a small, bright sun the reference estimator is heavy tailed
+    (most batches miss the sun), so only the image means are compared, and
+    the importance-sampled variance must be far lower."""
+    from vviewer_gb300.scene import EnvironmentType
+
+    def pair(spp, sun_peak, sun_sigma_deg):
+        e, info = scenes.sky_scene(1, 48, 32, spp, 6, 4, sun_peak=sun_peak, sun_sigma_deg=sun_sigma_deg)
+        e.scene.environment_type = EnvironmentType(mode)
+        e.scene.background_color = [0.2, 0.3, 0.4]
+        fs = e.scene.build()
+        sd = e.scene.scene_data(info.width, info.height)
+        B = info.samples // info.batch_size
+        return (_mean_and_var(oracle.render(fs, sd, info), B),
+                _mean_and_var(oracle.render(fs, sd, info, env_is=True), B))
+
+    (ref, vref), (isr, vis) = pair(1024, 50.0, 8.0)
+    z = (isr - ref) / np.sqrt(vref + vis + 1e-30)
+    assert (np.abs(z) > 4.0).mean() < 0.005, (np.abs(z) > 4.0).mean()
+    (ref, vref), (isr, vis) = pair(2048, 5.0e3, 2.0)
+    z_img = (isr.mean() - ref.mean()) / np.sqrt((vref.sum() + vis.sum()) / ref.size ** 2)
+    assert abs(z_img) < 4.0, z_img
+    assert vis.mean() < 0.05 * vref.mean()

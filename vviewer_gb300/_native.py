@@ -30,6 +30,7 @@ TEXTURE_RGBA8_LINEAR = 0
 TEXTURE_RGBA8_SRGB = 1
 TEXTURE_RGBA32F = 2
 RENDER_WANT_BATCH_M2 = 1
+RENDER_ENV_IS = 4
 
 
 class VvptError(RuntimeError):

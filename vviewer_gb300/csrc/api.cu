@@ -60,6 +60,10 @@ vvpt_status make_render_params(vvpt_ctx *ctx, const vvpt_scene *scene, const vvp
         return fail(ctx, VVPT_ERR_INVALID_ARG, "width * height * batches exceeds 2^32");
     hp.total_items = (uint32_t)total_items64;
     hp.want_m2 = (info->flags & VVPT_RENDER_WANT_BATCH_M2) ? 1u : 0u;
+    const int mode = (int)hp.env_type;
+    hp.env_light = ((info->flags & VVPT_RENDER_ENV_IS) && scene->view.env_func_int > 0.0f && (mode == 1 || mode == 2))
+                       ? 1u
+                       : 0u;
     return VVPT_OK;
 }
 
@@ -302,6 +306,8 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
         return st;
     if ((st = upload(ctx, scene->texels, pk.texels, bytes)) != VVPT_OK)
         return st;
+    if ((st = upload(ctx, scene->env_dist, pk.env_dist, bytes)) != VVPT_OK)
+        return st;
     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "scene upload");
 
     SceneView &v = scene->view;
@@ -324,6 +330,12 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     v.has_transparent = pk.has_transparent ? 1u : 0u;
     v.cull_o = pk.cull_o;
     v.cull_r = pk.cull_r;
+    v.env_w = pk.env_w;
+    v.env_h = pk.env_h;
+    v.env_func_int = pk.env_func_int;
+    v.env_func = scene->env_dist.as<float>();
+    v.env_cond_cdf = v.env_func + (size_t)pk.env_w * pk.env_h;
+    v.env_marg_cdf = v.env_cond_cdf + (size_t)(pk.env_w + 1) * pk.env_h;
     scene->bytes = bytes;
     scene->num_materials = desc->num_materials;
     *out_scene = guard.release();

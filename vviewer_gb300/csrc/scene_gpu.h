@@ -134,6 +134,14 @@ struct SceneView {
     // coordinate magnitude a triangle test sees per unit of world-space ray
     // direction is at most cull_o * |origin| + cull_r (max-norms)
     float cull_o, cull_r;
+    // importance sampling of the environment (piecewise constant over the
+    // equirect texels, function = dilated luminance x cos(latitude));
+    // env_func_int == 0: not samplable
+    const float *env_func;     // env_h x env_w
+    const float *env_cond_cdf; // env_h x (env_w + 1), per-row CDFs
+    const float *env_marg_cdf; // env_h + 1
+    uint32_t env_w, env_h;
+    float env_func_int;        // integral of env_func over [0,1]^2
 };
 
 }  // namespace vvpt

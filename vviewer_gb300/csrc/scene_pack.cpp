@@ -69,6 +69,62 @@ bool affine_inverse_rows(const float m[16], float4 rows[3])
     return true;
 }
 
+float build_env_distribution(const float *rgba, uint32_t w, uint32_t h, std::vector<float> &out)
+{
+    const size_t W = w, H = h;
+    std::vector<double> lum(W * H), f(W * H);
+    for (size_t i = 0; i < W * H; i++) {
+        const double v = 0.2126 * rgba[4 * i] + 0.7152 * rgba[4 * i + 1] + 0.0722 * rgba[4 * i + 2];
+        lum[i] = v > 0.0 && std::isfinite(v) ? v : 0.0;
+    }
+    for (size_t r = 0; r < H; r++) {
+        // latitude of the row centre: w = asin(y) * 0.3183 + 0.5
+        const double lat = (((double)r + 0.5) / (double)H - 0.5) / (double)0.3183f;
+        const double cosl = std::max(0.0, std::cos(std::min(std::max(lat, -0.5 * M_PI), 0.5 * M_PI)));
+        for (size_t c = 0; c < W; c++) {
+            double m = 0.0;
+            for (int dr = -1; dr <= 1; dr++) {
+                const size_t rr = (size_t)std::min<long>(std::max<long>((long)r + dr, 0), (long)H - 1);
+                for (int dc = -1; dc <= 1; dc++) {
+                    const size_t cc = (c + W + dc) % W;
+                    m = std::max(m, lum[rr * W + cc]);
+                }
+            }
+            f[r * W + c] = m * cosl;
+        }
+    }
+    out.assign(W * H + H * (W + 1) + (H + 1), 0.0f);
+    float *func = out.data(), *cond = func + W * H, *marg = cond + H * (W + 1);
+    std::vector<double> row_int(H, 0.0);
+    for (size_t r = 0; r < H; r++) {
+        double acc = 0.0;
+        for (size_t c = 0; c < W; c++)
+            acc += f[r * W + c];
+        row_int[r] = acc / (double)W;
+        double run = 0.0;
+        float *cr = cond + r * (W + 1);
+        cr[0] = 0.0f;
+        for (size_t c = 0; c < W; c++) {
+            run += f[r * W + c];
+            cr[c + 1] = acc > 0.0 ? (float)(run / acc) : (float)((double)(c + 1) / (double)W);
+        }
+        cr[W] = 1.0f;
+        for (size_t c = 0; c < W; c++)
+            func[r * W + c] = (float)f[r * W + c];
+    }
+    double total = 0.0;
+    for (size_t r = 0; r < H; r++)
+        total += row_int[r];
+    double run = 0.0;
+    marg[0] = 0.0f;
+    for (size_t r = 0; r < H; r++) {
+        run += row_int[r];
+        marg[r + 1] = total > 0.0 ? (float)(run / total) : (float)((double)(r + 1) / (double)H);
+    }
+    marg[H] = 1.0f;
+    return (float)(total / (double)H);
+}
+
 vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads)
 {
     out = PackedScene();
@@ -389,6 +445,10 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
             return fail(err, VVPT_ERR_INVALID_ARG, "environment must be an RGBA32F equirectangular image");
         env_index = (int)texs.size();
         add_texture(*desc->environment);
+        out.env_w = desc->environment->width;
+        out.env_h = desc->environment->height;
+        out.env_func_int = build_env_distribution(static_cast<const float *>(desc->environment->data), out.env_w,
+                                                  out.env_h, out.env_dist);
     }
 
     return VVPT_OK;

@@ -29,6 +29,11 @@ struct PackedScene {
     int32_t env_texture = -1;
     bool has_transparent = false;
     float cull_o = 0.0f, cull_r = 0.0f; // SceneView culling-margin bound
+    // environment sampling tables, one array: function (h x w), per-row CDFs
+    // (h x (w + 1)), marginal CDF (h + 1); empty without an environment
+    std::vector<float> env_dist;
+    uint32_t env_w = 0, env_h = 0;
+    float env_func_int = 0.0f;
     int tlas_depth = 0;
     int max_blas_depth = 0;
 };
@@ -36,6 +41,13 @@ struct PackedScene {
 // Returns VVPT_OK or an error status with `err` set. `threads` = 0 uses every
 // hardware thread for the BLAS builds.
 vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads = 0);
+
+// Piecewise-constant sampling tables of an RGBA32F equirect environment
+// (PackedScene::env_dist layout): function = luminance dilated over the 3x3
+// texel neighbourhood (so every texel the bilinear lookup can reach has
+// probability) times cos(latitude of the row centre), CDFs accumulated in
+// double. Returns the function's integral over [0,1]^2 (0: nothing to sample).
+float build_env_distribution(const float *rgba, uint32_t w, uint32_t h, std::vector<float> &out);
 
 // Row form of the 3x4 affine part of a column-major 4x4 matrix, and of its
 // inverse (computed in double, rounded to float). False when singular.

@@ -368,4 +368,76 @@ __device__ __forceinline__ float3 env_lookup(const SceneView &s, const float3 &d
     return f3(c.x, c.y, c.z);
 }
 
+// ---- environment importance sampling (an estimator addition: the
+// reference never light-samples the environment, lightSampling.glsl:101-106)
+//
+// Directions map to the texture like env_lookup: u = atan2(z, x) * 0.1591 +
+// 0.75 (wrapped), w = asin(y) * 0.3183 + 0.5, so a solid-angle density is the
+// (u, w) density times 0.1591 * 0.3183 / cos(latitude).
+constexpr float kEnvJacobian = 0.1591f * 0.3183f;
+
+// Density (solid angle) of sample_env producing `dir`.
+__device__ __forceinline__ float env_pdf(const SceneView &s, const float3 &dir)
+{
+    if (s.env_func_int <= 0.0f)
+        return 0.0f;
+    const float3 v = normalize3(dir);
+    const float y = fminf(fmaxf(v.y, -1.0f), 1.0f);
+    float u = atan2f(v.z, v.x) * 0.1591f + 0.5f;
+    const float w = asinf(y) * 0.3183f + 0.5f;
+    const float x = u + 0.25f;
+    u = x - floorf(x);
+    const float cosl = sqrtf(fmaxf(0.0f, 1.0f - y * y));
+    if (cosl < 1e-6f)
+        return 0.0f;
+    const uint32_t col = min((uint32_t)(u * (float)s.env_w), s.env_w - 1);
+    const uint32_t row = min((uint32_t)(w * (float)s.env_h), s.env_h - 1);
+    return s.env_func[(size_t)row * s.env_w + col] / s.env_func_int * kEnvJacobian / cosl;
+}
+
+// Last index i in [0, n) with cdf[i] <= x (cdf ascending, cdf[0] = 0): skips
+// zero-probability cells.
+__device__ __forceinline__ uint32_t cdf_find(const float *cdf, uint32_t n, float x)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cdf[mid] <= x)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Direction with density proportional to env_func (PBRT's piecewise-constant
+// 2D distribution: marginal over rows from u_row, conditional over the row's
+// columns from u_col). pdf = 0 when the cell maps outside the lookup's range.
+__device__ __forceinline__ float3 sample_env(const SceneView &s, float u_row, float u_col, float &pdf)
+{
+    pdf = 0.0f;
+    const uint32_t W = s.env_w, H = s.env_h;
+    const uint32_t r = cdf_find(s.env_marg_cdf, H, u_row);
+    const float m0 = s.env_marg_cdf[r], m1 = s.env_marg_cdf[r + 1];
+    const float dv = m1 > m0 ? (u_row - m0) / (m1 - m0) : 0.0f;
+    const float *cc = s.env_cond_cdf + (size_t)r * (W + 1);
+    const uint32_t c = cdf_find(cc, W, u_col);
+    const float c0 = cc[c], c1 = cc[c + 1];
+    const float du = c1 > c0 ? (u_col - c0) / (c1 - c0) : 0.0f;
+    const float u = ((float)c + du) / (float)W;
+    const float w = ((float)r + dv) / (float)H;
+    float x = u - 0.25f;
+    if (x < 0.0f)
+        x += 1.0f;
+    const float lon = (x - 0.5f) / 0.1591f;
+    if (fabsf(lon) > kPi)
+        return f3(0.0f, 1.0f, 0.0f);
+    const float lat = fminf(fmaxf((w - 0.5f) / 0.3183f, -0.5f * kPi), 0.5f * kPi);
+    const float cosl = cosf(lat);
+    if (cosl < 1e-6f)
+        return f3(0.0f, 1.0f, 0.0f);
+    pdf = s.env_func[(size_t)r * W + c] / s.env_func_int * kEnvJacobian / cosl;
+    return f3(cosl * cosf(lon), sinf(lat), cosl * sinf(lon));
+}
+
 }  // namespace vvpt

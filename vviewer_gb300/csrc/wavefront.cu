@@ -16,6 +16,7 @@
 namespace vvpt {
 
 // path flag bits
+constexpr uint32_t F_SAMPLED = 128u;     // ray direction sampled (BSDF or phase), pdf in nee_b.w
 constexpr uint32_t F_INSIDE = 1u;       // rayPayloadPrimary.insideVolume
 constexpr uint32_t F_DONE = 2u;         // sample finished, finalize in regen
 constexpr uint32_t F_ITEM = 4u;         // slot holds a work item
@@ -130,8 +131,12 @@ struct LightSample {
     bool delta;
 };
 
+// With env_light set, the environment is light number num_lights of the
+// uniform pick (importance sampled by sample_env); `allow_env` = false makes
+// that pick contribute nothing (the last event of a path, whose environment
+// contribution the reference's estimator never adds either).
 __device__ __forceinline__ LightSample sample_light(const SceneView &s, const RenderParams &p, const float3 &origin,
-                                                    uint32_t &rng)
+                                                    uint32_t &rng, bool allow_env)
 {
     LightSample ls;
     ls.delta = true;
@@ -139,13 +144,28 @@ __device__ __forceinline__ LightSample sample_light(const SceneView &s, const Re
     ls.pdf = 1.0f;
     ls.dir = f3(0.0f);
     ls.tmax = 10000.0f;
-    const uint32_t total = p.num_lights;
+    const uint32_t total = p.num_lights + p.env_light;
     if (total == 0)
         return ls;
     float pdf = 1.0f / (float)total;
     uint32_t li = (uint32_t)(rand1(rng) * (float)total);
     if (li >= total)
         li = total - 1;
+    if (li == p.num_lights) {
+        ls.delta = false;
+        if (!allow_env)
+            return ls;
+        const float u_row = rand1(rng);
+        const float u_col = rand1(rng);
+        float epdf;
+        ls.dir = sample_env(s, u_row, u_col, epdf);
+        ls.tmax = p.zfar;
+        if (epdf > 0.0f) {
+            ls.radiance = env_lookup(s, ls.dir) * ((int)p.env_type == 1 ? p.env_intensity : 1.0f);
+            ls.pdf = pdf * epdf;
+        }
+        return ls;
+    }
     const DevLightInstance &L = s.lights[li];
     const uint32_t type = L.info[3];
     if (type == 0) {
@@ -434,7 +454,12 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
 
 // Closest hit for every queued extension ray; hits are binned by material
 // model into the shade queues (material-sorted shading).
-__global__ void __launch_bounds__(256) k_extend(JobTable jt, PathState ps, Queues q, int pp)
+// Minimum resident blocks per SM requested for the extension kernel (caps its
+// registers); 1 leaves the register count to the compiler.
+#ifndef VVPT_EXTEND_MIN_BLOCKS
+#define VVPT_EXTEND_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
@@ -620,6 +645,9 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
         bool stop = false;
         bool terminal_no_rr = false; // returns before the RR block
         bool has_shadow = false, has_nee = false;
+        bool sampled = false;        // a new direction was sampled here (pdf in nee_pdf)
+        bool keep_sampled = false;   // pass-through: the direction keeps its sampling pdf
+        const bool last = (d + 1u >= p.depth);
         float3 sh_dir = f3(0.0f), sh_c = f3(0.0f);
         float sh_tmax = 0.0f;
         float3 nee_beta = f3(0.0f);
@@ -639,7 +667,9 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
             // light sample at the scatter point with the HG phase function
             // (process_volume_hit.glsl:42-79)
             float3 wo = -normalize3(dir);
-            LightSample ls = sample_light(s, p, scatter_pos, rng);
+            // in background mode 2 an escape before any surface event sees
+            // the solid colour, so the environment is not a light there
+            LightSample ls = sample_light(s, p, scatter_pos, rng, !last && !((int)p.env_type == 2 && sdepth == 0));
             if (!is_black(ls.radiance)) {
                 float ph = henyey_greenstein(dot3(wo, ls.dir), g);
                 float3 F = f3(ph);
@@ -658,6 +688,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
             origin = scatter_pos;
             dir = wi;
             has_nee = true;
+            sampled = true;
             nee_beta = beta;
             nee_pdf = spdf;
         } else if (!is_hit) {
@@ -665,6 +696,11 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
             stop = true;
             terminal_no_rr = true;
             const int mode = (int)p.env_type;
+            // with the environment light-sampled, a sampled direction's escape
+            // takes the BSDF side of the MIS weight
+            float wenv = 1.0f;
+            if (p.env_light && (flags & F_SAMPLED))
+                wenv = power_heuristic(ps.nee_b[slot].w, env_pdf(s, dir) / (float)(p.num_lights + 1u));
             if (mode == 0) {
                 if (sdepth == 0) {
                     write_alb = true;
@@ -679,7 +715,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
                     new_alb = bg;
                     new_nrm = f3(0.0f);
                 }
-                rad += bg * beta;
+                rad += bg * beta * wenv;
             } else if (mode == 2) {
                 if (sdepth == 0) {
                     write_alb = true;
@@ -687,7 +723,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
                     new_nrm = f3(0.0f);
                     rad += p.background * beta;
                 } else {
-                    rad += env_lookup(s, dir) * beta;
+                    rad += env_lookup(s, dir) * beta * wenv;
                 }
             }
         } else {
@@ -713,6 +749,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
                     origin = h.wpos;
                     dir = normalize3(dir);
                     passthrough = true;
+                    keep_sampled = (flags & F_SAMPLED) != 0;
                 }
             }
             if (passthrough) {
@@ -742,7 +779,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
                 } else {
                     sdepth = min(sdepth + 1u, 255u);
                     const float3 wo = world_to_local(h.frame, -dir);
-                    LightSample ls = sample_light(s, p, h.wpos, rng);
+                    LightSample ls = sample_light(s, p, h.wpos, rng, !last);
                     if (!is_black(ls.radiance)) {
                         float3 wi = world_to_local(h.frame, ls.dir);
                         float3 F;
@@ -792,6 +829,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
                         beta *= clamp3(Fs / spdf, 0.0f, 1.0f);
                         has_nee = true;
                     }
+                    sampled = has_nee;
                     nee_beta = beta;
                     nee_pdf = spdf;
                 }
@@ -815,13 +853,14 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
             has_nee = false;
         }
 
-        const bool last = (d + 1u >= p.depth);
         const bool done = stop || last;
         uint32_t nf = F_ITEM | (inside ? F_INSIDE : 0u) | ((min(d + 1u, 255u)) << kDepthShift) | (sdepth << kSurfShift);
         if (done)
             nf |= F_DONE;
         if (has_shadow)
             nf |= F_SHADOW;
+        if (sampled || keep_sampled)
+            nf |= F_SAMPLED;
         // a continuing path's emitter ray shares origin and direction with its
         // next extension ray and is resolved from that traversal
         const bool fuse = has_nee && !done && p.zfar <= kExtTmax;
@@ -842,7 +881,7 @@ __global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues
             ps.sh_dir[slot] = f4(sh_dir, sh_tmax);
             ps.sh_c[slot] = f4(sh_c, 0.0f);
         }
-        if (has_nee)
+        if (sampled)
             ps.nee_b[slot] = f4(nee_beta, nee_pdf);
         want_conn = has_shadow || (has_nee && !fuse);
         want_done = done;
@@ -1000,7 +1039,7 @@ __device__ __forceinline__ void emitter_eval(const SceneView &s, const RenderPar
         float3 obj_o = xform_point(w2o, o);
         float dist = length3(obj_o - wp);
         float light_pdf = point_pdf * (dist * dist) / dp;
-        pdf = light_pdf * (1.0f / (float)p.num_lights);
+        pdf = light_pdf * (1.0f / (float)(p.num_lights + p.env_light));
     } else {
         pdf = 0.0f;
         em = f3(0.0f);

@@ -26,6 +26,7 @@ struct RenderParams {
     uint32_t num_lights;  // pathTracingData.lights.r
     uint32_t total_items; // width * height * batches
     uint32_t want_m2;
+    uint32_t env_light;   // 1: the environment is sampled as one more light (VVPT_RENDER_ENV_IS)
 };
 
 // Structure-of-arrays path state, one entry per slot. A slot runs one

@@ -136,11 +136,13 @@ class GpuScene:
 
     def render(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
                outputs: dict | None = None, profile: bool = False,
-               host_outputs: dict | None = None) -> RenderResult | None:
+               host_outputs: dict | None = None, env_is: bool = False) -> RenderResult | None:
         """Renders into new host arrays, into caller-provided host arrays
         (`host_outputs`), or into device pointers when `outputs` maps
-        radiance/albedo/normal/radiance_m2 to device addresses."""
-        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_PROFILE_KERNELS if profile else 0)
+        radiance/albedo/normal/radiance_m2 to device addresses. env_is: the
+        environment is importance sampled as a light (VVPT_RENDER_ENV_IS)."""
+        flags = ((N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_PROFILE_KERNELS if profile else 0) |
+                 (N.RENDER_ENV_IS if env_is else 0))
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         if host_outputs is not None:
             o = N.Outputs(host_outputs.get("radiance"), host_outputs.get("albedo"), host_outputs.get("normal"),
@@ -165,11 +167,11 @@ class GpuScene:
         return RenderResult(rad, alb, nrm, m2, self.ctx.stats(), info.samples // info.batch_size)
 
     def submit(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
-               outputs: dict | None = None) -> "Job":
+               outputs: dict | None = None, env_is: bool = False) -> "Job":
         """Queues a render on the context's job engine (vvpt_submit). Outputs go
         to new host arrays, or to device pointers when `outputs` maps
         radiance/albedo/normal/radiance_m2 to device addresses."""
-        flags = N.RENDER_WANT_BATCH_M2 if want_m2 else 0
+        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_ENV_IS if env_is else 0)
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         job = Job(self, info, want_m2)
         if outputs is not None:

@@ -264,7 +264,7 @@ def random_scene(seed: int, min_tris: int = 10_000, max_tris: int = 2_000_000, m
     rng = np.random.Generator(np.random.PCG64(seed + 7919))
     target = float(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris))))
     n_spheres = int(rng.integers(1, 9))
-    freq = max(2, int(round(math.sqrt(target / (20.0 * n_spheres)))))
+    freq = max(2, int(math.ceil(math.sqrt(target / (20.0 * n_spheres)))))
     centers = []
     for k in range(n_spheres):
         r = float(rng.uniform(0.06, 0.12))
@@ -331,6 +331,163 @@ def job_mix(seed: int, n_jobs: int, n_scenes: int) -> list[tuple[int, RenderInfo
                      RenderInfo(samples=spp, depth=8, batch_size=4, width=w, height=h, filename=f"job{j}",
                                 write_files=False)))
     return jobs
+
+
+def env_directions(width: int, height: int) -> np.ndarray:
+    """World direction of every texel centre of an equirect environment image
+    under the lookup mapping (u = atan2(z, x) * 0.1591 + 0.75 wrapped,
+    w = asin(y) * 0.3183 + 0.5): H x W x 3."""
+    u = (np.arange(width) + 0.5) / width
+    w = (np.arange(height) + 0.5) / height
+    x = np.mod(u - 0.25, 1.0)
+    lon = (x - 0.5) / 0.1591
+    lat = np.clip((w - 0.5) / 0.3183, -math.pi / 2, math.pi / 2)
+    lat, lon = np.meshgrid(lat, lon, indexing="ij")
+    return np.stack([np.cos(lat) * np.cos(lon), np.sin(lat), np.cos(lat) * np.sin(lon)], -1)
+
+
+def procedural_sky(width: int = 4096, height: int = 2048, sun_dir=(0.4, 0.55, -0.35), sun_peak: float = 5.0e4,
+                   sun_sigma_deg: float = 0.8, zenith=(0.25, 0.45, 0.9), horizon=(0.9, 0.85, 0.8),
+                   ground=(0.25, 0.22, 0.2)) -> np.ndarray:
+    """RGBA32F equirect sky: a vertical gradient (ground below the horizon,
+    horizon to zenith above) plus a Gaussian sun of angular sigma
+    `sun_sigma_deg` and peak radiance `sun_peak` (warm white)."""
+    d = env_directions(width, height)
+    y = d[..., 1:2]
+    t = np.clip(y, 0.0, 1.0) ** 0.5
+    sky = np.where(y >= 0.0, np.asarray(horizon) * (1 - t) + np.asarray(zenith) * t, np.asarray(ground))
+    sd = np.asarray(sun_dir, dtype=np.float64)
+    sd = sd / np.linalg.norm(sd)
+    ang = np.arccos(np.clip(d @ sd, -1.0, 1.0))
+    sig = math.radians(sun_sigma_deg)
+    sun = sun_peak * np.exp(-0.5 * (ang / sig) ** 2)[..., None] * np.asarray([1.0, 0.95, 0.85])
+    rgb = sky + sun
+    return np.concatenate([rgb, np.ones_like(rgb[..., :1])], -1).astype(np.float32)
+
+
+def sky_scene(seed: int = 1, width: int = 96, height: int = 64, samples: int = 16, depth: int = 8,
+              batch_size: int = 4, sky_w: int = 512, sky_h: int = 256, sun_peak: float = 5.0e3,
+              sun_sigma_deg: float = 2.0) -> tuple[Engine, RenderInfo]:
+    """Displaced spheres on a ground quad under a procedural sky with a small
+    bright sun (background mode 1): the case environment importance sampling
+    is for."""
+    engine = Engine()
+    scene = engine.scene
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ground = engine.create_material(MaterialLambert, "ground")
+    ground.albedo = [0.6, 0.6, 0.6, 1.0]
+    gq = mesh_from_triangles("ground", quad((-4, 0, -4), (4, 0, -4), (4, 0, 4), (-4, 0, 4)), QUAD_UV)
+    so = scene.add_scene_object("ground", Transform((0, 0, 0)))
+    so.mesh = engine.add_mesh(gq)
+    so.material = ground
+    for k in range(3):
+        mesh = engine.add_mesh(displaced_sphere(6, 1.0, 0.05, 3.0, rng))
+        if k == 1:
+            mat = engine.create_material(MaterialPBRStandard, f"ball{k}")
+            mat.albedo = [0.8, 0.6, 0.3, 1.0]
+            mat.roughness = 0.3
+            mat.metallic = 1.0
+        else:
+            mat = engine.create_material(MaterialLambert, f"ball{k}")
+            mat.albedo = [*rng.uniform(0.2, 0.9, size=3).tolist(), 1.0]
+        b = scene.add_scene_object(f"ball{k}", Transform((-1.2 + 1.2 * k, 0.5, 0.0), (0.5, 0.5, 0.5)))
+        b.mesh = mesh
+        b.material = mat
+    scene.camera.transform = Transform((0.0, 1.2, 4.0), (1, 1, 1), (math.radians(-12.0), 0.0, 0.0))
+    scene.environment_map = procedural_sky(sky_w, sky_h, sun_peak=sun_peak, sun_sigma_deg=sun_sigma_deg)
+    scene.environment_type = EnvironmentType.HDRI
+    scene.environment_intensity = 1.0
+    info = RenderInfo(samples=samples, depth=depth, batch_size=batch_size, width=width, height=height,
+                      filename="sky", write_files=False)
+    return engine, info
+
+
+def instanced_sky_scene(seed: int = 1, width: int = 3840, height: int = 2160, samples: int = 16, depth: int = 8,
+                        batch_size: int = 4, n_meshes: int = 8, n_instances: int = 512, freq: int = 45,
+                        n_lights: int = 32, sky_w: int = 4096, sky_h: int = 2048) -> tuple[Engine, RenderInfo]:
+    """Open scene under a procedural sky: `n_instances` random rigid placements
+    (rotation about a random axis, translation) of `n_meshes` seeded
+    displaced spheres of 20 * freq^2 triangles (8 x 40,500 = 324,000 unique,
+    512 instances = 20,736,000 instanced triangles), a ground quad, `n_lights`
+    emissive quads as mesh lights, a thin lens of radius 0.02, and a
+    4096 x 2048 sky (gradient plus a Gaussian sun of peak 5e4)."""
+    engine = Engine()
+    scene = engine.scene
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ground = engine.create_material(MaterialLambert, "ground")
+    ground.albedo = [0.45, 0.42, 0.38, 1.0]
+    gq = mesh_from_triangles("ground", quad((-40, 0, -40), (40, 0, -40), (40, 0, 40), (-40, 0, 40)), QUAD_UV)
+    so = scene.add_scene_object("ground", Transform((0, 0, 0)))
+    so.mesh = engine.add_mesh(gq)
+    so.material = ground
+    meshes, radii = [], []
+    for k in range(n_meshes):
+        r = float(rng.uniform(0.5, 1.2))
+        meshes.append(engine.add_mesh(displaced_sphere(freq, r, 0.08 * r, 2.5, rng)))
+        radii.append(r)
+    mats = []
+    for k in range(8):
+        if k % 2 == 0:
+            m = engine.create_material(MaterialLambert, f"diffuse{k}")
+        else:
+            m = engine.create_material(MaterialPBRStandard, f"pbr{k}")
+            m.roughness = float(rng.uniform(0.05, 0.8))
+            m.metallic = float(rng.random() < 0.4)
+        m.albedo = [*rng.uniform(0.15, 0.9, size=3).tolist(), 1.0]
+        mats.append(m)
+    for i in range(n_instances):
+        k = int(rng.integers(0, n_meshes))
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        ang = float(rng.uniform(0, 2 * math.pi))
+        q = (math.cos(ang / 2), *(math.sin(ang / 2) * axis).tolist())
+        pos = (float(rng.uniform(-30, 30)), radii[k] * 1.02, float(rng.uniform(-30, 30)))
+        o = scene.add_scene_object(f"inst{i}", Transform(pos, (1, 1, 1), q))
+        o.mesh = meshes[k]
+        o.material = mats[int(rng.integers(0, len(mats)))]
+    lq = engine.add_mesh(mesh_from_triangles("light_quad", quad((-0.5, 0, -0.5), (0.5, 0, -0.5), (0.5, 0, 0.5),
+                                                                (-0.5, 0, 0.5)), QUAD_UV))
+    for k in range(n_lights):
+        m = engine.create_material(MaterialLambert, f"lamp{k}")
+        m.albedo = [0.8, 0.8, 0.8, 1.0]
+        m.emissive = [*rng.uniform(0.6, 1.0, size=3).tolist(), float(rng.uniform(20.0, 80.0))]
+        pos = (float(rng.uniform(-25, 25)), float(rng.uniform(2.5, 4.0)), float(rng.uniform(-25, 25)))
+        o = scene.add_scene_object(f"lamp{k}", Transform(pos, (0.6, 0.6, 0.6), (math.pi, 0.0, 0.0)))
+        o.mesh = lq
+        o.material = m
+    cam = scene.camera
+    cam.transform = Transform((0.0, 6.0, 34.0), (1, 1, 1), (math.radians(-10.0), 0.0, 0.0))
+    cam.lens_radius = 0.02
+    cam.focal_distance = 30.0
+    scene.environment_map = procedural_sky(sky_w, sky_h, sun_peak=5.0e4, sun_sigma_deg=0.5)
+    scene.environment_type = EnvironmentType.HDRI
+    scene.environment_intensity = 1.0
+    info = RenderInfo(samples=samples, depth=depth, batch_size=batch_size, width=width, height=height,
+                      filename="instanced_sky", write_files=False)
+    return engine, info
+
+
+SERVING_RESOLUTIONS = [(256, 256), (512, 512)]
+SERVING_SPPS = [8, 16, 32]
+
+
+def serving_requests(seed: int, n_requests: int, n_scenes: int, mean_gap_ms: float = 50.0):
+    """(arrival ms, scene index, render info) per request: Poisson arrivals
+    (exponential gaps, mean `mean_gap_ms`), scenes from the pool of the
+    batched workload, resolution from {256^2, 512^2} and spp from {8, 16, 32}
+    (preview renders: about 3.1M paths per request, an offered load of about
+    61M paths/s at 50 ms gaps, below one GPU's throughput)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gaps = rng.exponential(mean_gap_ms, n_requests)
+    t = np.cumsum(gaps) - gaps[0]
+    out = []
+    for j in range(n_requests):
+        w, h = SERVING_RESOLUTIONS[int(rng.integers(0, len(SERVING_RESOLUTIONS)))]
+        spp = SERVING_SPPS[int(rng.integers(0, len(SERVING_SPPS)))]
+        out.append((float(t[j]), int(rng.integers(0, n_scenes)),
+                    RenderInfo(samples=spp, depth=8, batch_size=4, width=w, height=h, filename=f"req{j}",
+                               write_files=False)))
+    return out
 
 
 def cornell_medium(seed: int = 1, width: int = 1920, height: int = 1080, samples: int = 256, depth: int = 12,
