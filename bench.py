@@ -504,13 +504,86 @@ def run_serving(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def denoiser_flops(h: int, w: int, n: int = 1) -> float:
+    """Multiply-add FLOPs of one U-Net forward pass (2 per MAC, 3x3 taps)."""
+    from oracle import denoiser_oracle as D
+    lv_of = []
+    for l in range(D.LEVELS):
+        lv_of += [l, l]
+    for l in range(D.LEVELS - 2, -1, -1):
+        lv_of += [l, l]
+    lv_of.append(0)
+    total = 0.0
+    for (cin, cout, _), l in zip(D.layers(), lv_of):
+        total += 2.0 * 9 * cin * cout * n * (h >> l) * (w >> l)
+    return total
+
+
+def run_denoise(args) -> None:
+    """Denoiser inference at 3840 x 2160 (one frame) and one training step on
+    8 crops of 256^2, CUDA events on the library stream; roofline against the
+    measured dense BF16 peak."""
+    import torch
+
+    from vviewer_gb300 import Context
+    from vviewer_gb300.denoiser import Denoiser
+    ctx = Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    dn = Denoiser(ctx, seed=1)
+    H, W = 2160, 3840
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rad = torch.rand((H, W, 4), device="cuda", generator=g) * 4
+    alb = torch.rand((H, W, 4), device="cuda", generator=g)
+    nrm = torch.rand((H, W, 4), device="cuda", generator=g)
+    out = torch.empty((H, W, 4), device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        dn.apply(rad, alb, nrm, out)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dn.apply(rad, alb, nrm, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    infer_ms = sum(ms) / len(ms)
+    flops = denoiser_flops(H, W)
+    # training step, 8 x 256^2
+    tb = [torch.rand((8, 256, 256, 4), device="cuda", generator=g) for _ in range(4)]
+    for _ in range(3):
+        dn.train_step(*tb, lr=1e-4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        dn.train_step(*tb, lr=1e-4)
+    torch.cuda.synchronize()
+    train_ms = (time.perf_counter() - t0) / 5 * 1e3
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    achieved = flops / (infer_ms / 1e3) / 1e12
+    line = {"metric": "denoised frames/s", "value": 1e3 / infer_ms, "unit": "frames/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": infer_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic inputs",
+            "config": {"workload": "denoise_3840x2160", "network": "U-Net 5 levels 32/48/64/96/128, 3x3",
+                       "train_batch": "8 x 256^2"},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "flops_per_frame": flops},
+            "train_step_ms": train_ms, "train_tflops": 3 * denoiser_flops(256, 256, 8) / (train_ms / 1e3) / 1e12}
+    dn.close()
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cornell_medium", "cornell", "instanced_sky", "batched64", "serving512"],
+    ap.add_argument("--workload", choices=["cornell_medium", "cornell", "instanced_sky", "batched64", "serving512",
+                                           "denoise"],
                     default="cornell_medium")
     ap.add_argument("--sequential", action="store_true", help="batched64: also time the jobs one by one")
     ap.add_argument("--requests", type=int, default=512, help="serving512: number of requests")
@@ -525,6 +598,8 @@ def main():
         run_batched(args)
     elif args.workload == "serving512":
         run_serving(args)
+    elif args.workload == "denoise":
+        run_denoise(args)
     else:
         run_ours(args)
 

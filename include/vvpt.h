@@ -446,6 +446,59 @@ VVPT_API vvpt_status vvpt_render_batch(vvpt_ctx *ctx,
                                        const vvpt_render_info *infos,
                                        const vvpt_outputs *outputs);
 
+/* ---- Learned denoiser ------------------------------------------------------
+ *
+ * Stands in for the reference's OpenImageDenoise call in storeToDisk
+ * (VulkanRendererPathTracing.cpp:985-1018): a 5-level U-Net (3x3 convs of
+ * 32/48/64/96/128 channels) over noisy radiance, albedo and normal, trained on
+ * the GPU on pairs the tracer renders (few-spp inputs, many-spp targets).
+ * Every convolution (forward, input gradient, weight gradient) runs on the
+ * BF16 tensor cores with FP32 accumulation in the library's own kernels;
+ * parameters are FP32 with an Adam optimiser. Images are device RGBA32F
+ * buffers (A ignored on input, 1 on output); width and height must be
+ * multiples of 16. Parameter layout: per layer, weights [cout][3][3][cin]
+ * then biases [cout]; layers: encoder (2 per level), decoder (2 per level,
+ * coarsest first), output. */
+typedef struct vvpt_denoiser vvpt_denoiser;
+
+typedef struct vvpt_denoise_batch {
+    const float *radiance; /* count x height x width RGBA32F, device */
+    const float *albedo;
+    const float *normal;
+    const float *target;   /* high-spp radiance, same layout */
+    uint32_t count;
+    uint32_t width;
+    uint32_t height;
+} vvpt_denoise_batch;
+
+/* New network with seeded initial weights (He-normal; the output layer
+ * small). */
+VVPT_API vvpt_status vvpt_denoiser_create(vvpt_ctx *ctx, uint64_t seed, vvpt_denoiser **out_denoiser);
+VVPT_API vvpt_status vvpt_denoiser_destroy(vvpt_denoiser *denoiser);
+VVPT_API vvpt_status vvpt_denoiser_num_params(vvpt_denoiser *denoiser, uint64_t *out_count);
+VVPT_API vvpt_status vvpt_denoiser_get_params(vvpt_denoiser *denoiser, float *host_params, uint64_t count);
+VVPT_API vvpt_status vvpt_denoiser_set_params(vvpt_denoiser *denoiser, const float *host_params, uint64_t count);
+/* Loss (mean absolute error of log(1 + radiance)) and its gradient with
+ * respect to every parameter, copied to the host; parameters unchanged. */
+VVPT_API vvpt_status vvpt_denoiser_gradients(vvpt_denoiser *denoiser,
+                                             const vvpt_denoise_batch *batch,
+                                             float *host_grads,
+                                             uint64_t count,
+                                             float *out_loss);
+/* One Adam step (beta 0.9 / 0.999) on the batch; returns the loss before it. */
+VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *denoiser,
+                                              const vvpt_denoise_batch *batch,
+                                              float learning_rate,
+                                              float *out_loss);
+/* Denoises one image: out = exp(network(log1p radiance, albedo, normal)) - 1. */
+VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *denoiser,
+                                         const float *radiance,
+                                         const float *albedo,
+                                         const float *normal,
+                                         float *out,
+                                         uint32_t width,
+                                         uint32_t height);
+
 #ifdef __cplusplus
 }
 #endif

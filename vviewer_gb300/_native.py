@@ -143,6 +143,11 @@ class EngineStats(C.Structure):
                 ("running", C.c_uint32), ("finished", C.c_uint32), ("slots", C.c_uint32)]
 
 
+class DenoiseBatch(C.Structure):
+    _fields_ = [("radiance", C.c_void_p), ("albedo", C.c_void_p), ("normal", C.c_void_p), ("target", C.c_void_p),
+                ("count", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 _SIGNATURES = {
@@ -171,6 +176,16 @@ _SIGNATURES = {
     "vvpt_job_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "vvpt_set_budget": (C.c_int, [C.c_void_p, C.c_uint64]),
     "vvpt_engine_stats_get": (C.c_int, [C.c_void_p, C.POINTER(EngineStats)]),
+    "vvpt_denoiser_create": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "vvpt_denoiser_destroy": (C.c_int, [C.c_void_p]),
+    "vvpt_denoiser_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "vvpt_denoiser_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "vvpt_denoiser_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "vvpt_denoiser_gradients": (C.c_int, [C.c_void_p, C.POINTER(DenoiseBatch), C.c_void_p, C.c_uint64,
+                                          C.POINTER(C.c_float)]),
+    "vvpt_denoiser_train_step": (C.c_int, [C.c_void_p, C.POINTER(DenoiseBatch), C.c_float, C.POINTER(C.c_float)]),
+    "vvpt_denoiser_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                      C.c_uint32]),
     "vvpt_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(SceneData),
                                     C.POINTER(RenderInfo), C.POINTER(Outputs)]),
 }

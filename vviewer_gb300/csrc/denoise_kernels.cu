@@ -1,0 +1,495 @@
+// Denoiser kernels (denoise_kernels.cuh). The convolutions are implicit GEMMs
+// on the BF16 tensor cores through warp-level mma.sync m16n8k16 with FP32
+// accumulators; operand tiles are staged in shared memory and read with
+// ldmatrix.
+#include <algorithm>
+
+#include "denoise_kernels.cuh"
+
+namespace vvdn {
+
+namespace {
+
+constexpr int kTileP = 64;  // pixels per block
+constexpr int kTileC = 64;  // output channels per block
+constexpr int kChunk = 32;  // input channels per K step
+constexpr int kPad = 40;    // shared row stride in bf16 (80 B: ldmatrix rows hit distinct banks)
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// 16 bf16 (two 16-byte vectors) or zeros
+__device__ __forceinline__ void load16(const bf16 *src, bool ok, bf16 *dst)
+{
+    uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+    if (ok) {
+        v0 = *reinterpret_cast<const uint4 *>(src);
+        v1 = *reinterpret_cast<const uint4 *>(src + 8);
+    }
+    *reinterpret_cast<uint4 *>(dst) = v0;
+    *reinterpret_cast<uint4 *>(dst + 8) = v1;
+}
+
+// Block: 128 threads = 4 warps; tile 64 pixels x 64 output channels; warp w
+// owns pixels [16w, 16w + 16) x all 64 channels (8 n-tiles of 8).
+__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
+{
+    __shared__ __align__(16) bf16 As[kTileP][kPad];
+    __shared__ __align__(16) bf16 Bs[kTileC][kPad];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)a.n * a.h * a.wd;
+    const long p0 = (long)blockIdx.x * kTileP;
+    const int c0 = blockIdx.y * kTileC;
+    // this thread's load row and 16-channel group
+    const int lr = tid >> 1, lg = (tid & 1) * 16;
+    const long lp = p0 + lr;
+    int ln = 0, ly = 0, lx = 0;
+    if (lp < P) {
+        ln = (int)(lp / ((long)a.h * a.wd));
+        const int rem = (int)(lp - (long)ln * a.h * a.wd);
+        ly = rem / a.wd;
+        lx = rem - ly * a.wd;
+    }
+    float acc[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+
+    for (int tap = 0; tap < 9; tap++) {
+        const int yy = ly + tap / 3 - 1, xx = lx + tap % 3 - 1;
+        const bool pix_ok = lp < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
+        const bf16 *src_row = a.in + (((long)ln * a.h + yy) * a.wd + xx) * a.cin;
+        const int wc = c0 + lr;
+        const bf16 *w_row = a.wgt + ((long)wc * 9 + tap) * a.cin;
+        for (int ci0 = 0; ci0 < a.cin; ci0 += kChunk) {
+            const int ci = ci0 + lg;
+            load16(src_row + ci, pix_ok && ci < a.cin, &As[lr][lg]);
+            load16(w_row + ci, wc < a.cout && ci < a.cin, &Bs[lr][lg]);
+            __syncthreads();
+#pragma unroll
+            for (int ks = 0; ks < kChunk; ks += 16) {
+                uint32_t a0, a1, a2, a3;
+                ldsm_x4(smem_addr(&As[warp * 16 + (lane & 15)][ks + (lane >> 4) * 8]), a0, a1, a2, a3);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    uint32_t b0, b1, b2, b3;
+                    ldsm_x4(smem_addr(&Bs[16 * j + (lane & 7) + ((lane >> 4) << 3)][ks + ((lane >> 3) & 1) * 8]),
+                            b0, b1, b2, b3);
+                    mma_bf16(acc[2 * j], a0, a1, a2, a3, b0, b1);
+                    mma_bf16(acc[2 * j + 1], a0, a1, a2, a3, b2, b3);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // epilogue: c0,c1 at (row g, cols 2t, 2t+1), c2,c3 at row g + 8
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const long p = p0 + warp * 16 + g + half * 8;
+        if (p >= P)
+            continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int col = c0 + 8 * j + 2 * t;
+            if (col >= a.cout)
+                continue;
+            float v0 = acc[j][2 * half], v1 = acc[j][2 * half + 1];
+            if (a.bias) {
+                v0 += a.bias[col];
+                v1 += a.bias[col + 1];
+            }
+            if (a.relu) {
+                v0 = fmaxf(v0, 0.0f);
+                v1 = fmaxf(v1, 0.0f);
+            }
+            const long o = p * a.cout + col;
+            if (a.mask) {
+                const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(a.mask + o);
+                if (!(__bfloat162float(m.x) > 0.0f))
+                    v0 = 0.0f;
+                if (!(__bfloat162float(m.y) > 0.0f))
+                    v1 = 0.0f;
+            }
+            if (a.out_f32)
+                *reinterpret_cast<float2 *>(reinterpret_cast<float *>(a.out) + o) = make_float2(v0, v1);
+            else
+                *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<bf16 *>(a.out) + o) = __floats2bfloat162_rn(v0, v1);
+        }
+    }
+}
+
+// Weight gradient for one tap: block tile 64 output channels x 64 input
+// channels, K = a slice of pixels in steps of 32. Warp w owns output
+// channels [16w, 16w + 16). Partial sums are added to dw with atomics.
+constexpr int kWgK = 32;
+__global__ void __launch_bounds__(128) k_conv3x3_wgrad(const bf16 *__restrict__ dout, int cout,
+                                                       const bf16 *__restrict__ in, int cin, int n, int h, int w,
+                                                       float *dw, long slice)
+{
+    __shared__ __align__(16) bf16 Ds[kWgK][kTileC + 8]; // [pixel][cout]
+    __shared__ __align__(16) bf16 Xs[kWgK][kTileC + 8]; // [pixel][cin]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tap = blockIdx.y % 9;
+    const int tiles_ci = (cin + kTileC - 1) / kTileC;
+    const int ct = blockIdx.y / 9;
+    const int co0 = (ct / tiles_ci) * kTileC, ci0 = (ct % tiles_ci) * kTileC;
+    const long P = (long)n * h * w;
+    const long pbeg = (long)blockIdx.x * slice, pend = min(P, pbeg + slice);
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    // load mapping: row = tid / 4 (pixel), group = (tid % 4) * 16 channels
+    const int lr = tid >> 2, lg = (tid & 3) * 16;
+    float acc[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    for (long pb = pbeg; pb < pend; pb += kWgK) {
+        const long p = pb + lr;
+        bool ok = p < pend;
+        int pn = 0, py = 0, px = 0;
+        if (ok) {
+            pn = (int)(p / ((long)h * w));
+            const int rem = (int)(p - (long)pn * h * w);
+            py = rem / w;
+            px = rem - py * w;
+        }
+        const int co = co0 + lg, ci = ci0 + lg;
+        load16(dout + p * cout + co, ok && co < cout, &Ds[lr][lg]);
+        const int yy = py + dy, xx = px + dx;
+        const bool xok = ok && yy >= 0 && yy < h && xx >= 0 && xx < w && ci < cin;
+        load16(in + (((long)pn * h + yy) * w + xx) * cin + ci, xok, &Xs[lr][lg]);
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < kWgK; ks += 16) {
+            // A[m = cout][k = pixel] from Ds[k][m] (transposed load)
+            uint32_t a0, a1, a2, a3;
+            ldsm_x4_t(smem_addr(&Ds[ks + (lane & 7) + ((lane >> 4) << 3)][warp * 16 + ((lane >> 3) & 1) * 8]), a0, a1,
+                      a2, a3);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                // B[k = pixel][n = cin] from Xs[k][n] (transposed load): two n-tiles
+                uint32_t b0, b1, b2, b3;
+                ldsm_x4_t(smem_addr(&Xs[ks + (lane & 7) + ((lane >> 3) & 1) * 8][16 * j + (lane >> 4) * 8]), b0, b1,
+                          b2, b3);
+                mma_bf16(acc[2 * j], a0, a1, a2, a3, b0, b1);
+                mma_bf16(acc[2 * j + 1], a0, a1, a2, a3, b2, b3);
+            }
+        }
+        __syncthreads();
+    }
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const int co = co0 + warp * 16 + g + half * 8;
+        if (co >= cout)
+            continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int ci = ci0 + 8 * j + 2 * t;
+            if (ci >= cin)
+                continue;
+            float *d = dw + ((long)co * 9 + tap) * cin + ci;
+            atomicAdd(d, acc[j][2 * half]);
+            atomicAdd(d + 1, acc[j][2 * half + 1]);
+        }
+    }
+}
+
+__global__ void k_bias_grad(const bf16 *dout, int cout, long P, float *dbias)
+{
+    // one block per 8 channels-group x pixel slice; simple strided sums
+    const int c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= cout)
+        return;
+    float s = 0.0f;
+    for (long p = blockIdx.x; p < P; p += gridDim.x)
+        s += __bfloat162float(dout[p * cout + c]);
+    atomicAdd(dbias + c, s);
+}
+
+__global__ void k_transform_weights(const bf16 *w, bf16 *wt, int cout, int cin)
+{
+    const long total = (long)cout * 9 * cin;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ci = (int)(i % cin);
+        const int tap = (int)((i / cin) % 9);
+        const int co = (int)(i / ((long)cin * 9));
+        wt[((long)ci * 9 + (8 - tap)) * cout + co] = w[i];
+    }
+}
+
+__global__ void k_to_bf16(const float *src, bf16 *dst, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+__global__ void k_pack_features(const float4 *rad, const float4 *alb, const float4 *nrm, bf16 *x, int npix)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const float4 r = rad[p], a = alb[p], q = nrm[p];
+        __align__(16) bf16 v[16];
+        v[0] = __float2bfloat16_rn(log1pf(fmaxf(r.x, 0.0f)));
+        v[1] = __float2bfloat16_rn(log1pf(fmaxf(r.y, 0.0f)));
+        v[2] = __float2bfloat16_rn(log1pf(fmaxf(r.z, 0.0f)));
+        v[3] = __float2bfloat16_rn(a.x);
+        v[4] = __float2bfloat16_rn(a.y);
+        v[5] = __float2bfloat16_rn(a.z);
+        v[6] = __float2bfloat16_rn(q.x);
+        v[7] = __float2bfloat16_rn(q.y);
+        v[8] = __float2bfloat16_rn(q.z);
+#pragma unroll
+        for (int k = 9; k < 16; k++)
+            v[k] = __float2bfloat16_rn(0.0f);
+        uint4 *dst = reinterpret_cast<uint4 *>(x + (long)p * 16);
+        dst[0] = *reinterpret_cast<const uint4 *>(&v[0]);
+        dst[1] = *reinterpret_cast<const uint4 *>(&v[8]);
+    }
+}
+
+__global__ void k_pack_target(const float4 *t, float *t3, int npix)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const float4 v = t[p];
+        t3[3 * p] = log1pf(fmaxf(v.x, 0.0f));
+        t3[3 * p + 1] = log1pf(fmaxf(v.y, 0.0f));
+        t3[3 * p + 2] = log1pf(fmaxf(v.z, 0.0f));
+    }
+}
+
+__global__ void k_avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c)
+{
+    const int ho = h / 2, wo = w / 2;
+    const long total = (long)n * ho * wo * c;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long q = i / c;
+        const int x = (int)(q % wo), y = (int)((q / wo) % ho), b = (int)(q / ((long)wo * ho));
+        const long base = (((long)b * h + 2 * y) * w + 2 * x) * c + ch;
+        const float s = __bfloat162float(in[base]) + __bfloat162float(in[base + c]) +
+                        __bfloat162float(in[base + (long)w * c]) + __bfloat162float(in[base + (long)w * c + c]);
+        out[i] = __float2bfloat16_rn(0.25f * s);
+    }
+}
+
+__global__ void k_upcat(const bf16 *coarse, int cc, const bf16 *skip, int cs, bf16 *out, int n, int h, int w)
+{
+    const int ct = cc + cs;
+    const long total = (long)n * h * w * ct;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % ct);
+        const long p = i / ct;
+        if (ch < cc) {
+            const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long)w * h));
+            out[i] = coarse[(((long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * cc + ch];
+        } else {
+            out[i] = skip[p * cs + (ch - cc)];
+        }
+    }
+}
+
+__global__ void k_upcat_backward_coarse(const bf16 *dcat, int cc, int cs, bf16 *dcoarse, int n, int h, int w)
+{
+    const int ct = cc + cs, ho = h / 2, wo = w / 2;
+    const long total = (long)n * ho * wo * cc;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % cc);
+        const long q = i / cc;
+        const int x = (int)(q % wo), y = (int)((q / wo) % ho), b = (int)(q / ((long)wo * ho));
+        const long base = (((long)b * h + 2 * y) * w + 2 * x) * ct + ch;
+        const float s = __bfloat162float(dcat[base]) + __bfloat162float(dcat[base + ct]) +
+                        __bfloat162float(dcat[base + (long)w * ct]) + __bfloat162float(dcat[base + (long)w * ct + ct]);
+        dcoarse[i] = __float2bfloat16_rn(s);
+    }
+}
+
+__global__ void k_upcat_backward_skip(const bf16 *dcat, int cc, int cs, bf16 *dskip, long npix)
+{
+    const int ct = cc + cs;
+    const long total = npix * cs;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % cs);
+        const long p = i / cs;
+        dskip[i] = dcat[p * ct + cc + ch];
+    }
+}
+
+__global__ void k_pool_backward_combine(const bf16 *dskip, const bf16 *dpooled, const bf16 *e, bf16 *de, int n, int h,
+                                        int w, int c)
+{
+    const long total = (long)n * h * w * c;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        const long p = i / c;
+        const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long)w * h));
+        float v = 0.25f * __bfloat162float(dpooled[(((long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch]);
+        if (dskip)
+            v += __bfloat162float(dskip[i]);
+        if (!(__bfloat162float(e[i]) > 0.0f))
+            v = 0.0f;
+        de[i] = __float2bfloat16_rn(v);
+    }
+}
+
+__global__ void k_l1_loss(const float *out, int cout, const float *t3, bf16 *dout, float *loss_sum, int npix)
+{
+    float local = 0.0f;
+    const float scale = 1.0f / (3.0f * (float)npix);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        for (int c = 0; c < cout; c++) {
+            float g = 0.0f;
+            if (c < 3) {
+                const float d = out[(long)p * cout + c] - t3[3 * p + c];
+                local += fabsf(d);
+                g = d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f);
+            }
+            dout[(long)p * cout + c] = __float2bfloat16_rn(g);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(loss_sum, local);
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2, float eps,
+                       float c1, float c2)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+__global__ void k_unpack_output(const float *y, int cout, float4 *out, int npix)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const float *v = y + (long)p * cout;
+        out[p] = make_float4(expm1f(fmaxf(v[0], 0.0f)), expm1f(fmaxf(v[1], 0.0f)), expm1f(fmaxf(v[2], 0.0f)), 1.0f);
+    }
+}
+
+int grid_for(long n, int block = 256)
+{
+    return (int)std::max<long>(1, std::min<long>((n + block - 1) / block, 152L * 16));
+}
+
+}  // namespace
+
+void conv3x3(const ConvArgs &a, cudaStream_t s)
+{
+    const long P = (long)a.n * a.h * a.wd;
+    dim3 grid((unsigned)((P + kTileP - 1) / kTileP), (unsigned)((a.cout + kTileC - 1) / kTileC));
+    k_conv3x3<<<grid, 128, 0, s>>>(a);
+}
+
+void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw, float *dbias,
+                   cudaStream_t s)
+{
+    const long P = (long)n * h * w;
+    const int tiles = ((cout + kTileC - 1) / kTileC) * ((cin + kTileC - 1) / kTileC);
+    // about 4 blocks per SM over all taps and tiles
+    long slices = std::max<long>(1, (152L * 4) / (9L * tiles));
+    long slice = (P + slices - 1) / slices;
+    slice = std::max<long>(kWgK, (slice + kWgK - 1) / kWgK * kWgK);
+    slices = (P + slice - 1) / slice;
+    dim3 grid((unsigned)slices, (unsigned)(9 * tiles));
+    k_conv3x3_wgrad<<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
+    if (dbias) {
+        dim3 gb((unsigned)std::min<long>(P, 1024), (unsigned)((cout + 127) / 128));
+        k_bias_grad<<<gb, 128, 0, s>>>(dout, cout, P, dbias);
+    }
+}
+
+void transform_weights(const bf16 *w, bf16 *wt, int cout, int cin, cudaStream_t s)
+{
+    k_transform_weights<<<grid_for((long)cout * 9 * cin), 256, 0, s>>>(w, wt, cout, cin);
+}
+
+void to_bf16(const float *src, bf16 *dst, size_t n, cudaStream_t s)
+{
+    k_to_bf16<<<grid_for((long)n), 256, 0, s>>>(src, dst, n);
+}
+
+void pack_features(const float *radiance, const float *albedo, const float *normal, bf16 *x, int npix, cudaStream_t s)
+{
+    k_pack_features<<<grid_for(npix), 256, 0, s>>>(reinterpret_cast<const float4 *>(radiance),
+                                                   reinterpret_cast<const float4 *>(albedo),
+                                                   reinterpret_cast<const float4 *>(normal), x, npix);
+}
+
+void pack_target(const float *target, float *t3, int npix, cudaStream_t s)
+{
+    k_pack_target<<<grid_for(npix), 256, 0, s>>>(reinterpret_cast<const float4 *>(target), t3, npix);
+}
+
+void avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c, cudaStream_t s)
+{
+    k_avgpool2<<<grid_for((long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(in, out, n, h, w, c);
+}
+
+void upcat(const bf16 *coarse, int cc, const bf16 *skip, int cs, bf16 *out, int n, int h, int w, cudaStream_t s)
+{
+    k_upcat<<<grid_for((long)n * h * w * (cc + cs)), 256, 0, s>>>(coarse, cc, skip, cs, out, n, h, w);
+}
+
+void upcat_backward(const bf16 *dcat, int cc, int cs, bf16 *dcoarse, bf16 *dskip, int n, int h, int w, cudaStream_t s)
+{
+    k_upcat_backward_coarse<<<grid_for((long)n * (h / 2) * (w / 2) * cc), 256, 0, s>>>(dcat, cc, cs, dcoarse, n, h, w);
+    if (dskip)
+        k_upcat_backward_skip<<<grid_for((long)n * h * w * cs), 256, 0, s>>>(dcat, cc, cs, dskip, (long)n * h * w);
+}
+
+void pool_backward_combine(const bf16 *dskip, const bf16 *dpooled, const bf16 *e, bf16 *de, int n, int h, int w, int c,
+                           cudaStream_t s)
+{
+    k_pool_backward_combine<<<grid_for((long)n * h * w * c), 256, 0, s>>>(dskip, dpooled, e, de, n, h, w, c);
+}
+
+void l1_loss(const float *out, int cout, const float *t3, bf16 *dout, float *loss_sum, int npix, cudaStream_t s)
+{
+    k_l1_loss<<<grid_for(npix), 256, 0, s>>>(out, cout, t3, dout, loss_sum, npix);
+}
+
+void adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2, float eps, int t,
+          cudaStream_t s)
+{
+    const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
+    k_adam<<<grid_for((long)n), 256, 0, s>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+}
+
+void unpack_output(const float *y, int cout, float *out_rgba, int npix, cudaStream_t s)
+{
+    k_unpack_output<<<grid_for(npix), 256, 0, s>>>(y, cout, reinterpret_cast<float4 *>(out_rgba), npix);
+}
+
+}  // namespace vvdn

@@ -1,0 +1,70 @@
+// Kernels of the learned denoiser: BF16 tensor-core 3x3 convolutions as
+// implicit GEMMs (forward, input gradient, weight gradient) with FP32
+// accumulation, and the elementwise kernels around them (feature packing,
+// 2x2 average pool, nearest upsample + concat, L1 loss in the log domain,
+// Adam). Activations are NHWC bf16, weights [Cout][3][3][Cin] bf16 with FP32
+// master copies. Channel counts (inputs and outputs) are multiples of 16.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vvdn {
+
+typedef __nv_bfloat16 bf16;
+
+struct ConvArgs {
+    const bf16 *in;    // [P][cin]
+    int cin;
+    const bf16 *wgt;   // [cout][9][cin]
+    const float *bias; // [cout] or null
+    void *out;         // [P][cout] bf16, or f32 when out_f32
+    int cout;
+    int out_f32;
+    int relu;
+    const bf16 *mask;  // [P][cout] or null: output *= (mask > 0)
+    int n, h, wd;      // P = n * h * wd
+};
+
+// out = act(conv3x3(in, w) + bias) (zero padding); with transformed weights
+// (w_t[ci][8 - tap][co]) and a mask the same kernel is the input gradient.
+void conv3x3(const ConvArgs &a, cudaStream_t s);
+
+// dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
+// dbias[co] += sum_p dout[p][co] (dbias may be null).
+void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw,
+                   float *dbias, cudaStream_t s);
+
+// w_t[ci][8 - tap][co] = w[co][tap][ci]
+void transform_weights(const bf16 *w, bf16 *wt, int cout, int cin, cudaStream_t s);
+
+// f32 master weights -> bf16 copy
+void to_bf16(const float *src, bf16 *dst, size_t n, cudaStream_t s);
+
+// Input features from RGBA32F buffers: log(1 + max(radiance, 0)), albedo,
+// normal, zeros to 16 channels. `target` (optional) -> log(1 + max(t, 0)),
+// 3 floats per pixel.
+void pack_features(const float *radiance, const float *albedo, const float *normal, bf16 *x, int npix,
+                   cudaStream_t s);
+void pack_target(const float *target, float *t3, int npix, cudaStream_t s);
+
+void avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c, cudaStream_t s);
+// out[.., 0:cc] = nearest-upsampled coarse (h/2 x w/2), out[.., cc:cc+cs] = skip
+void upcat(const bf16 *coarse, int cc, const bf16 *skip, int cs, bf16 *out, int n, int h, int w, cudaStream_t s);
+// split the gradient of an upcat: dcoarse = sum over the 2x2 block of the
+// first cc channels; dskip = the rest
+void upcat_backward(const bf16 *dcat, int cc, int cs, bf16 *dcoarse, bf16 *dskip, int n, int h, int w,
+                    cudaStream_t s);
+// de = (dskip + dpooled[p / 2] / 4) * (e > 0); dskip may be null
+void pool_backward_combine(const bf16 *dskip, const bf16 *dpooled, const bf16 *e, bf16 *de, int n, int h, int w,
+                           int c, cudaStream_t s);
+// L1 loss between out[.., 0:3] (f32, stride cout) and t3; dout (bf16, stride
+// cout, zero beyond channel 3) = sign(out - t) / (3 * npix); loss_sum += |diff|
+void l1_loss(const float *out, int cout, const float *t3, bf16 *dout, float *loss_sum, int npix, cudaStream_t s);
+// Adam (Kingma and Ba 2015) with bias correction; t = step number from 1
+void adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2, float eps, int t,
+          cudaStream_t s);
+// out RGBA32F = exp(max(y, 0)) - 1 for the first 3 channels, A = 1
+void unpack_output(const float *y, int cout, float *out_rgba, int npix, cudaStream_t s);
+
+}  // namespace vvdn

@@ -208,17 +208,13 @@ __device__ __forceinline__ float3 wt_xform_vector(const float4 *rows, const floa
 }
 
 // Closest hit over all TLAS instances among candidates strictly after
-// `after`. One stack serves both levels: entering an instance transforms the
-// ray into its object space and pushes a return marker; popping the marker
-// restores the world-space ray. The loop alternates two phases (the
-// "while-while" traversal of Aila and Laine, HPG 2009, with speculative
-// traversal): a node phase that visits nodes until this lane holds a leaf,
-// and a triangle phase that tests the held leaf. A lane that already holds a
-// leaf keeps visiting nodes of the same instance while other lanes of its
-// warp still look for one, so the warp enters the triangle phase with most
-// lanes busy. Visiting order never changes the result: culling is
-// conservative and ties resolve by (t, instance, primitive). `err` receives
-// status bits.
+// `after`, as one flat loop over a single stack. Every loop step is one of:
+// a triangle test, a node visit (both children's boxes), or a stack
+// transition (enter an instance: transform the ray into its object space and
+// push a return marker; pop the marker: back to the world-space ray). Keeping
+// the two levels in one loop keeps a warp's lanes in step: a lane inside an
+// instance never holds lanes that are still in the TLAS, as nested per-level
+// loops would. `err` receives status bits.
 constexpr int kTagNode = 0, kTagLeaf = 1, kTagInst = 2, kTagReturn = 3;
 
 __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
@@ -238,8 +234,8 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     uint32_t inst_id = kNoHit;
     uint32_t node_base = s.tlas_root, tri_base = 0;
     bool in_blas = false;
-    int node = 0;                       // inner node to visit (local index), -1 none
-    int leaf_first = 0, leaf_count = 0; // held leaf: triangles still to test (local indices)
+    int node = 0;                 // inner node to visit (local index), -1 none
+    int leaf_first = 0, leaf_count = 0; // triangles still to test (local indices)
     int2 stack[kTraversalStack];
     int sp = 0;
     auto push = [&](int value, int tag, int count) {
@@ -249,92 +245,7 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             err |= kErrStackOverflow;
     };
     for (;;) {
-        // ---- node phase
-        for (;;) {
-            if (node >= 0) {
-                const BVHNode n = load_node(s.nodes, (int)node_base + node);
-                float tl, tr;
-                const float far_t = cull_far(best.t, slack);
-                box2(n, co, cinvd, box_tmin, far_t, tl, tr);
-                const bool hl = tl <= far_t && n.c.x >= 0;
-                const bool hr = tr <= far_t && n.c.y >= 0;
-                // near child first
-                const bool swap = hl && hr && tr < tl;
-                int next = -1;
-#pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const bool right = (k == 0) == swap;
-                    const bool h = right ? hr : hl;
-                    if (!h)
-                        continue;
-                    const int idx = right ? n.c.y : n.c.x;
-                    const int cnt = right ? n.c.w : n.c.z;
-                    if (cnt == 0) {
-                        if (next < 0)
-                            next = idx;
-                        else
-                            push(idx, kTagNode, 0);
-                    } else if (in_blas) {
-                        if (leaf_count == 0) {
-                            leaf_first = idx;
-                            leaf_count = cnt;
-                        } else {
-                            push(idx, kTagLeaf, cnt);
-                        }
-                    } else {
-                        push(idx, kTagInst, cnt);
-                    }
-                }
-                node = next;
-            } else {
-                if (sp == 0)
-                    break;
-                const int2 e = stack[sp - 1];
-                const int tag = (int)((unsigned)e.y >> 28);
-                const int cnt = e.y & 0x0FFFFFFF;
-                // a held leaf is tested before the ray changes space or a
-                // second leaf is taken
-                if (leaf_count > 0 && tag != kTagNode)
-                    break;
-                sp--;
-                if (tag == kTagNode) {
-                    node = e.x;
-                } else if (tag == kTagLeaf) {
-                    leaf_first = e.x;
-                    leaf_count = cnt;
-                } else if (tag == kTagInst) {
-                    if (cnt > 1)
-                        push(e.x + 1, kTagInst, cnt - 1);
-                    inst_id = __ldg(s.tlas_order + e.x);
-                    const DevInstance &inst = s.instances[inst_id];
-                    const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
-                    co = wt_xform_point(rows, o);
-                    const float3 cd = wt_xform_vector(rows, d);
-                    cinvd = safe_inv(cd);
-                    wr = wt_setup(co, cd);
-                    node_base = inst.node_offset;
-                    tri_base = inst.tri_offset;
-                    in_blas = true;
-                    push(0, kTagReturn, 0);
-                    node = 0;
-                } else {
-                    // back to the TLAS
-                    co = o;
-                    cinvd = winvd;
-                    node_base = s.tlas_root;
-                    in_blas = false;
-                    inst_id = kNoHit;
-                }
-            }
-            // leave once this lane holds a leaf and no lane of the warp that
-            // is still here lacks one (a heuristic: any lane subset is correct)
-            if (leaf_count > 0 && __all_sync(__activemask(), leaf_count > 0))
-                break;
-        }
-        if (leaf_count == 0)
-            break; // node phase ended with an empty stack: done
-        // ---- triangle phase
-        do {
+        if (leaf_count > 0) {
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
             const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
             const uint32_t prim = __float_as_uint(p0.w);
@@ -349,7 +260,78 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             }
             leaf_first++;
             leaf_count--;
-        } while (leaf_count > 0);
+            continue;
+        }
+        if (node >= 0) {
+            const BVHNode n = load_node(s.nodes, (int)node_base + node);
+            float tl, tr;
+            const float far_t = cull_far(best.t, slack);
+            box2(n, co, cinvd, box_tmin, far_t, tl, tr);
+            const bool hl = tl <= far_t && n.c.x >= 0;
+            const bool hr = tr <= far_t && n.c.y >= 0;
+            // near child first
+            const bool swap = hl && hr && tr < tl;
+            int next = -1;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const bool right = (k == 0) == swap;
+                const bool h = right ? hr : hl;
+                if (!h)
+                    continue;
+                const int idx = right ? n.c.y : n.c.x;
+                const int cnt = right ? n.c.w : n.c.z;
+                if (cnt == 0) {
+                    if (next < 0)
+                        next = idx;
+                    else
+                        push(idx, kTagNode, 0);
+                } else if (in_blas) {
+                    if (leaf_count == 0) {
+                        leaf_first = idx;
+                        leaf_count = cnt;
+                    } else {
+                        push(idx, kTagLeaf, cnt);
+                    }
+                } else {
+                    push(idx, kTagInst, cnt);
+                }
+            }
+            node = next;
+            continue;
+        }
+        if (sp == 0)
+            break;
+        const int2 e = stack[--sp];
+        const int tag = (int)((unsigned)e.y >> 28);
+        const int cnt = e.y & 0x0FFFFFFF;
+        if (tag == kTagNode) {
+            node = e.x;
+        } else if (tag == kTagLeaf) {
+            leaf_first = e.x;
+            leaf_count = cnt;
+        } else if (tag == kTagInst) {
+            if (cnt > 1)
+                push(e.x + 1, kTagInst, cnt - 1);
+            inst_id = __ldg(s.tlas_order + e.x);
+            const DevInstance &inst = s.instances[inst_id];
+            const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
+            co = wt_xform_point(rows, o);
+            const float3 cd = wt_xform_vector(rows, d);
+            cinvd = safe_inv(cd);
+            wr = wt_setup(co, cd);
+            node_base = inst.node_offset;
+            tri_base = inst.tri_offset;
+            in_blas = true;
+            push(0, kTagReturn, 0);
+            node = 0;
+        } else {
+            // back to the TLAS
+            co = o;
+            cinvd = winvd;
+            node_base = s.tlas_root;
+            in_blas = false;
+            inst_id = kNoHit;
+        }
     }
     return best;
 }

@@ -454,10 +454,15 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
 
 // Closest hit for every queued extension ray; hits are binned by material
 // model into the shade queues (material-sorted shading).
-// Minimum resident blocks per SM requested for the extension kernel (caps its
-// registers); 1 leaves the register count to the compiler.
+// Minimum resident blocks of 256 threads per SM requested for the traversal
+// kernels, which caps their registers (4: 64 registers, 50% occupancy); the
+// traversal is latency bound and gains more from resident warps than it
+// loses to the few spilled registers.
 #ifndef VVPT_EXTEND_MIN_BLOCKS
-#define VVPT_EXTEND_MIN_BLOCKS 1
+#define VVPT_EXTEND_MIN_BLOCKS 4
+#endif
+#ifndef VVPT_TRACE_MIN_BLOCKS
+#define VVPT_TRACE_MIN_BLOCKS 1
 #endif
 __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
@@ -539,7 +544,7 @@ __device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams 
 // The pending emitter rays whose first candidate is transparent (or below the
 // extension ray's tmin): the full candidate walk, before shade adds this
 // iteration's contributions.
-__global__ void __launch_bounds__(256) k_walk(JobTable jt, PathState ps, Queues q)
+__global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_walk(JobTable jt, PathState ps, Queues q)
 {
     const uint32_t n = q.counters[C_WALK];
     uint32_t err = 0;
@@ -1196,7 +1201,7 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 }
 
 // Shadow rays of the events shaded this iteration.
-__global__ void __launch_bounds__(256) k_shadow(JobTable jt, PathState ps, Queues q)
+__global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable jt, PathState ps, Queues q)
 {
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
@@ -1225,7 +1230,7 @@ __global__ void __launch_bounds__(256) k_shadow(JobTable jt, PathState ps, Queue
 
 // BSDF-direction emitter rays of paths that end at this event (their next
 // extension ray is never traced, so the emitter ray cannot ride on it).
-__global__ void __launch_bounds__(256) k_emitter(JobTable jt, PathState ps, Queues q)
+__global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_emitter(JobTable jt, PathState ps, Queues q)
 {
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;

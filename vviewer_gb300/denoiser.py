@@ -1,0 +1,69 @@
+"""Learned denoiser (vvpt_denoiser_*): a U-Net over noisy radiance, albedo and
+normal, trained on the GPU by the library's own BF16 tensor-core kernels.
+Images are torch CUDA tensors [n, h, w, 4] float32 (RGBA)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+class Denoiser:
+    def __init__(self, ctx, seed: int = 1):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(ctx.lib.vvpt_denoiser_create(ctx.handle, int(seed), C.byref(h)))
+        self.handle = h
+        n = C.c_uint64()
+        ctx.check(ctx.lib.vvpt_denoiser_num_params(self.handle, C.byref(n)))
+        self.num_params = int(n.value)
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.vvpt_denoiser_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, dtype=np.float32)
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_get_params(self.handle, out.ctypes.data, self.num_params))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_set_params(self.handle, p.ctypes.data, self.num_params))
+
+    @staticmethod
+    def _batch(radiance, albedo, normal, target) -> N.DenoiseBatch:
+        n, h, w, c = radiance.shape
+        for t in (radiance, albedo, normal, target):
+            assert t.is_cuda and t.is_contiguous() and tuple(t.shape) == (n, h, w, 4)
+        return N.DenoiseBatch(radiance.data_ptr(), albedo.data_ptr(), normal.data_ptr(), target.data_ptr(), n, w, h)
+
+    def gradients(self, radiance, albedo, normal, target) -> tuple[float, np.ndarray]:
+        b = self._batch(radiance, albedo, normal, target)
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_gradients(self.handle, C.byref(b), g.ctypes.data, self.num_params,
+                                                            C.byref(loss)))
+        return float(loss.value), g
+
+    def train_step(self, radiance, albedo, normal, target, lr: float = 1e-3) -> float:
+        b = self._batch(radiance, albedo, normal, target)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_train_step(self.handle, C.byref(b), float(lr), C.byref(loss)))
+        return float(loss.value)
+
+    def apply(self, radiance, albedo, normal, out) -> None:
+        """One image: [h, w, 4] CUDA tensors in, out [h, w, 4] written."""
+        h, w, _ = radiance.shape
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_apply(self.handle, radiance.data_ptr(), albedo.data_ptr(),
+                                                        normal.data_ptr(), out.data_ptr(), w, h))
