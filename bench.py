@@ -258,6 +258,9 @@ def run_ours(args) -> None:
     paths_per_step = W * H * (info.samples // info.batch_size) * info.batch_size
 
     env_is = bool(desc.get("env_is", False))
+    tuning = None
+    if not args.no_autotune:
+        tuning = gpu.autotune(sd, info, budget_ms=4000.0, env_is=env_is)
     for _ in range(args.warmup):
         gpu.render(sd, info, outputs=dev_ptrs, env_is=env_is)
     torch.cuda.synchronize()
@@ -332,7 +335,7 @@ def run_ours(args) -> None:
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {**desc, "parallelism": f"replicas x{world}",
+            "config": {**desc, "parallelism": f"replicas x{world}", "tuning": tuning,
                        "l2": "512 MB L2 flush before every step; working set (path state + per-batch sums) > L2"},
             "e2e": e2e, "roofline": roofline, "gpu_launches": launches, "clocks": clock,
             "segments_per_step": int(stats.segments), "shadow_rays_per_step": int(stats.shadow_rays),
@@ -391,6 +394,12 @@ def run_batched(args) -> None:
             j.release()
         return lat
 
+    # queue sizes and persistent-block counts for the engine (it starts with
+    # the context's tuning at the first submit)
+    tuning = None
+    if not args.no_autotune:
+        rep = type(mix[0][1])(samples=64, depth=8, batch_size=4, width=1024, height=1024, write_files=False)
+        tuning = gpus[0].autotune(engines[0].scene.scene_data(1024, 1024), rep, budget_ms=4000.0)
     warm = scenes.job_mix(2, 4, N_SCENES)
     for _ in range(max(args.warmup, 1)):
         js = [gpus[k].submit(engines[k].scene.scene_data(64, 64),
@@ -420,7 +429,7 @@ def run_batched(args) -> None:
             "data": "synthetic (seeded procedural scenes)",
             "config": {"workload": "batched_64_jobs", "jobs": 64, "scenes": N_SCENES, "scene_triangles": tris,
                        "resolutions": "256^2 / 512^2 / 1024^2 / 1920x1080", "spp": "16 / 64 / 256",
-                       "depth": 8, "batch_size": 4, "paths_per_step": paths, "seed": 1,
+                       "depth": 8, "batch_size": 4, "paths_per_step": paths, "seed": 1, "tuning": tuning,
                        "l2": "per-job batch sums and path state far above L2"},
             "e2e": {"value": paths * args.steps / sum(e2e_t), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": sum(3 * i.width * i.height * 16 for _, i in mix)},
@@ -455,6 +464,10 @@ def run_serving(args) -> None:
     reqs = scenes.serving_requests(1, args.requests, N_SCENES)
     sds = [engines[k].scene.scene_data(i.width, i.height) for _, k, i in reqs]
     paths = sum(i.width * i.height * (i.samples // i.batch_size) * i.batch_size for _, _, i in reqs)
+    tuning = None
+    if not args.no_autotune:
+        rep = type(reqs[0][2])(samples=16, depth=8, batch_size=4, width=512, height=512, write_files=False)
+        tuning = gpus[0].autotune(engines[0].scene.scene_data(512, 512), rep, budget_ms=3000.0)
     for _ in range(max(args.warmup, 1)):
         j = gpus[0].submit(sds[0], reqs[0][2])
         j.wait()
@@ -490,7 +503,7 @@ def run_serving(args) -> None:
             "config": {"workload": "serving_512_requests", "requests": len(reqs), "mean_gap_ms": 50.0,
                        "scenes": N_SCENES, "scene_triangles": tris, "resolutions": "256^2 / 512^2",
                        "spp": "8 / 16 / 32", "depth": 8, "batch_size": 4, "paths": paths, "seed": 1,
-                       "budget_bytes": 150 * (1 << 30), "outputs": "host"},
+                       "budget_bytes": 150 * (1 << 30), "outputs": "host", "tuning": tuning},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                            "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
                            "mean": float(lat.mean())},
@@ -588,6 +601,7 @@ def main():
     ap.add_argument("--sequential", action="store_true", help="batched64: also time the jobs one by one")
     ap.add_argument("--requests", type=int, default=512, help="serving512: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (no vvpt_autotune pass)")
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)

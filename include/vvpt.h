@@ -369,6 +369,20 @@ typedef struct vvpt_tuning {
 VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *tuning);
 VVPT_API vvpt_status vvpt_get_tuning(vvpt_ctx *ctx, vvpt_tuning *out_tuning);
 
+/* Autotuner (no counterpart in the reference): times short renders of the
+ * request (its image size and depth, a few batches sized to about
+ * budget_ms / 12 each) and picks blocks per SM, path slots and iterations
+ * per CUDA graph by coordinate descent on measured paths/s. The result is
+ * stored as the context's tuning (used by vvpt_render and by a job engine
+ * started afterwards) and returned in out_tuning (may be NULL). Images do
+ * not depend on the tuning. */
+VVPT_API vvpt_status vvpt_autotune(vvpt_ctx *ctx,
+                                   vvpt_scene *scene,
+                                   const vvpt_scene_data *scene_data,
+                                   const vvpt_render_info *info,
+                                   double budget_ms,
+                                   vvpt_tuning *out_tuning);
+
 /* ---- Jobs: batched and served renders ------------------------------------
  *
  * No counterpart in the reference, whose render() is synchronous and

@@ -175,6 +175,24 @@ def test_gpu_render_meets_reference_golden(ctx, name):
     assert exact >= 0.9
 
 
+def test_autotune_picks_a_candidate_and_keeps_images(ctx):
+    e, info = scenes.cornell_box(7, 96, 64, 16, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(96, 64)
+    g = ctx.upload(fs)
+    before = g.render(sd, info)
+    try:
+        t = g.autotune(sd, info, budget_ms=400.0)
+        assert t["blocks_per_sm"] in (0, 2, 3, 4, 6, 8)
+        assert t["slots"] in (0, 1 << 19, 1 << 20, 3 << 19, 1 << 21)
+        assert t["iterations_per_graph"] in (0, 4, 8, 16)
+        after = g.render(sd, info)
+        assert (after.radiance == before.radiance).all()
+    finally:
+        ctx.set_tuning()
+        g.release()
+
+
 def test_render_is_deterministic_across_schedules(ctx):
     e, info = scenes.cornell_box(6, 64, 64, 32, 8, 4)
     fs = e.scene.build()

@@ -253,8 +253,10 @@ VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *t)
 {
     if (!ctx || !t)
         return VVPT_ERR_INVALID_ARG;
-    if (t->threads_per_block && (t->threads_per_block % 32 != 0 || t->threads_per_block > 1024))
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "threads_per_block must be a multiple of 32, at most 1024");
+    if (t->threads_per_block && (t->threads_per_block % 32 != 0 || t->threads_per_block > 256))
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "threads_per_block must be a multiple of 32, at most 256");
+    if (t->blocks_per_sm > 64 || t->iterations_per_graph > 256)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "blocks_per_sm at most 64, iterations_per_graph at most 256");
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->tuning = *t;
     return VVPT_OK;
@@ -652,6 +654,96 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "render finish");
     ctx->stats = stats;
     ctx->progress.store(1.0f);
+    return VVPT_OK;
+}
+
+VVPT_API vvpt_status vvpt_autotune(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_scene_data *sd,
+                                   const vvpt_render_info *info, double budget_ms, vvpt_tuning *out)
+{
+    if (!ctx || !scene || !sd || !info)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "null argument");
+    RenderParams hp;
+    vvpt_status st = make_render_params(ctx, scene, sd, info, hp);
+    if (st != VVPT_OK)
+        return st;
+    if (hp.total_items == 0 || hp.depth == 0)
+        return fail(ctx, VVPT_ERR_INVALID_ARG, "autotune needs a request that traces paths");
+    const size_t img = (size_t)hp.width * hp.height * sizeof(float4);
+    DevBuf outb;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        cudaSetDevice(ctx->device);
+        VV_CUDA(outb.alloc(3 * img), "cudaMalloc autotune outputs");
+    }
+    vvpt_outputs o{};
+    o.radiance = outb.as<float>();
+    o.albedo = o.radiance + img / sizeof(float);
+    o.normal = o.albedo + img / sizeof(float);
+    o.on_device = 1;
+    // probe: the request's image size and depth, few batches
+    vvpt_render_info probe = *info;
+    probe.flags &= ~(uint32_t)VVPT_RENDER_PROFILE_KERNELS;
+    probe.samples = info->batch_size;
+    const vvpt_tuning start = ctx->tuning;
+    auto trial = [&](const vvpt_tuning &t, double &paths_per_ms) -> vvpt_status {
+        {
+            std::lock_guard<std::mutex> lk(ctx->mu);
+            ctx->tuning = t;
+        }
+        vvpt_status r = vvpt_render(ctx, scene, sd, &probe, &o);
+        if (r != VVPT_OK)
+            return r;
+        paths_per_ms = (double)ctx->stats.paths / std::max(ctx->stats.device_ms, 1e-3);
+        return VVPT_OK;
+    };
+    // size the probe so that one trial takes about budget / 12
+    double ppm = 0.0;
+    vvpt_tuning best = start;
+    if ((st = trial(best, ppm)) != VVPT_OK)
+        return st;
+    const double per_trial_ms = std::max(budget_ms, 100.0) / 12.0;
+    const double want_paths = ppm * per_trial_ms;
+    const double batch_paths = (double)hp.width * hp.height * info->batch_size;
+    const uint32_t batches = (uint32_t)std::min<double>(std::max(1.0, want_paths / batch_paths), hp.batches);
+    probe.samples = info->batch_size * batches;
+    if ((st = trial(best, ppm)) != VVPT_OK) // warm-up at the probe size
+        return st;
+    double best_ppm = 0.0;
+    if ((st = trial(best, best_ppm)) != VVPT_OK)
+        return st;
+    // coordinate descent: blocks per SM, slots, iterations per graph
+    auto sweep = [&](auto apply, std::initializer_list<uint32_t> values) -> vvpt_status {
+        vvpt_tuning base = best;
+        for (uint32_t v : values) {
+            vvpt_tuning t = base;
+            apply(t, v);
+            double p = 0.0;
+            vvpt_status r = trial(t, p);
+            if (r == VVPT_ERR_OOM)
+                continue; // candidate too large for this device: skip it
+            if (r != VVPT_OK)
+                return r;
+            if (p > best_ppm * 1.01) {
+                best_ppm = p;
+                best = t;
+            }
+        }
+        return VVPT_OK;
+    };
+    if ((st = sweep([](vvpt_tuning &t, uint32_t v) { t.blocks_per_sm = v; }, {2u, 3u, 4u, 6u, 8u})) != VVPT_OK)
+        return st;
+    if ((st = sweep([](vvpt_tuning &t, uint32_t v) { t.slots = v; }, {1u << 19, 1u << 20, 3u << 19, 1u << 21})) !=
+        VVPT_OK)
+        return st;
+    if ((st = sweep([](vvpt_tuning &t, uint32_t v) { t.iterations_per_graph = v; }, {4u, 8u, 16u})) != VVPT_OK)
+        return st;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->tuning = best;
+        outb.release();
+    }
+    if (out)
+        *out = best;
     return VVPT_OK;
 }
 

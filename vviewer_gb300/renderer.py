@@ -191,6 +191,17 @@ class GpuScene:
         job.id = int(jid.value)
         return job
 
+    def autotune(self, scene_data: N.SceneData, info: RenderInfo, budget_ms: float = 3000.0,
+                 env_is: bool = False) -> dict:
+        """Picks the context's tuning for requests like `info` (vvpt_autotune)."""
+        flags = N.RENDER_ENV_IS if env_is else 0
+        ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
+        t = N.Tuning()
+        self.ctx.check(self.ctx.lib.vvpt_autotune(self.ctx.handle, self.handle, C.byref(scene_data), C.byref(ri),
+                                                  float(budget_ms), C.byref(t)))
+        return {"slots": t.slots, "blocks_per_sm": t.blocks_per_sm, "threads_per_block": t.threads_per_block,
+                "iterations_per_graph": t.iterations_per_graph}
+
     def trace_closest(self, rays: np.ndarray) -> np.ndarray:
         """rays: N x 8 float32 (origin, tmin, direction, tmax) -> structured hits."""
         rays = np.ascontiguousarray(rays, dtype=np.float32)
