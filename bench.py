@@ -589,6 +589,115 @@ def run_denoise(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _rel_rmse(img, ref) -> float:
+    """Relative RMSE of an image against a reference: ||img - ref|| / ||ref|| over
+    all pixels and the 3 radiance channels."""
+    d = img[..., :3].double() - ref[..., :3].double()
+    return float(d.pow(2).mean().sqrt() / ref[..., :3].double().pow(2).mean().sqrt())
+
+
+def run_converged(args) -> None:
+    """Converged images per hour at relative RMSE <= 1e-2 against a
+    4096-spp render, on the instanced sky scene at 960 x 540 (environment
+    importance sampled): the plain tracer (spp needed from the measured error
+    at 256 spp, error ~ spp^-1/2) against the tracer plus the learned denoiser
+    (smallest spp whose denoised image meets the target), the denoiser trained
+    first on tracer pairs of other seeds (4 spp inputs, 1024 spp targets)."""
+    import torch
+
+    from vviewer_gb300 import Context, scenes
+    from vviewer_gb300.denoiser import Denoiser
+    ctx = Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    W, H = 960, 544  # multiple of 16 for the denoiser
+    target = 1e-2
+
+    def render(g, sd, info, spp):
+        info.samples = spp
+        bufs = {k: torch.zeros((H, W, 4), device="cuda") for k in ("radiance", "albedo", "normal")}
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        g.render(sd, info, outputs={k: v.data_ptr() for k, v in bufs.items()}, env_is=True)
+        torch.cuda.synchronize()
+        return bufs, time.perf_counter() - t
+
+    # training pairs: crops of renders of other seeds
+    dn = Denoiser(ctx, seed=1)
+    crops = {k: [] for k in ("radiance", "albedo", "normal", "target")}
+    t_train = time.perf_counter()
+    for seed in range(2, 10):
+        e, info = scenes.instanced_sky_scene(seed, 512, 512, 4, 8, 4, sky_w=2048, sky_h=1024)
+        g = ctx.upload(e.scene.build())
+        sd = e.scene.scene_data(512, 512)
+        noisy, _ = render(g, sd, info, 4)
+        ref, _ = render(g, sd, info, 1024)
+        g.release()
+        for k in ("radiance", "albedo", "normal"):
+            crops[k].append(noisy[k])
+        crops["target"].append(ref["radiance"])
+    batch = {k: torch.stack(v).contiguous() for k, v in crops.items()}
+    losses = []
+    for step in range(args.train_steps):
+        idx = torch.randint(0, batch["radiance"].shape[0], (4,), device="cuda")
+        ys = torch.randint(0, 512 - 256 + 1, (1,)).item() // 16 * 16
+        xs = torch.randint(0, 512 - 256 + 1, (1,)).item() // 16 * 16
+        sub = [batch[k][idx, ys:ys + 256, xs:xs + 256].contiguous() for k in ("radiance", "albedo", "normal", "target")]
+        lr = 2e-3 if step < args.train_steps * 3 // 4 else 5e-4
+        losses.append(dn.train_step(*sub, lr=lr))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t_train
+
+    e, info = scenes.instanced_sky_scene(1, W, H, 16, 8, 4, sky_w=4096, sky_h=2048)
+    g = ctx.upload(e.scene.build())
+    sd = e.scene.scene_data(W, H)
+    ref, t_ref = render(g, sd, info, 4096)
+    # plain tracer: error at 256 spp, spp ~ (e / target)^2 more for the target
+    img256, t256 = render(g, sd, info, 256)
+    e256 = _rel_rmse(img256["radiance"], ref["radiance"])
+    paths_per_s = W * H * 256 / t256
+    spp_plain = 256 * (e256 / target) ** 2
+    t_plain = W * H * spp_plain / paths_per_s
+    # tracer + denoiser
+    den = torch.zeros((H, W, 4), device="cuda")
+    rows = []
+    best = None
+    for spp in (4, 8, 16, 32, 64, 128):
+        img, t_r = render(g, sd, info, spp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dn.apply(img["radiance"], img["albedo"], img["normal"], den)
+        torch.cuda.synchronize()
+        t_d = time.perf_counter() - t0
+        err_noisy = _rel_rmse(img["radiance"], ref["radiance"])
+        err = _rel_rmse(den, ref["radiance"])
+        rows.append({"spp": spp, "rel_rmse_noisy": err_noisy, "rel_rmse_denoised": err, "render_s": t_r,
+                     "denoise_s": t_d})
+        if err <= target and best is None:
+            best = (spp, t_r + t_d, err)
+    g.release()
+    line = {"metric": "converged images/hour", "unit": "images/h", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tracer, bf16 denoiser",
+            "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": "converged_instanced_sky_960x544", "target_rel_rmse": target,
+                       "reference": "4096 spp (GPU tracer)", "train": f"{args.train_steps} steps, 4 x 256^2 crops "
+                       "of 8 seeds (4 spp inputs, 1024 spp targets)"},
+            "plain": {"rel_rmse_at_256spp": e256, "spp_needed": spp_plain, "seconds": t_plain,
+                      "images_per_hour": 3600.0 / t_plain, "paths_per_s": paths_per_s},
+            "denoised_sweep": rows, "train_s": t_train, "final_train_loss": float(np.mean(losses[-20:])),
+            "reference_s": t_ref}
+    if best:
+        line["value"] = 3600.0 / best[1]
+        line["denoised"] = {"spp": best[0], "seconds": best[1], "rel_rmse": best[2]}
+        line["gain_vs_plain"] = t_plain / best[1]
+    else:
+        line["value"] = None
+        line["note"] = "no denoised spp in the sweep met the target"
+    dn.close()
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -596,10 +705,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["cornell_medium", "cornell", "instanced_sky", "batched64", "serving512",
-                                           "denoise"],
+                                           "denoise", "converged"],
                     default="cornell_medium")
     ap.add_argument("--sequential", action="store_true", help="batched64: also time the jobs one by one")
     ap.add_argument("--requests", type=int, default=512, help="serving512: number of requests")
+    ap.add_argument("--train-steps", type=int, default=1500, help="converged: denoiser training steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (no vvpt_autotune pass)")
     ap.add_argument("--width", type=int, default=0)
@@ -614,6 +724,8 @@ def main():
         run_serving(args)
     elif args.workload == "denoise":
         run_denoise(args)
+    elif args.workload == "converged":
+        run_converged(args)
     else:
         run_ours(args)
 

@@ -55,93 +55,156 @@ __device__ __forceinline__ void load16(const bf16 *src, bool ok, bf16 *dst)
     *reinterpret_cast<uint4 *>(dst + 8) = v1;
 }
 
-// Block: 128 threads = 4 warps; tile 64 pixels x 64 output channels; warp w
-// owns pixels [16w, 16w + 16) x all 64 channels (8 n-tiles of 8).
-__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
+// Asynchronous 16-byte global -> shared copy; src_bytes = 0 writes zeros
+// (padding, channels past cin, rows past cout).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid)
 {
-    __shared__ __align__(16) bf16 As[kTileP][kPad];
-    __shared__ __align__(16) bf16 Bs[kTileC][kPad];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long P = (long)a.n * a.h * a.wd;
-    const long p0 = (long)blockIdx.x * kTileP;
-    const int c0 = blockIdx.y * kTileC;
-    // this thread's load row and 16-channel group
-    const int lr = tid >> 1, lg = (tid & 1) * 16;
-    const long lp = p0 + lr;
-    int ln = 0, ly = 0, lx = 0;
-    if (lp < P) {
-        ln = (int)(lp / ((long)a.h * a.wd));
-        const int rem = (int)(lp - (long)ln * a.h * a.wd);
-        ly = rem / a.wd;
-        lx = rem - ly * a.wd;
-    }
-    float acc[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; j++)
-        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(smem)), "l"(gmem),
+                 "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-    for (int tap = 0; tap < 9; tap++) {
-        const int yy = ly + tap / 3 - 1, xx = lx + tap % 3 - 1;
-        const bool pix_ok = lp < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
-        const bf16 *src_row = a.in + (((long)ln * a.h + yy) * a.wd + xx) * a.cin;
-        const int wc = c0 + lr;
-        const bf16 *w_row = a.wgt + ((long)wc * 9 + tap) * a.cin;
-        for (int ci0 = 0; ci0 < a.cin; ci0 += kChunk) {
-            const int ci = ci0 + lg;
-            load16(src_row + ci, pix_ok && ci < a.cin, &As[lr][lg]);
-            load16(w_row + ci, wc < a.cout && ci < a.cin, &Bs[lr][lg]);
-            __syncthreads();
+// Forward tile: 256 threads = 8 warps; block tile 128 pixels x BN output
+// channels (BN = 64: warps 4 x 2 of 32 x 32; BN = 32: warps 8 x 1 of 16 x 32,
+// for the 32- and 16-channel layers). K runs over (tap, 32-channel chunk)
+// with a 3-stage cp.async pipeline.
+constexpr int kBM = 128, kBK = 32, kStages = 3, kLds = kBK + 8;
+
+template <int BN, int WM>
+__global__ void __launch_bounds__(256) k_conv3x3(ConvArgs a)
+{
+    constexpr int WN = 32;                // channels per warp
+    constexpr int WARPS_M = kBM / WM;     // 4 or 8
+    constexpr int MT = WM / 16, NT = WN / 8;
+    static_assert(WARPS_M * (BN / WN) == 8, "8 warps");
+    __shared__ __align__(128) bf16 sA[kStages][kBM][kLds];
+    __shared__ __align__(128) bf16 sB[kStages][BN][kLds];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wm = warp % WARPS_M, wn = warp / WARPS_M;
+    const long P = (long)a.n * a.h * a.wd;
+    const long p0 = (long)blockIdx.x * kBM;
+    const int c0 = blockIdx.y * BN;
+    const int nchunks = (a.cin + kBK - 1) / kBK;
+    const int KT = 9 * nchunks;
+    // A loads: row tid / 2, two 8-channel vectors starting at (tid % 2) * 16
+    const int ar = tid >> 1, av = (tid & 1) * 16;
+    const long ap = p0 + ar;
+    int an = 0, ay = 0, ax = 0;
+    if (ap < P) {
+        an = (int)(ap / ((long)a.h * a.wd));
+        const int rem = (int)(ap - (long)an * a.h * a.wd);
+        ay = rem / a.wd;
+        ax = rem - ay * a.wd;
+    }
+    // B loads: row tid / 4, one 8-channel vector at (tid % 4) * 8 (BN * 4 threads)
+    const int br = tid >> 2, bv = (tid & 3) * 8;
+    const int bc = c0 + br;
+
+    auto load_stage = [&](int stage, int kt) {
+        const int tap = kt / nchunks, ci0 = (kt - tap * nchunks) * kBK;
+        const int yy = ay + tap / 3 - 1, xx = ax + tap % 3 - 1;
+        const bool pix_ok = ap < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
+        const long pix = pix_ok ? (((long)an * a.h + yy) * a.wd + xx) : 0;
 #pragma unroll
-            for (int ks = 0; ks < kChunk; ks += 16) {
-                uint32_t a0, a1, a2, a3;
-                ldsm_x4(smem_addr(&As[warp * 16 + (lane & 15)][ks + (lane >> 4) * 8]), a0, a1, a2, a3);
+        for (int v = 0; v < 2; v++) {
+            const int ci = ci0 + av + 8 * v;
+            const bool ok = pix_ok && ci < a.cin;
+            cp_async16(&sA[stage][ar][av + 8 * v], ok ? (const void *)(a.in + pix * a.cin + ci) : (const void *)a.in,
+                       ok);
+        }
+        if (br < BN) {
+            const int ci = ci0 + bv;
+            const bool okb = bc < a.cout && ci < a.cin;
+            cp_async16(&sB[stage][br][bv], okb ? (const void *)(a.wgt + ((long)bc * 9 + tap) * a.cin + ci)
+                                               : (const void *)a.wgt,
+                       okb);
+        }
+    };
+
+    float acc[MT][NT][4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    uint32_t b0, b1, b2, b3;
-                    ldsm_x4(smem_addr(&Bs[16 * j + (lane & 7) + ((lane >> 4) << 3)][ks + ((lane >> 3) & 1) * 8]),
-                            b0, b1, b2, b3);
-                    mma_bf16(acc[2 * j], a0, a1, a2, a3, b0, b1);
-                    mma_bf16(acc[2 * j + 1], a0, a1, a2, a3, b2, b3);
+    for (int i = 0; i < MT; i++)
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+            acc[i][j][0] = acc[i][j][1] = acc[i][j][2] = acc[i][j][3] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < kStages - 1; s++) {
+        if (s < KT)
+            load_stage(s, s);
+        cp_async_commit();
+    }
+    for (int kt = 0; kt < KT; kt++) {
+        cp_async_wait<kStages - 2>();
+        __syncthreads();
+        // refill the stage consumed in the previous iteration
+        const int nk = kt + kStages - 1;
+        if (nk < KT)
+            load_stage(nk % kStages, nk);
+        cp_async_commit();
+        const int st = kt % kStages;
+#pragma unroll
+        for (int ks = 0; ks < kBK; ks += 16) {
+            uint32_t af[MT][4], bfr[NT / 2][4];
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++)
+                ldsm_x4(smem_addr(&sA[st][wm * WM + mt * 16 + (lane & 15)][ks + (lane >> 4) * 8]), af[mt][0],
+                        af[mt][1], af[mt][2], af[mt][3]);
+#pragma unroll
+            for (int j = 0; j < NT / 2; j++)
+                ldsm_x4(smem_addr(&sB[st][wn * WN + 16 * j + (lane & 7) + ((lane >> 4) << 3)]
+                                      [ks + ((lane >> 3) & 1) * 8]),
+                        bfr[j][0], bfr[j][1], bfr[j][2], bfr[j][3]);
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++)
+#pragma unroll
+                for (int j = 0; j < NT / 2; j++) {
+                    mma_bf16(acc[mt][2 * j], af[mt][0], af[mt][1], af[mt][2], af[mt][3], bfr[j][0], bfr[j][1]);
+                    mma_bf16(acc[mt][2 * j + 1], af[mt][0], af[mt][1], af[mt][2], af[mt][3], bfr[j][2], bfr[j][3]);
                 }
-            }
-            __syncthreads();
         }
     }
+    cp_async_wait<0>();
     // epilogue: c0,c1 at (row g, cols 2t, 2t+1), c2,c3 at row g + 8
     const int g = lane >> 2, t = lane & 3;
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
-        const long p = p0 + warp * 16 + g + half * 8;
-        if (p >= P)
-            continue;
+    for (int mt = 0; mt < MT; mt++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int col = c0 + 8 * j + 2 * t;
-            if (col >= a.cout)
+        for (int half = 0; half < 2; half++) {
+            const long p = p0 + wm * WM + mt * 16 + g + half * 8;
+            if (p >= P)
                 continue;
-            float v0 = acc[j][2 * half], v1 = acc[j][2 * half + 1];
-            if (a.bias) {
-                v0 += a.bias[col];
-                v1 += a.bias[col + 1];
+#pragma unroll
+            for (int j = 0; j < NT; j++) {
+                const int col = c0 + wn * WN + 8 * j + 2 * t;
+                if (col >= a.cout)
+                    continue;
+                float v0 = acc[mt][j][2 * half], v1 = acc[mt][j][2 * half + 1];
+                if (a.bias) {
+                    v0 += a.bias[col];
+                    v1 += a.bias[col + 1];
+                }
+                if (a.relu) {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                const long o = p * a.cout + col;
+                if (a.mask) {
+                    const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(a.mask + o);
+                    if (!(__bfloat162float(m.x) > 0.0f))
+                        v0 = 0.0f;
+                    if (!(__bfloat162float(m.y) > 0.0f))
+                        v1 = 0.0f;
+                }
+                if (a.out_f32)
+                    *reinterpret_cast<float2 *>(reinterpret_cast<float *>(a.out) + o) = make_float2(v0, v1);
+                else
+                    *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<bf16 *>(a.out) + o) =
+                        __floats2bfloat162_rn(v0, v1);
             }
-            if (a.relu) {
-                v0 = fmaxf(v0, 0.0f);
-                v1 = fmaxf(v1, 0.0f);
-            }
-            const long o = p * a.cout + col;
-            if (a.mask) {
-                const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(a.mask + o);
-                if (!(__bfloat162float(m.x) > 0.0f))
-                    v0 = 0.0f;
-                if (!(__bfloat162float(m.y) > 0.0f))
-                    v1 = 0.0f;
-            }
-            if (a.out_f32)
-                *reinterpret_cast<float2 *>(reinterpret_cast<float *>(a.out) + o) = make_float2(v0, v1);
-            else
-                *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<bf16 *>(a.out) + o) = __floats2bfloat162_rn(v0, v1);
         }
-    }
 }
 
 // Weight gradient for one tap: block tile 64 output channels x 64 input
@@ -408,8 +471,16 @@ int grid_for(long n, int block = 256)
 void conv3x3(const ConvArgs &a, cudaStream_t s)
 {
     const long P = (long)a.n * a.h * a.wd;
-    dim3 grid((unsigned)((P + kTileP - 1) / kTileP), (unsigned)((a.cout + kTileC - 1) / kTileC));
-    k_conv3x3<<<grid, 128, 0, s>>>(a);
+    // 32-wide channel tiles where they leave fewer channels of the last tile
+    // empty than 64-wide ones (16, 32, 80, 96, 160, 224 channels)
+    const int waste64 = (a.cout + 63) / 64 * 64 - a.cout, waste32 = (a.cout + 31) / 32 * 32 - a.cout;
+    if (waste32 < waste64) {
+        dim3 grid((unsigned)((P + kBM - 1) / kBM), (unsigned)((a.cout + 31) / 32));
+        k_conv3x3<32, 16><<<grid, 256, 0, s>>>(a);
+    } else {
+        dim3 grid((unsigned)((P + kBM - 1) / kBM), (unsigned)((a.cout + 63) / 64));
+        k_conv3x3<64, 32><<<grid, 256, 0, s>>>(a);
+    }
 }
 
 void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw, float *dbias,

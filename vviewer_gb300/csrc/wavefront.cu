@@ -464,6 +464,9 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
 #ifndef VVPT_TRACE_MIN_BLOCKS
 #define VVPT_TRACE_MIN_BLOCKS 4
 #endif
+#ifndef VVPT_SHADE_MIN_BLOCKS
+#define VVPT_SHADE_MIN_BLOCKS 1
+#endif
 __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_EXT0 + pp];
@@ -606,7 +609,7 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 // One shading event per queued path: the body of rayPrimary*.rchit.glsl:45-175
 // (hits) or rayPrimary.rmiss.glsl:40-106 (misses), followed by Russian
 // roulette (russian_roulette.glsl:1-11).
-__global__ void __launch_bounds__(256) k_shade(JobTable jt, PathState ps, Queues q, int pp)
+__global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
     const uint32_t n = nl + np + nm;
