@@ -504,6 +504,12 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *denoiser,
                                               const vvpt_denoise_batch *batch,
                                               float learning_rate,
                                               float *out_loss);
+/* Convolution kernels: the tcgen05 tensor-core path (default: TMEM
+ * accumulators, one-thread MMA issue from shared-memory descriptors) or the
+ * warp-level mma.sync path (BF16 m16n8k16). Both accumulate in FP32; the
+ * second serves as a cross-check of the first. */
+enum { VVPT_DENOISER_TCGEN05 = 0, VVPT_DENOISER_MMA_SYNC = 1 };
+VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *denoiser, int kind);
 /* Denoises one image: out = exp(network(log1p radiance, albedo, normal)) - 1. */
 VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *denoiser,
                                          const float *radiance,

@@ -97,3 +97,28 @@ def test_training_on_tracer_pairs_beats_the_noisy_render(ctx):
     assert np.isfinite(den).all() and (den[..., 3] == 1.0).all()
     assert e_den < 0.7 * e_noisy, (e_den, e_noisy)
     dn.close()
+
+
+def test_tcgen05_and_mma_sync_kernels_agree(ctx):
+    """The tcgen05 convolutions (TMEM accumulators, default) against the
+    warp-level mma.sync ones on the same network and inputs: partial tiles at
+    every level (2 x 64 x 48 pixels, 24 at the coarsest level)."""
+    import torch
+    rng = np.random.default_rng(6)
+    n, h, w = 2, 64, 48
+    ins = [_cuda(rng.gamma(1.0, 0.5, (n, h, w, 4))), _cuda(rng.uniform(0, 1, (n, h, w, 4))),
+           _cuda(rng.uniform(0, 1, (n, h, w, 4))), _cuda(rng.gamma(1.0, 0.5, (n, h, w, 4)))]
+    dn = Denoiser(ctx, seed=9)
+    out = {}
+    for kind in ("mma_sync", "tcgen05"):
+        dn.set_kernels(kind)
+        loss, g = dn.gradients(*ins)
+        o = torch.zeros((h, w, 4), device="cuda")
+        dn.apply(ins[0][0], ins[1][0], ins[2][0], o)
+        torch.cuda.synchronize()
+        out[kind] = (loss, g, o.cpu().numpy())
+    (l0, g0, o0), (l1, g1, o1) = out["mma_sync"], out["tcgen05"]
+    assert abs(l0 - l1) <= 1e-3 * l0
+    assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
+    assert np.allclose(o1, o0, rtol=2e-2, atol=1e-3)
+    dn.close()

@@ -101,7 +101,8 @@ struct vvpt_denoiser {
     // shape-dependent buffers
     int n = 0, h = 0, w = 0;
     bool with_grads = false;
-    DevBuf acts, gacts, out_f32, target3, dout, loss;
+    DevBuf acts, gacts, out_f32, target3, dout, loss, err;
+    bool mma_sync = false; // warp-level mma.sync convolutions instead of tcgen05
     // tensors: x[l], a[l], e[l]; u[l], b[l], d[l] (l < 4)
     // gskip[l]: gradient of e_l through the decoder's concat (gradient pool only)
     Tensor x[kLevels], a[kLevels], e[kLevels], u[kLevels - 1], b[kLevels - 1], d[kLevels - 1], gskip[kLevels - 1];
@@ -183,7 +184,7 @@ void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, b
     a.n = dn->n;
     a.h = dn->h >> level;
     a.wd = dn->w >> level;
-    vvdn::conv3x3(a, s);
+    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>());
 }
 
 // input gradient of layer li: din = conv(dout, w_t) * (mask > 0)
@@ -203,7 +204,7 @@ void conv_dgrad(vvpt_denoiser *dn, int li, const bf16 *dout, bf16 *din, const bf
     a.n = dn->n;
     a.h = dn->h >> level;
     a.wd = dn->w >> level;
-    vvdn::conv3x3(a, s);
+    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>());
 }
 
 void conv_wgrad(vvpt_denoiser *dn, int li, const bf16 *dout, const bf16 *in, int level, cudaStream_t s)
@@ -268,6 +269,20 @@ void backward(vvpt_denoiser *dn, cudaStream_t s)
     }
 }
 
+// reads and clears the tcgen05 status word (stream-synchronous)
+vvpt_status check_device_status(vvpt_denoiser *dn, cudaStream_t s)
+{
+    vvpt_ctx *ctx = dn->ctx;
+    uint32_t e = 0;
+    VV_CUDA(cudaMemcpyAsync(&e, dn->err.ptr, sizeof(e), cudaMemcpyDeviceToHost, s), "read denoiser status");
+    VV_CUDA(cudaStreamSynchronize(s), "denoiser");
+    if (e) {
+        VV_CUDA(cudaMemsetAsync(dn->err.ptr, 0, sizeof(uint32_t), s), "clear denoiser status");
+        return fail(ctx, VVPT_ERR_DEVICE, "denoiser: a tensor-core wait timed out");
+    }
+    return VVPT_OK;
+}
+
 vvpt_status check_shape(vvpt_ctx *ctx, uint32_t n, uint32_t w, uint32_t h)
 {
     if (n == 0 || w == 0 || h == 0 || w % 16 || h % 16)
@@ -301,6 +316,8 @@ vvpt_status loss_and_grads(vvpt_denoiser *dn, const vvpt_denoise_batch *bt, floa
     float l = 0.0f;
     VV_CUDA(cudaMemcpyAsync(&l, dn->loss.ptr, sizeof(float), cudaMemcpyDeviceToHost, s), "read loss");
     VV_CUDA(cudaStreamSynchronize(s), "denoiser step");
+    if ((st = check_device_status(dn, s)) != VVPT_OK)
+        return st;
     if (loss_out)
         *loss_out = l / (3.0f * (float)p0);
     return VVPT_OK;
@@ -337,10 +354,12 @@ VVPT_API vvpt_status vvpt_denoiser_create(vvpt_ctx *ctx, uint64_t seed, vvpt_den
     VV_CUDA(dn->adam_m.alloc(dn->nparams * sizeof(float)), "cudaMalloc denoiser optimiser");
     VV_CUDA(dn->adam_v.alloc(dn->nparams * sizeof(float)), "cudaMalloc denoiser optimiser");
     VV_CUDA(dn->w16.alloc(dn->nw16 * sizeof(bf16)), "cudaMalloc denoiser weights");
+    VV_CUDA(dn->err.alloc(sizeof(uint32_t)), "cudaMalloc denoiser status");
     VV_CUDA(dn->wt16.alloc(dn->nw16 * sizeof(bf16)), "cudaMalloc denoiser weights");
     cudaStream_t s = vv_stream(ctx);
     VV_CUDA(cudaMemcpyAsync(dn->params.ptr, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice, s),
             "upload parameters");
+    VV_CUDA(cudaMemsetAsync(dn->err.ptr, 0, sizeof(uint32_t), s), "clear denoiser status");
     VV_CUDA(cudaMemsetAsync(dn->adam_m.ptr, 0, dn->nparams * sizeof(float), s), "clear optimiser");
     VV_CUDA(cudaMemsetAsync(dn->adam_v.ptr, 0, dn->nparams * sizeof(float), s), "clear optimiser");
     VV_CUDA(cudaStreamSynchronize(s), "denoiser create");
@@ -422,6 +441,14 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *dn, const vvpt_deno
     return VVPT_OK;
 }
 
+VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *dn, int kind)
+{
+    if (!dn || (kind != VVPT_DENOISER_TCGEN05 && kind != VVPT_DENOISER_MMA_SYNC))
+        return VVPT_ERR_INVALID_ARG;
+    dn->mma_sync = kind == VVPT_DENOISER_MMA_SYNC;
+    return VVPT_OK;
+}
+
 VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *dn, const float *radiance, const float *albedo,
                                          const float *normal, float *out, uint32_t width, uint32_t height)
 {
@@ -439,8 +466,7 @@ VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *dn, const float *radianc
     forward(dn, radiance, albedo, normal, s);
     vvdn::unpack_output(dn->out_f32.as<float>(), kOutCh, out, (int)(width * height), s);
     VV_CUDA(cudaGetLastError(), "denoiser kernels");
-    VV_CUDA(cudaStreamSynchronize(s), "denoise");
-    return VVPT_OK;
+    return check_device_status(dn, s);
 }
 
 }  // extern "C"

@@ -466,11 +466,234 @@ int grid_for(long n, int block = 256)
     return (int)std::max<long>(1, std::min<long>((n + block - 1) / block, 152L * 16));
 }
 
+
+// ---------------------------------------------------------------------------
+// tcgen05 convolution (5th-generation tensor cores, accumulator in TMEM).
+//
+// CTA = 128 threads, tile = 128 pixels (UMMA M = 128: pixel i of the tile is
+// TMEM lane i) x all output channels (N = cout <= 256, one accumulator of N
+// f32 columns). K runs over (tap, 32-channel chunk); each chunk is two
+// m128 nN k16 BF16 MMAs issued by one thread from shared-memory operands in
+// the canonical K-major no-swizzle layout (8-row x 16-byte core matrices:
+// LBO = 128 B between the core matrices along K, SBO = 512 B between 8-row
+// groups). Operands are gathered by all threads with cp.async (zero fill for
+// padding) into two stages; tcgen05.commit arrives on the stage's mbarrier
+// when the MMAs that read it are done, which gates its refill. Waits are
+// bounded by the global timer; on a timeout the kernel records an error,
+// stops issuing and still frees its TMEM.
+constexpr int kTcM = 128, kTcBK = 32, kTcStages = 2;
+constexpr int kTcABytes = kTcM * kTcBK * 2;           // 8 KB
+constexpr int kTcBBytesMax = 256 * kTcBK * 2;         // 16 KB
+constexpr int kTcStageBytes = kTcABytes + kTcBBytesMax;
+constexpr int kTcSmem = kTcStages * kTcStageBytes;    // 48 KB
+constexpr unsigned long long kTcWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    const unsigned long long t0 = globaltimer();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+        if (globaltimer() - t0 > kTcWaitNs)
+            return false;
+    }
+}
+
+// shared-memory matrix descriptor: start, LBO, SBO (16-byte units),
+// version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint32_t *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint32_t tmem_holder;
+    __shared__ __align__(8) uint64_t mbar[kTcStages];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long P = (long)a.n * a.h * a.wd;
+    const long p0 = (long)blockIdx.x * kTcM;
+    const int N = (a.cout + 15) & ~15;
+    const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
+    const int KT = 9 * nchunks;
+
+    if (tid == 0) {
+        for (int st = 0; st < kTcStages; st++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[st])));
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_holder)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_holder;
+
+    // this thread's pixel (A row = tid)
+    const long ap = p0 + tid;
+    int an = 0, ay = 0, ax = 0;
+    if (ap < P) {
+        an = (int)(ap / ((long)a.h * a.wd));
+        const int rem = (int)(ap - (long)an * a.h * a.wd);
+        ay = rem / a.wd;
+        ax = rem - ay * a.wd;
+    }
+    // instruction descriptor: D f32, A/B bf16, both K-major, N >> 3, M >> 4
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+    const uint32_t sbase = smem_addr(smem);
+
+    for (int kt = 0; kt < KT; kt++) {
+        const int st = kt & 1;
+        if (kt >= kTcStages) {
+            if (!mbar_wait(smem_addr(&mbar[st]), ((kt - kTcStages) >> 1) & 1))
+                atomicOr(&abort_flag, 1);
+        }
+        __syncthreads();
+        if (abort_flag)
+            break;
+        uint8_t *sA = smem + st * kTcStageBytes;
+        uint8_t *sB = sA + kTcABytes;
+        const int tap = kt / nchunks, ci0 = (kt - tap * nchunks) * kTcBK;
+        const int yy = ay + tap / 3 - 1, xx = ax + tap % 3 - 1;
+        const bool pix_ok = ap < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
+        const long pix = pix_ok ? (((long)an * a.h + yy) * a.wd + xx) : 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int ci = ci0 + 8 * c;
+            const bool ok = pix_ok && ci < a.cin;
+            cp_async16(sA + (tid >> 3) * 512 + c * 128 + (tid & 7) * 16,
+                       ok ? (const void *)(a.in + pix * a.cin + ci) : (const void *)a.in, ok);
+        }
+        for (int n = tid; n < N; n += 128) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int ci = ci0 + 8 * c;
+                const bool ok = n < a.cout && ci < a.cin;
+                cp_async16(sB + (n >> 3) * 512 + c * 128 + (n & 7) * 16,
+                           ok ? (const void *)(a.wgt + ((long)n * 9 + tap) * a.cin + ci) : (const void *)a.wgt, ok);
+            }
+        }
+        cp_async_commit();
+        cp_async_wait<0>();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a_addr = sbase + st * kTcStageBytes, b_addr = a_addr + kTcABytes;
+#pragma unroll
+            for (int j = 0; j < kTcBK / 16; j++) {
+                const uint64_t ad = umma_desc(a_addr + j * 256, 128, 512);
+                const uint64_t bd = umma_desc(b_addr + j * 256, 128, 512);
+                const uint32_t accumulate = (kt > 0 || j > 0) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                             "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&mbar[st])));
+        }
+    }
+    // the last commit covers every MMA this CTA issued
+    if (!abort_flag && KT > 0) {
+        const int last = KT - 1;
+        if (!mbar_wait(smem_addr(&mbar[last & 1]), (last >> 1) & 1))
+            atomicOr(&abort_flag, 1);
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!abort_flag) {
+        const long p = p0 + warp * 32 + lane;
+        for (int c = 0; c < N; c += 16) {
+            uint32_t r[16];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                         "%12, %13, %14, %15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15])
+                         : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (p >= P || c >= a.cout)
+                continue;
+            float v[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                v[k] = __uint_as_float(r[k]);
+                if (a.bias)
+                    v[k] += a.bias[c + k];
+                if (a.relu)
+                    v[k] = fmaxf(v[k], 0.0f);
+            }
+            const long o = p * a.cout + c;
+            if (a.mask) {
+                __align__(16) bf16 m[16];
+                *reinterpret_cast<uint4 *>(&m[0]) = *reinterpret_cast<const uint4 *>(a.mask + o);
+                *reinterpret_cast<uint4 *>(&m[8]) = *reinterpret_cast<const uint4 *>(a.mask + o + 8);
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    if (!(__bfloat162float(m[k]) > 0.0f))
+                        v[k] = 0.0f;
+            }
+            if (a.out_f32) {
+                float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + o);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            } else {
+                __align__(16) __nv_bfloat162 h[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    h[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+                uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(a.out) + o);
+                dst[0] = *reinterpret_cast<const uint4 *>(&h[0]);
+                dst[1] = *reinterpret_cast<const uint4 *>(&h[4]);
+            }
+        }
+    } else if (tid == 0) {
+        atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
 }  // namespace
 
-void conv3x3(const ConvArgs &a, cudaStream_t s)
+void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
 {
     const long P = (long)a.n * a.h * a.wd;
+    if (err && a.cout <= 256) {
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+            attr_set = true;
+        }
+        const int N = (a.cout + 15) & ~15;
+        int ncols = 32;
+        while (ncols < N)
+            ncols <<= 1;
+        k_conv3x3_tc<<<(unsigned)((P + kTcM - 1) / kTcM), 128, kTcSmem, s>>>(a, ncols, err);
+        return;
+    }
     // 32-wide channel tiles where they leave fewer channels of the last tile
     // empty than 64-wide ones (16, 32, 80, 96, 160, 224 channels)
     const int waste64 = (a.cout + 63) / 64 * 64 - a.cout, waste32 = (a.cout + 31) / 32 * 32 - a.cout;

@@ -28,7 +28,10 @@ struct ConvArgs {
 
 // out = act(conv3x3(in, w) + bias) (zero padding); with transformed weights
 // (w_t[ci][8 - tap][co]) and a mask the same kernel is the input gradient.
-void conv3x3(const ConvArgs &a, cudaStream_t s);
+// With `err` set (and cout <= 256) it runs on the tcgen05 tensor cores and
+// `err` receives a status bit if one of its waits timed out; with err null
+// it runs the warp-level mma.sync kernel.
+void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err);
 
 // dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
 // dbias[co] += sum_p dout[p][co] (dbias may be null).

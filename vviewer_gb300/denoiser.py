@@ -31,6 +31,10 @@ class Denoiser:
         except Exception:
             pass
 
+    def set_kernels(self, kind: str) -> None:
+        """'tcgen05' (default) or 'mma_sync' convolution kernels."""
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_set_kernels(self.handle, {"tcgen05": 0, "mma_sync": 1}[kind]))
+
     def params(self) -> np.ndarray:
         out = np.zeros(self.num_params, dtype=np.float32)
         self.ctx.check(self.ctx.lib.vvpt_denoiser_get_params(self.handle, out.ctypes.data, self.num_params))
