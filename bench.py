@@ -225,6 +225,20 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def replica_throughput(local_ms: float, units_per_rank: float, world: int, device=None) -> tuple[float, float]:
+    """Whole-job throughput of N independent replicas: the slowest rank's time
+    (max over ranks) and world * units / that time. Collective over the
+    default process group when world > 1 (NCCL on GPUs, gloo in the tests)."""
+    total_ms = local_ms
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * units_per_rank / (total_ms / 1e3)
+
+
 def run_ours(args) -> None:
     import torch
     import torch.distributed as dist
@@ -284,12 +298,7 @@ def run_ours(args) -> None:
             step_ms.append(e0.elapsed_time(e1))
             launches += int(ctx.stats().kernel_launches)
     clock = clocks.summary()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * paths_per_step * args.steps / (total_ms / 1e3)
+    total_ms, value = replica_throughput(sum(step_ms), paths_per_step * args.steps, world, "cuda")
     stats = ctx.stats()
 
     # e2e: host (pinned) output buffers, SceneData/RenderInfo from the host every step
@@ -306,11 +315,8 @@ def run_ours(args) -> None:
         dt = time.perf_counter() - t
         if i >= args.warmup:
             e2e_s.append(dt)
-    e2e_total = sum(e2e_s)
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_ms, _ = replica_throughput(1e3 * sum(e2e_s), paths_per_step * args.steps, world, "cuda")
+    e2e_total = e2e_ms / 1e3
     import ctypes as C
 
     from vviewer_gb300 import _native as N
