@@ -25,6 +25,7 @@ from vviewer_gb300.renderer import RenderInfo
 from vviewer_gb300.scene import EnvironmentType, Engine, MaterialLambert, Transform
 
 pytestmark = pytest.mark.gpu
+N_BVH_AUTO, N_BVH_HOST = 0, 1
 
 
 def assert_hits_equal(hg, ho):
@@ -284,3 +285,21 @@ def test_progress_reaches_one(ctx):
     ctx.lib.vvpt_progress(ctx.handle, C.byref(p))
     assert p.value == 1.0
     g.release()
+
+
+def test_gpu_bvh_builder_gives_the_same_hits(ctx):
+    """Meshes of 65,536 triangles or more are built on the GPU by default;
+    the host builder (VVPT_BVH_BUILDER_HOST) must give identical closest hits
+    (both are exact), and both must match the oracle."""
+    e, _ = scenes.cornell_medium(4, 64, 64, 4, 8, 4, freq=60, spheres=2)  # 2 x 72,000 triangles
+    fs = e.scene.build()
+    rays = np.concatenate([make_rays(fs, 100_000, 17, -0.2, 1.2), make_near_rays(fs, 20_000, 18)])
+    hits = {}
+    for builder in (N_BVH_AUTO, N_BVH_HOST):
+        ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, builder))
+        g = ctx.upload(fs)
+        hits[builder] = g.trace_closest(rays)
+        g.release()
+    ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, N_BVH_AUTO))
+    assert_hits_equal(hits[N_BVH_AUTO], hits[N_BVH_HOST])
+    assert_hits_equal(hits[N_BVH_AUTO], oracle.trace_closest(fs, rays))

@@ -175,6 +175,7 @@ _SIGNATURES = {
     "vvpt_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
     "vvpt_job_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "vvpt_set_budget": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vvpt_set_bvh_builder": (C.c_int, [C.c_void_p, C.c_int]),
     "vvpt_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SceneData), C.POINTER(RenderInfo), C.c_double,
                                 C.POINTER(Tuning)]),
     "vvpt_engine_stats_get": (C.c_int, [C.c_void_p, C.POINTER(EngineStats)]),

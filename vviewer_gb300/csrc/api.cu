@@ -14,6 +14,7 @@
 
 #include "../../include/vvpt.h"
 #include "internal.h"
+#include "bvh_build.h"
 #include "scene_pack.h"
 #include "scene_gpu.h"
 #include "traverse.cuh"
@@ -262,6 +263,15 @@ VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *t)
     return VVPT_OK;
 }
 
+VVPT_API vvpt_status vvpt_set_bvh_builder(vvpt_ctx *ctx, int builder)
+{
+    if (!ctx || (builder != VVPT_BVH_BUILDER_AUTO && builder != VVPT_BVH_BUILDER_HOST))
+        return VVPT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->bvh_builder = builder;
+    return VVPT_OK;
+}
+
 VVPT_API vvpt_status vvpt_get_tuning(vvpt_ctx *ctx, vvpt_tuning *t)
 {
     if (!ctx || !t)
@@ -280,7 +290,13 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
 
     PackedScene pk;
     std::string err;
-    vvpt_status st = pack_scene(desc, pk, err);
+    BlasBuilder gpu_builder;
+    if (ctx->bvh_builder == VVPT_BVH_BUILDER_AUTO) {
+        cudaStream_t bs = vv_stream(ctx);
+        gpu_builder = [bs](const std::vector<Box3> &boxes, const BVHBuildOptions &opt, BVHBuildResult &res,
+                           std::string &e) { return build_bvh2_gpu(boxes, opt, bs, res, e); };
+    }
+    vvpt_status st = pack_scene(desc, pk, err, 0, gpu_builder);
     if (st != VVPT_OK)
         return fail(ctx, st, err);
     auto scene = new vvpt_scene();

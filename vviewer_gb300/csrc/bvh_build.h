@@ -6,7 +6,11 @@
 // built with VK_BUILD_ACCELERATION_STRUCTURE_PREFER_FAST_TRACE_BIT_KHR).
 #pragma once
 #include <stdint.h>
+
+#include <string>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "scene_gpu.h"
 
@@ -35,5 +39,12 @@ struct BVHBuildResult {
 // Builds a BVH over `boxes`. Always emits at least a root node (an empty
 // input gives a root with two empty children).
 BVHBuildResult build_bvh2(const std::vector<Box3> &boxes, const BVHBuildOptions &opt = BVHBuildOptions());
+
+// The same BVH built on the GPU (bvh_gpu.cu), one tree level per round of
+// kernels on `stream`; node and order arrays come back to the host. Returns
+// false (err set, or err empty for trees the host builds trivially: at most
+// max_leaf primitives) when it did not build.
+bool build_bvh2_gpu(const std::vector<Box3> &boxes, const BVHBuildOptions &opt, cudaStream_t stream,
+                    BVHBuildResult &out, std::string &err);
 
 }  // namespace vvpt

@@ -10,10 +10,7 @@ namespace vvdn {
 
 namespace {
 
-constexpr int kTileP = 64;  // pixels per block
-constexpr int kTileC = 64;  // output channels per block
-constexpr int kChunk = 32;  // input channels per K step
-constexpr int kPad = 40;    // shared row stride in bf16 (80 B: ldmatrix rows hit distinct banks)
+constexpr int kTileC = 64;  // channels per weight-gradient block tile
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
@@ -481,12 +478,12 @@ int grid_for(long n, int block = 256)
 // when the MMAs that read it are done, which gates its refill. Waits are
 // bounded by the global timer; on a timeout the kernel records an error,
 // stops issuing and still frees its TMEM.
-constexpr int kTcM = 128, kTcBK = 32, kTcStages = 2;
-constexpr int kTcABytes = kTcM * kTcBK * 2;           // 8 KB
-constexpr int kTcBBytesMax = 256 * kTcBK * 2;         // 16 KB
-constexpr int kTcStageBytes = kTcABytes + kTcBBytesMax;
-constexpr int kTcSmem = kTcStages * kTcStageBytes;    // 48 KB
+constexpr int kTcM = 128, kTcBK = 64, kTcStages = 4;
+constexpr int kTcABytes = kTcM * kTcBK * 2; // 16 KB
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
+
+// dynamic shared memory of one CTA for N output channels
+__host__ __device__ constexpr int tc_stage_bytes(int N) { return kTcABytes + N * kTcBK * 2; }
 
 __device__ __forceinline__ unsigned long long globaltimer()
 {
@@ -530,8 +527,11 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
     const long P = (long)a.n * a.h * a.wd;
     const long p0 = (long)blockIdx.x * kTcM;
     const int N = (a.cout + 15) & ~15;
+    const int stage_bytes = tc_stage_bytes(N);
     const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
     const int KT = 9 * nchunks;
+    // core-matrix strides: K-adjacent 128 B, 8-row groups (kTcBK / 8) * 128 B
+    constexpr uint32_t kLbo = 128, kSbo = (kTcBK / 8) * 128;
 
     if (tid == 0) {
         for (int st = 0; st < kTcStages; st++)
@@ -561,48 +561,53 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
     const uint32_t sbase = smem_addr(smem);
 
-    for (int kt = 0; kt < KT; kt++) {
-        const int st = kt & 1;
-        if (kt >= kTcStages) {
-            if (!mbar_wait(smem_addr(&mbar[st]), ((kt - kTcStages) >> 1) & 1))
-                atomicOr(&abort_flag, 1);
-        }
-        __syncthreads();
-        if (abort_flag)
-            break;
-        uint8_t *sA = smem + st * kTcStageBytes;
+    auto load_chunk = [&](int kt) {
+        uint8_t *sA = smem + (kt % kTcStages) * stage_bytes;
         uint8_t *sB = sA + kTcABytes;
         const int tap = kt / nchunks, ci0 = (kt - tap * nchunks) * kTcBK;
         const int yy = ay + tap / 3 - 1, xx = ax + tap % 3 - 1;
         const bool pix_ok = ap < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
         const long pix = pix_ok ? (((long)an * a.h + yy) * a.wd + xx) : 0;
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
+        for (int c = 0; c < kTcBK / 8; c++) {
             const int ci = ci0 + 8 * c;
             const bool ok = pix_ok && ci < a.cin;
-            cp_async16(sA + (tid >> 3) * 512 + c * 128 + (tid & 7) * 16,
+            cp_async16(sA + (tid >> 3) * kSbo + c * kLbo + (tid & 7) * 16,
                        ok ? (const void *)(a.in + pix * a.cin + ci) : (const void *)a.in, ok);
         }
         for (int n = tid; n < N; n += 128) {
+            const bf16 *wrow = a.wgt + ((long)n * 9 + tap) * a.cin;
 #pragma unroll
-            for (int c = 0; c < 4; c++) {
+            for (int c = 0; c < kTcBK / 8; c++) {
                 const int ci = ci0 + 8 * c;
                 const bool ok = n < a.cout && ci < a.cin;
-                cp_async16(sB + (n >> 3) * 512 + c * 128 + (n & 7) * 16,
-                           ok ? (const void *)(a.wgt + ((long)n * 9 + tap) * a.cin + ci) : (const void *)a.wgt, ok);
+                cp_async16(sB + (n >> 3) * kSbo + c * kLbo + (n & 7) * 16, ok ? (const void *)(wrow + ci) : (const void *)a.wgt,
+                           ok);
             }
         }
+    };
+
+    // prologue: chunks 0 .. S-2 in flight
+#pragma unroll
+    for (int c = 0; c < kTcStages - 1; c++) {
+        if (c < KT)
+            load_chunk(c);
         cp_async_commit();
-        cp_async_wait<0>();
+    }
+    for (int kt = 0; kt < KT; kt++) {
+        cp_async_wait<kTcStages - 2>(); // this thread's copies of chunk kt landed
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        if (abort_flag)
+            break;
+        const int st = kt % kTcStages;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a_addr = sbase + st * kTcStageBytes, b_addr = a_addr + kTcABytes;
+            const uint32_t a_addr = sbase + st * stage_bytes, b_addr = a_addr + kTcABytes;
 #pragma unroll
             for (int j = 0; j < kTcBK / 16; j++) {
-                const uint64_t ad = umma_desc(a_addr + j * 256, 128, 512);
-                const uint64_t bd = umma_desc(b_addr + j * 256, 128, 512);
+                const uint64_t ad = umma_desc(a_addr + j * 2 * kLbo, kLbo, kSbo);
+                const uint64_t bd = umma_desc(b_addr + j * 2 * kLbo, kLbo, kSbo);
                 const uint32_t accumulate = (kt > 0 || j > 0) ? 1u : 0u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
@@ -611,11 +616,24 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 smem_addr(&mbar[st])));
         }
+        // refill the stage of chunk kt - 1 with chunk kt + S - 1 once the MMAs
+        // that read it are done (chunk kt's MMAs keep the tensor core busy)
+        const int nk = kt + kTcStages - 1;
+        if (nk < KT) {
+            if (kt >= 1) {
+                const int prev = kt - 1;
+                if (!mbar_wait(smem_addr(&mbar[prev % kTcStages]), (prev / kTcStages) & 1))
+                    atomicOr(&abort_flag, 1);
+            }
+            load_chunk(nk);
+        }
+        cp_async_commit();
     }
+    cp_async_wait<0>();
     // the last commit covers every MMA this CTA issued
     if (!abort_flag && KT > 0) {
         const int last = KT - 1;
-        if (!mbar_wait(smem_addr(&mbar[last & 1]), (last >> 1) & 1))
+        if (!mbar_wait(smem_addr(&mbar[last % kTcStages]), (last / kTcStages) & 1))
             atomicOr(&abort_flag, 1);
     }
     __syncthreads();
@@ -684,14 +702,15 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
     if (err && a.cout <= 256) {
         static bool attr_set = false;
         if (!attr_set) {
-            cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+            cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kTcStages * tc_stage_bytes(256));
             attr_set = true;
         }
         const int N = (a.cout + 15) & ~15;
         int ncols = 32;
         while (ncols < N)
             ncols <<= 1;
-        k_conv3x3_tc<<<(unsigned)((P + kTcM - 1) / kTcM), 128, kTcSmem, s>>>(a, ncols, err);
+        k_conv3x3_tc<<<(unsigned)((P + kTcM - 1) / kTcM), 128, kTcStages * tc_stage_bytes(N), s>>>(a, ncols, err);
         return;
     }
     // 32-wide channel tiles where they leave fewer channels of the last tile

@@ -87,6 +87,7 @@ struct vvpt_ctx {
     std::mutex engine_mu;
     vvpt::Engine *engine = nullptr;
     uint64_t budget_bytes = 0; // 0: no limit beyond the device's memory
+    int bvh_builder = 0;       // VVPT_BVH_BUILDER_*
     std::chrono::steady_clock::time_point created = std::chrono::steady_clock::now();
 };
 

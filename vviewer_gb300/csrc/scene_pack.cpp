@@ -11,6 +11,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <thread>
 
 #include "bvh_build.h"
@@ -125,7 +126,8 @@ float build_env_distribution(const float *rgba, uint32_t w, uint32_t h, std::vec
     return (float)(total / (double)H);
 }
 
-vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads)
+vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads,
+                       const BlasBuilder &large_builder, uint32_t large_min)
 {
     out = PackedScene();
     // ---- validation (indices the shaders would dereference)
@@ -204,6 +206,8 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
     std::sort(order.begin(), order.end(),
               [&](uint32_t a, uint32_t b) { return desc->meshes[a].num_triangles > desc->meshes[b].num_triangles; });
     std::atomic<uint32_t> next{0};
+    std::mutex large_mu;
+    std::string large_err; // a failed large build falls back to the host builder
     const unsigned hw = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
     auto worker = [&]() {
         for (;;) {
@@ -229,7 +233,16 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
             }
             BVHBuildOptions opt;
             opt.threads = (k == 0 && md.num_triangles > 100000) ? (int)hw : 1;
-            builds[m].bvh = build_bvh2(boxes, opt);
+            bool built = false;
+            if (large_builder && md.num_triangles >= large_min) {
+                std::lock_guard<std::mutex> lk(large_mu);
+                std::string e;
+                built = large_builder(boxes, opt, builds[m].bvh, e);
+                if (!built && !e.empty() && large_err.empty())
+                    large_err = e;
+            }
+            if (!built)
+                builds[m].bvh = build_bvh2(boxes, opt);
             Box3 r;
             for (int a = 0; a < 3; a++) {
                 r.lo[a] = INFINITY;
@@ -251,6 +264,9 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
         for (auto &t : th)
             t.join();
     }
+
+    if (!large_err.empty())
+        return fail(err, VVPT_ERR_DEVICE, large_err);
 
     std::vector<MeshInfo> minfo(nm);
     std::vector<BVHNode> &nodes = out.nodes;

@@ -6,6 +6,7 @@
 #pragma once
 #include <stdint.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -38,9 +39,19 @@ struct PackedScene {
     int max_blas_depth = 0;
 };
 
+// Builder for large BLAS (e.g. the GPU builder): fills `out` and returns true,
+// or returns false to leave the mesh to the host builder (err set on failure).
+struct Box3;
+struct BVHBuildOptions;
+struct BVHBuildResult;
+using BlasBuilder = std::function<bool(const std::vector<Box3> &, const BVHBuildOptions &, BVHBuildResult &,
+                                       std::string &)>;
+
 // Returns VVPT_OK or an error status with `err` set. `threads` = 0 uses every
-// hardware thread for the BLAS builds.
-vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads = 0);
+// hardware thread for the BLAS builds. Meshes of at least `large_min`
+// triangles go to `large_builder` when one is given (one at a time).
+vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads = 0,
+                       const BlasBuilder &large_builder = BlasBuilder(), uint32_t large_min = 65536);
 
 // Piecewise-constant sampling tables of an RGBA32F equirect environment
 // (PackedScene::env_dist layout): function = luminance dilated over the 3x3
