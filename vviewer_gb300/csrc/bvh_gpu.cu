@@ -12,7 +12,9 @@
 //                all centroids coincide
 //   k_partition  every primitive moves to its side (per-task cursors)
 //   k_emit       the task's node is written (both children's boxes and links);
-//                children above the leaf size become next-level tasks
+//                children above the leaf size become next-level tasks, smaller
+//                ones are finished by the same thread (split while the SAH
+//                says so, as the host builder does)
 // The host only reads the task count per level. Positions inside a leaf keep
 // the order the partition left them in, so the build is not deterministic
 // across runs; traversal results do not depend on it (exact closest hit under
@@ -305,11 +307,117 @@ __global__ void k_clear_median(GBox *m, int n)
     }
 }
 
+// A child of at most max_leaf primitives is finished by its parent's thread
+// with the same rule as the host builder: split while the SAH says a split
+// is cheaper than the leaf (traversal cost 1, intersection cost 1 per
+// primitive); with so few primitives the candidate planes are the gaps
+// between the sorted centroids. Returns the parent's link and count.
+__device__ void small_subtree(int b, int n, int depth, int *idx, const GBox *boxes, const float4 *cent,
+                              BVHNode *nodes, int *counters, int &link, int &count, GBox &box)
+{
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = 0; i < n; i++) {
+        const GBox g = boxes[idx[b + i]];
+        for (int j = 0; j < 3; j++) {
+            lo[j] = fminf(lo[j], g.lo[j]);
+            hi[j] = fmaxf(hi[j], g.hi[j]);
+        }
+    }
+    for (int j = 0; j < 3; j++) {
+        box.lo[j] = lo[j];
+        box.hi[j] = hi[j];
+    }
+    link = b;
+    count = n;
+    if (n <= 1)
+        return;
+    const double parent_area = (double)half_area(lo, hi);
+    double best = 1e300;
+    int best_axis = -1, best_k = 0;
+    int order[8];
+    for (int a = 0; a < 3; a++) {
+        // sort this range's positions by centroid on axis a (n <= 8)
+        for (int i = 0; i < n; i++)
+            order[i] = idx[b + i];
+        for (int i = 1; i < n; i++) {
+            const int x = order[i];
+            const float4 cx = cent[x];
+            const float vx = a == 0 ? cx.x : (a == 1 ? cx.y : cx.z);
+            int j = i - 1;
+            while (j >= 0) {
+                const float4 cj = cent[order[j]];
+                const float vj = a == 0 ? cj.x : (a == 1 ? cj.y : cj.z);
+                if (vj <= vx)
+                    break;
+                order[j + 1] = order[j];
+                j--;
+            }
+            order[j + 1] = x;
+        }
+        for (int k = 1; k < n; k++) {
+            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            for (int i = 0; i < n; i++) {
+                const GBox g = boxes[order[i]];
+                float *l = i < k ? llo : rlo, *h = i < k ? lhi : rhi;
+                for (int j = 0; j < 3; j++) {
+                    l[j] = fminf(l[j], g.lo[j]);
+                    h[j] = fmaxf(h[j], g.hi[j]);
+                }
+            }
+            const double cost = (double)half_area(llo, lhi) * k + (double)half_area(rlo, rhi) * (n - k);
+            if (cost < best) {
+                best = cost;
+                best_axis = a;
+                best_k = k;
+            }
+        }
+    }
+    const double split_cost = 1.0 + (parent_area > 0.0 ? best / parent_area : (double)n);
+    if (best_axis < 0 || (double)n <= split_cost)
+        return; // leaf
+    // reorder the range by the best axis and build both sides
+    for (int i = 0; i < n; i++)
+        order[i] = idx[b + i];
+    for (int i = 1; i < n; i++) {
+        const int x = order[i];
+        const float4 cx = cent[x];
+        const float vx = best_axis == 0 ? cx.x : (best_axis == 1 ? cx.y : cx.z);
+        int j = i - 1;
+        while (j >= 0) {
+            const float4 cj = cent[order[j]];
+            const float vj = best_axis == 0 ? cj.x : (best_axis == 1 ? cj.y : cj.z);
+            if (vj <= vx)
+                break;
+            order[j + 1] = order[j];
+            j--;
+        }
+        order[j + 1] = x;
+    }
+    for (int i = 0; i < n; i++)
+        idx[b + i] = order[i];
+    const int node = atomicAdd(&counters[0], 1);
+    int ll, lc, rl, rc;
+    GBox lb, rb;
+    small_subtree(b, best_k, depth + 1, idx, boxes, cent, nodes, counters, ll, lc, lb);
+    small_subtree(b + best_k, n - best_k, depth + 1, idx, boxes, cent, nodes, counters, rl, rc, rb);
+    atomicMax(&counters[2], depth + 1);
+    BVHNode nd;
+    nd.lxy = make_float4(lb.lo[0], lb.hi[0], lb.lo[1], lb.hi[1]);
+    nd.rxy = make_float4(rb.lo[0], rb.hi[0], rb.lo[1], rb.hi[1]);
+    nd.lrz = make_float4(lb.lo[2], lb.hi[2], rb.lo[2], rb.hi[2]);
+    nd.c = make_int4(ll, rl, lc, rc);
+    nodes[node] = nd;
+    link = node;
+    count = 0;
+}
+
 // One thread per task: the node record, child tasks for children above the
-// leaf size; child task ids go to child_task[2t + side].
+// leaf size (small children finished here); child task ids go to
+// child_task[2t + side].
 __global__ void k_emit(const Task *tasks, int ntasks, Split *splits, const GBox *median_boxes, BVHNode *nodes,
                        int *counters /* [0] nodes, [1] next tasks, [2] max depth */, Task *next, int *child_task,
-                       int max_leaf, int max_depth)
+                       int max_leaf, int max_depth, int *idx, const GBox *boxes, const float4 *cent)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks)
@@ -336,10 +444,13 @@ __global__ void k_emit(const Task *tasks, int ntasks, Split *splits, const GBox 
         const int b = side == 0 ? T.begin : T.begin + S.nl;
         const int e = side == 0 ? T.begin + S.nl : T.end;
         const int n = e - b;
-        if (n <= max_leaf || T.depth + 1 >= max_depth) {
+        child_task[2 * t + side] = -1;
+        if (T.depth + 1 >= max_depth) {
             link[side] = b;
             cnt[side] = n;
-            child_task[2 * t + side] = -1;
+        } else if (n <= max_leaf && n <= 8) {
+            GBox bx;
+            small_subtree(b, n, T.depth + 1, idx, boxes, cent, nodes, counters, link[side], cnt[side], bx);
         } else {
             const int node = atomicAdd(&counters[0], 1);
             const int nt = atomicAdd(&counters[1], 1);
@@ -408,7 +519,7 @@ bool build_bvh2_gpu(const std::vector<Box3> &boxes, const BVHBuildOptions &opt, 
         }
         return true;
     };
-    const int max_nodes = std::max(1, n); // inner nodes of a binary tree over n leaves' primitives
+    const int max_nodes = std::max(1, n); // a binary tree whose leaves hold >= 1 primitive has < n inner nodes
     DevMem d_boxes, d_cent, d_idx[2], d_task_of[2], d_side, d_tasks[2], d_bins, d_splits, d_cursors, d_nodes,
         d_counters, d_child, d_median;
     if (!ck(cudaMalloc(&d_boxes.p, sizeof(GBox) * n), "alloc") || !ck(cudaMalloc(&d_cent.p, sizeof(float4) * n), "alloc") ||
@@ -504,7 +615,8 @@ bool build_bvh2_gpu(const std::vector<Box3> &boxes, const BVHBuildOptions &opt, 
         cudaMemsetAsync(d_counters.as<int>() + 1, 0, 4, s);
         k_emit<<<(ntasks + 127) / 128, 128, 0, s>>>(tasks, ntasks, d_splits.as<Split>(), d_median.as<GBox>(),
                                                     d_nodes.as<BVHNode>(), d_counters.as<int>(), next,
-                                                    d_child.as<int>(), opt.max_leaf, opt.max_depth);
+                                                    d_child.as<int>(), opt.max_leaf, opt.max_depth,
+                                                    d_idx[1].as<int>(), d_boxes.as<GBox>(), d_cent.as<float4>());
         k_retask<<<grid_of(n), 256, 0, s>>>(d_side.as<int>(), d_child.as<int>(), n, d_task_of[1].as<int>());
         std::swap(d_idx[0].p, d_idx[1].p);
         std::swap(d_task_of[0].p, d_task_of[1].p);

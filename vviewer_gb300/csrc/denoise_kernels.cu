@@ -478,12 +478,11 @@ int grid_for(long n, int block = 256)
 // when the MMAs that read it are done, which gates its refill. Waits are
 // bounded by the global timer; on a timeout the kernel records an error,
 // stops issuing and still frees its TMEM.
-constexpr int kTcM = 128, kTcBK = 64, kTcStages = 4;
-constexpr int kTcABytes = kTcM * kTcBK * 2; // 16 KB
+constexpr int kTcM = 128, kTcStages = 4;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
-// dynamic shared memory of one CTA for N output channels
-__host__ __device__ constexpr int tc_stage_bytes(int N) { return kTcABytes + N * kTcBK * 2; }
+// shared memory of one pipeline stage: A (128 pixels x BK) and B (N x BK)
+__host__ __device__ constexpr int tc_stage_bytes(int N, int BK) { return (kTcM + N) * BK * 2; }
 
 __device__ __forceinline__ unsigned long long globaltimer()
 {
@@ -517,8 +516,12 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+// BK = 32 or 64 input channels per pipeline stage (32 for layers whose
+// input channel count is not a multiple of 64, so no stage is half empty)
+template <int kTcBK>
 __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint32_t *err)
 {
+    constexpr int kTcABytes = kTcM * kTcBK * 2;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_holder;
     __shared__ __align__(8) uint64_t mbar[kTcStages];
@@ -527,7 +530,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
     const long P = (long)a.n * a.h * a.wd;
     const long p0 = (long)blockIdx.x * kTcM;
     const int N = (a.cout + 15) & ~15;
-    const int stage_bytes = tc_stage_bytes(N);
+    const int stage_bytes = tc_stage_bytes(N, kTcBK);
     const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
     const int KT = 9 * nchunks;
     // core-matrix strides: K-adjacent 128 B, 8-row groups (kTcBK / 8) * 128 B
@@ -702,15 +705,21 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
     if (err && a.cout <= 256) {
         static bool attr_set = false;
         if (!attr_set) {
-            cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kTcStages * tc_stage_bytes(256));
+            cudaFuncSetAttribute(k_conv3x3_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kTcStages * tc_stage_bytes(256, 32));
+            cudaFuncSetAttribute(k_conv3x3_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kTcStages * tc_stage_bytes(256, 64));
             attr_set = true;
         }
         const int N = (a.cout + 15) & ~15;
         int ncols = 32;
         while (ncols < N)
             ncols <<= 1;
-        k_conv3x3_tc<<<(unsigned)((P + kTcM - 1) / kTcM), 128, kTcStages * tc_stage_bytes(N), s>>>(a, ncols, err);
+        const unsigned grid = (unsigned)((P + kTcM - 1) / kTcM);
+        if (a.cin % 64 == 0)
+            k_conv3x3_tc<64><<<grid, 128, kTcStages * tc_stage_bytes(N, 64), s>>>(a, ncols, err);
+        else
+            k_conv3x3_tc<32><<<grid, 128, kTcStages * tc_stage_bytes(N, 32), s>>>(a, ncols, err);
         return;
     }
     // 32-wide channel tiles where they leave fewer channels of the last tile
