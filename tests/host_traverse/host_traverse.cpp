@@ -32,6 +32,12 @@ static inline int __all_sync(unsigned, int pred) { return pred; }
 
 using namespace vvpt;
 
+// the shared-memory TLAS cache of the device kernels: never filled here
+// (vvpt_tlas_cache_count stays 0)
+namespace vvpt {
+float4 vvpt_tlas_cache[4];
+}
+
 extern "C" int host_trace_closest(const vvpt_scene_desc *desc, const vvpt_ray *rays, uint32_t n, vvpt_hit *hits,
                                   uint32_t *err_bits, char *msg, int msg_len)
 {
@@ -51,6 +57,7 @@ extern "C" int host_trace_closest(const vvpt_scene_desc *desc, const vvpt_ray *r
     v.instances = pk.instances.data();
     v.tlas_order = pk.tlas_order.data();
     v.tlas_root = pk.tlas_root;
+    v.tlas_count = (uint32_t)(pk.nodes.size() - pk.tlas_root);
     v.num_instances = desc->num_instances;
     v.cull_o = pk.cull_o;
     v.cull_r = pk.cull_r;

@@ -336,6 +336,7 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     v.instances = scene->instances.as<DevInstance>();
     v.tlas_order = scene->tlas_order.as<uint32_t>();
     v.tlas_root = pk.tlas_root;
+    v.tlas_count = (uint32_t)(pk.nodes.size() - pk.tlas_root);
     v.num_instances = desc->num_instances;
     v.materials = scene->materials.as<DevMaterial>();
     v.num_materials = desc->num_materials;

@@ -467,22 +467,28 @@ int grid_for(long n, int block = 256)
 // ---------------------------------------------------------------------------
 // tcgen05 convolution (5th-generation tensor cores, accumulator in TMEM).
 //
-// CTA = 128 threads, tile = 128 pixels (UMMA M = 128: pixel i of the tile is
-// TMEM lane i) x all output channels (N = cout <= 256, one accumulator of N
-// f32 columns). K runs over (tap, 32-channel chunk); each chunk is two
-// m128 nN k16 BF16 MMAs issued by one thread from shared-memory operands in
-// the canonical K-major no-swizzle layout (8-row x 16-byte core matrices:
-// LBO = 128 B between the core matrices along K, SBO = 512 B between 8-row
-// groups). Operands are gathered by all threads with cp.async (zero fill for
-// padding) into two stages; tcgen05.commit arrives on the stage's mbarrier
-// when the MMAs that read it are done, which gates its refill. Waits are
-// bounded by the global timer; on a timeout the kernel records an error,
-// stops issuing and still frees its TMEM.
-constexpr int kTcM = 128, kTcStages = 4;
+// CTA = 128 threads, tile = 128 consecutive pixels of one image row (UMMA
+// M = 128: pixel i of the tile is TMEM lane i) x all output channels (N =
+// cout <= 256, one accumulator of N f32 columns). For each 32-channel chunk
+// of the input the CTA stages a halo of 3 rows x 130 pixels once in shared
+// memory; every one of the 9 taps is then an MMA over a shifted view of it
+// (the operand descriptor starts 16 bytes per pixel and one halo row further),
+// so the input is read once per chunk instead of once per tap. Layout, K-major
+// without swizzle: for each halo row and 8-channel group the 130 pixels are
+// consecutive 16-byte rows, so 8 consecutive pixels form a core matrix (SBO
+// 128 B between pixel groups, LBO 130 x 16 B between channel groups). The
+// weights of one (chunk, tap) step go to one of 4 stages. One thread issues
+// the MMAs (two m128 nN k16 per step) and commits each step to its stage's
+// mbarrier; refills wait on the mbarrier of the step two back (MMAs complete
+// in issue order). Waits are bounded by the global timer; on a timeout the
+// kernel records an error, stops issuing and still frees its TMEM.
+constexpr int kTcM = 128, kTcBK = 32, kTcKC = kTcBK / 8, kTcBStages = 4, kTcHaloPx = kTcM + 2;
+constexpr int kTcHaloRow = kTcKC * kTcHaloPx * 16;  // one halo row: 4 channel groups x 130 pixels x 16 B
+constexpr int kTcHaloBytes = 3 * kTcHaloRow;        // 24,960 B
+constexpr int kTcHaloAlloc = 25088;                 // rounded up to 1 KB multiples
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
-// shared memory of one pipeline stage: A (128 pixels x BK) and B (N x BK)
-__host__ __device__ constexpr int tc_stage_bytes(int N, int BK) { return (kTcM + N) * BK * 2; }
+__host__ __device__ constexpr int tc_smem_bytes(int N) { return 2 * kTcHaloAlloc + kTcBStages * N * kTcBK * 2; }
 
 __device__ __forceinline__ unsigned long long globaltimer()
 {
@@ -516,28 +522,28 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// BK = 32 or 64 input channels per pipeline stage (32 for layers whose
-// input channel count is not a multiple of 64, so no stage is half empty)
-template <int kTcBK>
 __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint32_t *err)
 {
-    constexpr int kTcABytes = kTcM * kTcBK * 2;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_holder;
-    __shared__ __align__(8) uint64_t mbar[kTcStages];
+    __shared__ __align__(8) uint64_t mbar[kTcBStages];
     __shared__ int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long P = (long)a.n * a.h * a.wd;
-    const long p0 = (long)blockIdx.x * kTcM;
+    const int tiles_x = (a.wd + kTcM - 1) / kTcM;
+    const int tx = blockIdx.x % tiles_x;
+    const int y = (blockIdx.x / tiles_x) % a.h;
+    const int nb = blockIdx.x / (tiles_x * a.h);
+    const int x0 = tx * kTcM;
     const int N = (a.cout + 15) & ~15;
-    const int stage_bytes = tc_stage_bytes(N, kTcBK);
+    const int bstage_bytes = N * kTcBK * 2;
     const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
-    const int KT = 9 * nchunks;
-    // core-matrix strides: K-adjacent 128 B, 8-row groups (kTcBK / 8) * 128 B
-    constexpr uint32_t kLbo = 128, kSbo = (kTcBK / 8) * 128;
+    const int S = 9 * nchunks;
+    uint8_t *halo[2] = {smem, smem + kTcHaloAlloc};
+    uint8_t *bst = smem + 2 * kTcHaloAlloc;
+    const uint32_t sbase = smem_addr(smem);
 
     if (tid == 0) {
-        for (int st = 0; st < kTcStages; st++)
+        for (int st = 0; st < kTcBStages; st++)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[st])));
         abort_flag = 0;
     }
@@ -550,99 +556,85 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_holder;
-
-    // this thread's pixel (A row = tid)
-    const long ap = p0 + tid;
-    int an = 0, ay = 0, ax = 0;
-    if (ap < P) {
-        an = (int)(ap / ((long)a.h * a.wd));
-        const int rem = (int)(ap - (long)an * a.h * a.wd);
-        ay = rem / a.wd;
-        ax = rem - ay * a.wd;
-    }
-    // instruction descriptor: D f32, A/B bf16, both K-major, N >> 3, M >> 4
+    // D f32, A/B bf16, both K-major, N >> 3, M >> 4
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
-    const uint32_t sbase = smem_addr(smem);
 
-    auto load_chunk = [&](int kt) {
-        uint8_t *sA = smem + (kt % kTcStages) * stage_bytes;
-        uint8_t *sB = sA + kTcABytes;
-        const int tap = kt / nchunks, ci0 = (kt - tap * nchunks) * kTcBK;
-        const int yy = ay + tap / 3 - 1, xx = ax + tap % 3 - 1;
-        const bool pix_ok = ap < P && yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd;
-        const long pix = pix_ok ? (((long)an * a.h + yy) * a.wd + xx) : 0;
-#pragma unroll
-        for (int c = 0; c < kTcBK / 8; c++) {
-            const int ci = ci0 + 8 * c;
-            const bool ok = pix_ok && ci < a.cin;
-            cp_async16(sA + (tid >> 3) * kSbo + c * kLbo + (tid & 7) * 16,
-                       ok ? (const void *)(a.in + pix * a.cin + ci) : (const void *)a.in, ok);
-        }
-        for (int n = tid; n < N; n += 128) {
-            const bf16 *wrow = a.wgt + ((long)n * 9 + tap) * a.cin;
-#pragma unroll
-            for (int c = 0; c < kTcBK / 8; c++) {
-                const int ci = ci0 + 8 * c;
-                const bool ok = n < a.cout && ci < a.cin;
-                cp_async16(sB + (n >> 3) * kSbo + c * kLbo + (n & 7) * 16, ok ? (const void *)(wrow + ci) : (const void *)a.wgt,
-                           ok);
+    auto load_step = [&](int st) {
+        const int c = st / 9, tap = st - c * 9, ci0 = c * kTcBK;
+        if (tap == 0) {
+            // halo of chunk c: 3 rows x 130 pixels x 4 channel groups
+            uint8_t *h = halo[c & 1];
+            for (int i = tid; i < 3 * kTcKC * kTcHaloPx; i += 128) {
+                const int px = i % kTcHaloPx, kc = (i / kTcHaloPx) % kTcKC, hr = i / (kTcHaloPx * kTcKC);
+                const int yy = y + hr - 1, xx = x0 - 1 + px, ci = ci0 + 8 * kc;
+                const bool ok = yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd && ci < a.cin;
+                const bf16 *src = ok ? a.in + (((long)nb * a.h + yy) * a.wd + xx) * a.cin + ci : a.in;
+                cp_async16(h + ((hr * kTcKC + kc) * kTcHaloPx + px) * 16, src, ok);
             }
+        }
+        uint8_t *b = bst + (st % kTcBStages) * bstage_bytes;
+        for (int i = tid; i < N * kTcKC; i += 128) {
+            const int n = i / kTcKC, kc = i - n * kTcKC, ci = ci0 + 8 * kc;
+            const bool ok = n < a.cout && ci < a.cin;
+            const bf16 *src = ok ? a.wgt + ((long)n * 9 + tap) * a.cin + ci : a.wgt;
+            cp_async16(b + (n >> 3) * (kTcKC * 128) + kc * 128 + (n & 7) * 16, src, ok);
         }
     };
 
-    // prologue: chunks 0 .. S-2 in flight
-#pragma unroll
-    for (int c = 0; c < kTcStages - 1; c++) {
-        if (c < KT)
-            load_chunk(c);
+    // prologue: steps 0 and 1
+    for (int st = 0; st < 2; st++) {
+        if (st < S)
+            load_step(st);
         cp_async_commit();
     }
-    for (int kt = 0; kt < KT; kt++) {
-        cp_async_wait<kTcStages - 2>(); // this thread's copies of chunk kt landed
+    for (int st = 0; st < S; st++) {
+        cp_async_wait<1>(); // this thread's copies of step st landed
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (abort_flag)
             break;
-        const int st = kt % kTcStages;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a_addr = sbase + st * stage_bytes, b_addr = a_addr + kTcABytes;
+            const int c = st / 9, tap = st - c * 9, dy = tap / 3, dx = tap % 3;
+            const uint32_t a_addr = sbase + (c & 1) * kTcHaloAlloc + dy * kTcHaloRow + dx * 16;
+            const uint32_t b_addr = sbase + 2 * kTcHaloAlloc + (st % kTcBStages) * bstage_bytes;
 #pragma unroll
             for (int j = 0; j < kTcBK / 16; j++) {
-                const uint64_t ad = umma_desc(a_addr + j * 2 * kLbo, kLbo, kSbo);
-                const uint64_t bd = umma_desc(b_addr + j * 2 * kLbo, kLbo, kSbo);
-                const uint32_t accumulate = (kt > 0 || j > 0) ? 1u : 0u;
+                const uint64_t ad = umma_desc(a_addr + j * 2 * kTcHaloPx * 16, kTcHaloPx * 16, 128);
+                const uint64_t bd = umma_desc(b_addr + j * 2 * 128, 128, kTcKC * 128);
+                const uint32_t accumulate = (st > 0 || j > 0) ? 1u : 0u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
                              "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_addr(&mbar[st])));
+                smem_addr(&mbar[st % kTcBStages])));
         }
-        // refill the stage of chunk kt - 1 with chunk kt + S - 1 once the MMAs
-        // that read it are done (chunk kt's MMAs keep the tensor core busy)
-        const int nk = kt + kTcStages - 1;
-        if (nk < KT) {
-            if (kt >= 1) {
-                const int prev = kt - 1;
-                if (!mbar_wait(smem_addr(&mbar[prev % kTcStages]), (prev / kTcStages) & 1))
+        // step st + 2 reuses the weight stage of step st - 2 and, at a chunk
+        // start, the halo of chunk (st + 2) / 9 - 2: both done once step st - 2
+        // is (in-order completion)
+        const int nx = st + 2;
+        if (nx < S) {
+            if (st >= 2) {
+                const int prev = st - 2;
+                if (!mbar_wait(smem_addr(&mbar[prev % kTcBStages]), (prev / kTcBStages) & 1))
                     atomicOr(&abort_flag, 1);
             }
-            load_chunk(nk);
+            load_step(nx);
         }
         cp_async_commit();
     }
     cp_async_wait<0>();
-    // the last commit covers every MMA this CTA issued
-    if (!abort_flag && KT > 0) {
-        const int last = KT - 1;
-        if (!mbar_wait(smem_addr(&mbar[last % kTcStages]), (last / kTcStages) & 1))
+    if (!abort_flag && S > 0) {
+        const int last = S - 1;
+        if (!mbar_wait(smem_addr(&mbar[last % kTcBStages]), (last / kTcBStages) & 1))
             atomicOr(&abort_flag, 1);
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!abort_flag) {
-        const long p = p0 + warp * 32 + lane;
+        const int x = x0 + warp * 32 + lane;
+        const long p = ((long)nb * a.h + y) * a.wd + x;
         for (int c = 0; c < N; c += 16) {
             uint32_t r[16];
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
@@ -652,7 +644,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
                            "=r"(r[14]), "=r"(r[15])
                          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
             asm volatile("tcgen05.wait::ld.sync.aligned;");
-            if (p >= P || c >= a.cout)
+            if (x >= a.wd || c >= a.cout)
                 continue;
             float v[16];
 #pragma unroll
@@ -679,13 +671,13 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
                 for (int k = 0; k < 4; k++)
                     dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
             } else {
-                __align__(16) __nv_bfloat162 h[8];
+                __align__(16) __nv_bfloat162 hh[8];
 #pragma unroll
                 for (int k = 0; k < 8; k++)
-                    h[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+                    hh[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
                 uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(a.out) + o);
-                dst[0] = *reinterpret_cast<const uint4 *>(&h[0]);
-                dst[1] = *reinterpret_cast<const uint4 *>(&h[4]);
+                dst[0] = *reinterpret_cast<const uint4 *>(&hh[0]);
+                dst[1] = *reinterpret_cast<const uint4 *>(&hh[4]);
             }
         }
     } else if (tid == 0) {
@@ -705,21 +697,15 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
     if (err && a.cout <= 256) {
         static bool attr_set = false;
         if (!attr_set) {
-            cudaFuncSetAttribute(k_conv3x3_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kTcStages * tc_stage_bytes(256, 32));
-            cudaFuncSetAttribute(k_conv3x3_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kTcStages * tc_stage_bytes(256, 64));
+            cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes(256));
             attr_set = true;
         }
         const int N = (a.cout + 15) & ~15;
         int ncols = 32;
         while (ncols < N)
             ncols <<= 1;
-        const unsigned grid = (unsigned)((P + kTcM - 1) / kTcM);
-        if (a.cin % 64 == 0)
-            k_conv3x3_tc<64><<<grid, 128, kTcStages * tc_stage_bytes(N, 64), s>>>(a, ncols, err);
-        else
-            k_conv3x3_tc<32><<<grid, 128, kTcStages * tc_stage_bytes(N, 32), s>>>(a, ncols, err);
+        const long tiles = (long)a.n * a.h * ((a.wd + kTcM - 1) / kTcM);
+        k_conv3x3_tc<<<(unsigned)tiles, 128, tc_smem_bytes(N), s>>>(a, ncols, err);
         return;
     }
     // 32-wide channel tiles where they leave fewer channels of the last tile

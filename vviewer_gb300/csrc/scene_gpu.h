@@ -120,6 +120,7 @@ struct SceneView {
     const DevInstance *instances;
     const uint32_t *tlas_order; // TLAS leaf order -> instance slot
     uint32_t tlas_root;        // node index of the TLAS root
+    uint32_t tlas_count;       // TLAS nodes (from tlas_root to the end of `nodes`)
     uint32_t num_instances;
     const DevMaterial *materials;
     uint32_t num_materials;

@@ -207,6 +207,54 @@ __device__ __forceinline__ float3 wt_xform_vector(const float4 *rows, const floa
     return r;
 }
 
+// Top of the TLAS staged in shared memory: a traversal kernel fills it at its
+// start with the first kTlasCacheNodes nodes of one live scene (the scene of
+// its block's first queue entry; launched with kTlasCacheBytes of dynamic
+// shared memory), and trace_after reads TLAS nodes of that scene from it.
+// Kernels that do not fill it clear it (tlas_cache_none).
+constexpr int kTlasCacheNodes = 128;
+constexpr int kTlasCacheBytes = kTlasCacheNodes * (int)sizeof(BVHNode);
+extern __shared__ __align__(16) float4 vvpt_tlas_cache[];
+__shared__ const BVHNode *vvpt_tlas_cache_src;
+__shared__ int vvpt_tlas_cache_count;
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void tlas_cache_fill(const SceneView &s)
+{
+    const BVHNode *src = s.nodes + s.tlas_root;
+    const int cnt = min((int)s.tlas_count, kTlasCacheNodes);
+    const float4 *f = reinterpret_cast<const float4 *>(src);
+    for (int i = threadIdx.x; i < 4 * cnt; i += blockDim.x)
+        vvpt_tlas_cache[i] = __ldg(f + i);
+    if (threadIdx.x == 0) {
+        vvpt_tlas_cache_src = src;
+        vvpt_tlas_cache_count = cnt;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void tlas_cache_none()
+{
+    if (threadIdx.x == 0) {
+        vvpt_tlas_cache_src = nullptr;
+        vvpt_tlas_cache_count = 0;
+    }
+    __syncthreads();
+}
+#endif
+
+__device__ __forceinline__ BVHNode load_node_cached(int idx)
+{
+    const float4 *p = vvpt_tlas_cache + 4 * idx;
+    BVHNode n;
+    n.lxy = p[0];
+    n.rxy = p[1];
+    n.lrz = p[2];
+    const float4 c = p[3];
+    n.c = make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), __float_as_int(c.w));
+    return n;
+}
+
 // Closest hit over all TLAS instances among candidates strictly after
 // `after`, as one flat loop over a single stack. Every loop step is one of:
 // a triangle test, a node visit (both children's boxes), or a stack
@@ -238,6 +286,9 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     int leaf_first = 0, leaf_count = 0; // triangles still to test (local indices)
     int2 stack[kTraversalStack];
     int sp = 0;
+    // TLAS nodes below this index come from shared memory when the cache
+    // holds this scene's TLAS
+    const int cached = vvpt_tlas_cache_src == s.nodes + s.tlas_root ? vvpt_tlas_cache_count : 0;
     auto push = [&](int value, int tag, int count) {
         if (sp < kTraversalStack)
             stack[sp++] = make_int2(value, (tag << 28) | count);
@@ -263,7 +314,8 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             continue;
         }
         if (node >= 0) {
-            const BVHNode n = load_node(s.nodes, (int)node_base + node);
+            const BVHNode n = (!in_blas && node < cached) ? load_node_cached(node)
+                                                          : load_node(s.nodes, (int)node_base + node);
             float tl, tr;
             const float far_t = cull_far(best.t, slack);
             box2(n, co, cinvd, box_tmin, far_t, tl, tr);

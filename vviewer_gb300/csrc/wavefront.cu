@@ -472,6 +472,10 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
     uint32_t err = 0;
+    if (blockIdx.x * blockDim.x < n)
+        tlas_cache_fill(jt.jobs[ps.job[queue[blockIdx.x * blockDim.x]]].scene);
+    else
+        tlas_cache_none();
     // Lanes run independently: a lane takes its next ray as soon as its
     // current one is done, so a warp is never held by its slowest ray. The
     // shade bin is written per queue entry and compacted by k_partition.
@@ -551,6 +555,10 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_walk(JobTable jt
 {
     const uint32_t n = q.counters[C_WALK];
     uint32_t err = 0;
+    if (blockIdx.x * blockDim.x < n)
+        tlas_cache_fill(jt.jobs[ps.job[q.walk[blockIdx.x * blockDim.x]]].scene);
+    else
+        tlas_cache_none();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = q.walk[i];
         const JobView &J = jt.jobs[ps.job[slot]];
@@ -614,6 +622,15 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
     const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
     const uint32_t n = nl + np + nm;
     uint32_t err = 0, walks = 0;
+    {
+        const uint32_t f = blockIdx.x * blockDim.x;
+        if (f < n) {
+            const uint32_t slot = f < nl ? q.shade_l[f] : (f < nl + np ? q.shade_p[f - nl] : q.shade_m[f - nl - np]);
+            tlas_cache_fill(jt.jobs[ps.job[slot]].scene);
+        } else {
+            tlas_cache_none();
+        }
+    }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         uint32_t slot = 0;
@@ -1209,6 +1226,10 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
     uint32_t nsh = 0;
+    if (blockIdx.x * blockDim.x < n)
+        tlas_cache_fill(jt.jobs[ps.job[q.conn[blockIdx.x * blockDim.x]]].scene);
+    else
+        tlas_cache_none();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = q.conn[i];
         const uint32_t flags = ps.flags[slot];
@@ -1238,6 +1259,10 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_emitter(JobTable
     const uint32_t n = q.counters[C_CONN];
     uint32_t err = 0;
     uint32_t nnee = 0;
+    if (blockIdx.x * blockDim.x < n)
+        tlas_cache_fill(jt.jobs[ps.job[q.conn[blockIdx.x * blockDim.x]]].scene);
+    else
+        tlas_cache_none();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = q.conn[i];
         const uint32_t flags = ps.flags[slot];
@@ -1290,6 +1315,7 @@ __global__ void k_reduce(RenderParams p, BatchResults br, float4 *rad, float4 *a
 __global__ void k_trace_closest(SceneView s, const float4 *rays, uint32_t n, float4 *tuv, uint32_t *ids, uint32_t *err_out)
 {
     uint32_t err = 0;
+    tlas_cache_fill(s);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 a = rays[2 * i], b = rays[2 * i + 1];
         Hit h = trace_closest(s, f3(a), f3(b), a.w, b.w, err);
@@ -1334,22 +1360,22 @@ void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Qu
         k_regen<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
         break;
     case K_EXTEND:
-        k_extend<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
+        k_extend<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
         break;
     case K_PARTITION:
         k_partition<<<shape.grid, shape.block, 0, stream>>>(ps, q, pp);
         break;
     case K_WALK:
-        k_walk<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
+        k_walk<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
         break;
     case K_SHADE:
-        k_shade<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q, pp);
+        k_shade<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
         break;
     case K_SHADOW:
-        k_shadow<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
+        k_shadow<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
         break;
     case K_EMITTER:
-        k_emitter<<<shape.grid, shape.block, 0, stream>>>(jt, ps, q);
+        k_emitter<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
         break;
     default:
         break;
@@ -1370,7 +1396,7 @@ void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, fl
     int grid = (int)std::min<uint32_t>((n + 255) / 256, 65535u);
     if (grid < 1)
         grid = 1;
-    k_trace_closest<<<grid, 256, 0, stream>>>(s, rays, n, tuv, ids, err);
+    k_trace_closest<<<grid, 256, kTlasCacheBytes, stream>>>(s, rays, n, tuv, ids, err);
 }
 
 }  // namespace vvpt
