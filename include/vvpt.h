@@ -511,11 +511,20 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *denoiser,
                                               const vvpt_denoise_batch *batch,
                                               float learning_rate,
                                               float *out_loss);
-/* Convolution kernels: the tcgen05 tensor-core path (default: TMEM
- * accumulators, one-thread MMA issue from shared-memory descriptors) or the
- * warp-level mma.sync path (BF16 m16n8k16). Both accumulate in FP32; the
- * second serves as a cross-check of the first. */
-enum { VVPT_DENOISER_TCGEN05 = 0, VVPT_DENOISER_MMA_SYNC = 1 };
+/* Convolution kernels. TCGEN05 (default): tcgen05 tensor cores with TMEM
+ * accumulators; layers whose weights fit in shared memory run the strip
+ * kernel (TMA-fed ring of input rows, weights resident, one wave of
+ * persistent CTAs), the others a per-tile kernel. MMA_SYNC: the warp-level
+ * BF16 m16n8k16 path. TCGEN05_TILES: the per-tile tcgen05 kernels only.
+ * TCGEN05_PERSISTENT: the strip kernel on a small grid, so that every CTA
+ * walks several row segments. All accumulate in FP32; the last three serve
+ * as cross-checks of the first. */
+enum {
+    VVPT_DENOISER_TCGEN05 = 0,
+    VVPT_DENOISER_MMA_SYNC = 1,
+    VVPT_DENOISER_TCGEN05_TILES = 2,
+    VVPT_DENOISER_TCGEN05_PERSISTENT = 3
+};
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *denoiser, int kind);
 /* Denoises one image: out = exp(network(log1p radiance, albedo, normal)) - 1. */
 VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *denoiser,

@@ -105,25 +105,31 @@ def test_training_on_tracer_pairs_beats_the_noisy_render(ctx):
     dn.close()
 
 
-def test_tcgen05_and_mma_sync_kernels_agree(ctx):
-    """The tcgen05 convolutions (TMEM accumulators, default) against the
-    warp-level mma.sync ones on the same network and inputs: partial tiles at
-    every level (2 x 64 x 48 pixels, 24 at the coarsest level)."""
+@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_tiles", "tcgen05_persistent"])
+@pytest.mark.parametrize("n,h,w", [(2, 64, 48), (1, 48, 272)])
+def test_tcgen05_and_mma_sync_kernels_agree(ctx, kind, n, h, w):
+    """The tcgen05 convolutions (TMEM accumulators) against the warp-level
+    mma.sync ones on the same network and inputs: the default mix (strip
+    kernel where the weights fit), the per-tile kernels alone, and the strip
+    kernel on a 16-CTA grid (every CTA walks several row segments, so ring
+    slots and accumulators change phase across segments). Partial tiles at
+    every level: 2 x 64 x 48 pixels (narrower than one 130-pixel input box)
+    and 48 x 272 (three 128-pixel columns at full resolution, the last 16
+    wide; 136 at the next level)."""
     import torch
     rng = np.random.default_rng(6)
-    n, h, w = 2, 64, 48
     ins = [_cuda(rng.gamma(1.0, 0.5, (n, h, w, 4))), _cuda(rng.uniform(0, 1, (n, h, w, 4))),
            _cuda(rng.uniform(0, 1, (n, h, w, 4))), _cuda(rng.gamma(1.0, 0.5, (n, h, w, 4)))]
     dn = Denoiser(ctx, seed=9)
     out = {}
-    for kind in ("mma_sync", "tcgen05"):
-        dn.set_kernels(kind)
+    for k in ("mma_sync", kind):
+        dn.set_kernels(k)
         loss, g = dn.gradients(*ins)
         o = torch.zeros((h, w, 4), device="cuda")
         dn.apply(ins[0][0], ins[1][0], ins[2][0], o)
         torch.cuda.synchronize()
-        out[kind] = (loss, g, o.cpu().numpy())
-    (l0, g0, o0), (l1, g1, o1) = out["mma_sync"], out["tcgen05"]
+        out[k] = (loss, g, o.cpu().numpy())
+    (l0, g0, o0), (l1, g1, o1) = out["mma_sync"], out[kind]
     assert abs(l0 - l1) <= 1e-3 * l0
     assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
     assert np.allclose(o1, o0, rtol=2e-2, atol=1e-3)

@@ -103,6 +103,7 @@ struct vvpt_denoiser {
     bool with_grads = false;
     DevBuf acts, gacts, out_f32, target3, dout, loss, err;
     bool mma_sync = false; // warp-level mma.sync convolutions instead of tcgen05
+    vvdn::ConvKernels conv_kind = vvdn::kConvAuto;
     // tensors: x[l], a[l], e[l]; u[l], b[l], d[l] (l < 4)
     // gskip[l]: gradient of e_l through the decoder's concat (gradient pool only)
     Tensor x[kLevels], a[kLevels], e[kLevels], u[kLevels - 1], b[kLevels - 1], d[kLevels - 1], gskip[kLevels - 1];
@@ -184,7 +185,7 @@ void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, b
     a.n = dn->n;
     a.h = dn->h >> level;
     a.wd = dn->w >> level;
-    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>());
+    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>(), dn->conv_kind);
 }
 
 // input gradient of layer li: din = conv(dout, w_t) * (mask > 0)
@@ -204,7 +205,7 @@ void conv_dgrad(vvpt_denoiser *dn, int li, const bf16 *dout, bf16 *din, const bf
     a.n = dn->n;
     a.h = dn->h >> level;
     a.wd = dn->w >> level;
-    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>());
+    vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>(), dn->conv_kind);
 }
 
 void conv_wgrad(vvpt_denoiser *dn, int li, const bf16 *dout, const bf16 *in, int level, cudaStream_t s)
@@ -443,9 +444,12 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *dn, const vvpt_deno
 
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *dn, int kind)
 {
-    if (!dn || (kind != VVPT_DENOISER_TCGEN05 && kind != VVPT_DENOISER_MMA_SYNC))
+    if (!dn || kind < VVPT_DENOISER_TCGEN05 || kind > VVPT_DENOISER_TCGEN05_PERSISTENT)
         return VVPT_ERR_INVALID_ARG;
     dn->mma_sync = kind == VVPT_DENOISER_MMA_SYNC;
+    dn->conv_kind = kind == VVPT_DENOISER_TCGEN05_TILES        ? vvdn::kConvTiles
+                    : kind == VVPT_DENOISER_TCGEN05_PERSISTENT ? vvdn::kConvPersistent
+                                                               : vvdn::kConvAuto;
     return VVPT_OK;
 }
 

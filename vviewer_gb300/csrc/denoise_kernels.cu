@@ -4,6 +4,9 @@
 // ldmatrix.
 #include <algorithm>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "denoise_kernels.cuh"
 
 namespace vvdn {
@@ -342,77 +345,139 @@ __global__ void k_pack_target(const float4 *t, float *t3, int npix)
     }
 }
 
+// The layout kernels below move 8 channels (16 bytes) per thread: channel
+// counts are multiples of 8, so every access is one aligned 128-bit load or
+// store and a warp covers 512 consecutive bytes. Index arithmetic is 32-bit
+// (element counts stay below 2^31; the host checks).
+__device__ __forceinline__ void unpack8(const uint4 &v, float (&f)[8])
+{
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float2 t = __bfloat1622float2(h[k]);
+        f[2 * k] = t.x;
+        f[2 * k + 1] = t.y;
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8])
+{
+    uint4 v;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    return v;
+}
+
+__device__ __forceinline__ uint4 ld16(const bf16 *p) { return __ldg(reinterpret_cast<const uint4 *>(p)); }
+__device__ __forceinline__ void st16(bf16 *p, const uint4 &v) { *reinterpret_cast<uint4 *>(p) = v; }
+
 __global__ void k_avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c)
 {
-    const int ho = h / 2, wo = w / 2;
-    const long total = (long)n * ho * wo * c;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        const long q = i / c;
-        const int x = (int)(q % wo), y = (int)((q / wo) % ho), b = (int)(q / ((long)wo * ho));
-        const long base = (((long)b * h + 2 * y) * w + 2 * x) * c + ch;
-        const float s = __bfloat162float(in[base]) + __bfloat162float(in[base + c]) +
-                        __bfloat162float(in[base + (long)w * c]) + __bfloat162float(in[base + (long)w * c + c]);
-        out[i] = __float2bfloat16_rn(0.25f * s);
+    const unsigned ho = h / 2, wo = w / 2, g = c / 8;
+    const unsigned total = (unsigned)n * ho * wo * g;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cg = i % g, q = i / g;
+        const unsigned x = q % wo, y = (q / wo) % ho, b = q / (wo * ho);
+        const size_t base = (((size_t)b * h + 2 * y) * w + 2 * x) * c + 8 * cg, row = (size_t)w * c;
+        float a[8], t[8];
+        unpack8(ld16(in + base), a);
+        unpack8(ld16(in + base + c), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] += t[k];
+        unpack8(ld16(in + base + row), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] += t[k];
+        unpack8(ld16(in + base + row + c), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] = 0.25f * (a[k] + t[k]);
+        st16(out + (size_t)i * 8, pack8(a));
     }
 }
 
 __global__ void k_upcat(const bf16 *coarse, int cc, const bf16 *skip, int cs, bf16 *out, int n, int h, int w)
 {
-    const int ct = cc + cs;
-    const long total = (long)n * h * w * ct;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % ct);
-        const long p = i / ct;
-        if (ch < cc) {
-            const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long)w * h));
-            out[i] = coarse[(((long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * cc + ch];
+    const unsigned gc = cc / 8, gt = (cc + cs) / 8;
+    const unsigned total = (unsigned)n * h * w * gt;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cg = i % gt, p = i / gt;
+        uint4 v;
+        if (cg < gc) {
+            const unsigned x = p % w, y = (p / w) % h, b = p / (w * h);
+            v = ld16(coarse + (((size_t)b * (h / 2) + y / 2) * (w / 2) + x / 2) * cc + 8 * cg);
         } else {
-            out[i] = skip[p * cs + (ch - cc)];
+            v = ld16(skip + (size_t)p * cs + 8 * (cg - gc));
         }
+        st16(out + (size_t)i * 8, v);
     }
 }
 
 __global__ void k_upcat_backward_coarse(const bf16 *dcat, int cc, int cs, bf16 *dcoarse, int n, int h, int w)
 {
-    const int ct = cc + cs, ho = h / 2, wo = w / 2;
-    const long total = (long)n * ho * wo * cc;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % cc);
-        const long q = i / cc;
-        const int x = (int)(q % wo), y = (int)((q / wo) % ho), b = (int)(q / ((long)wo * ho));
-        const long base = (((long)b * h + 2 * y) * w + 2 * x) * ct + ch;
-        const float s = __bfloat162float(dcat[base]) + __bfloat162float(dcat[base + ct]) +
-                        __bfloat162float(dcat[base + (long)w * ct]) + __bfloat162float(dcat[base + (long)w * ct + ct]);
-        dcoarse[i] = __float2bfloat16_rn(s);
+    const int ct = cc + cs;
+    const unsigned ho = h / 2, wo = w / 2, g = cc / 8;
+    const unsigned total = (unsigned)n * ho * wo * g;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cg = i % g, q = i / g;
+        const unsigned x = q % wo, y = (q / wo) % ho, b = q / (wo * ho);
+        const size_t base = (((size_t)b * h + 2 * y) * w + 2 * x) * ct + 8 * cg, row = (size_t)w * ct;
+        float a[8], t[8];
+        unpack8(ld16(dcat + base), a);
+        unpack8(ld16(dcat + base + ct), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] += t[k];
+        unpack8(ld16(dcat + base + row), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] += t[k];
+        unpack8(ld16(dcat + base + row + ct), t);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            a[k] += t[k];
+        st16(dcoarse + (size_t)i * 8, pack8(a));
     }
 }
 
-__global__ void k_upcat_backward_skip(const bf16 *dcat, int cc, int cs, bf16 *dskip, long npix)
+__global__ void k_upcat_backward_skip(const bf16 *dcat, int cc, int cs, bf16 *dskip, unsigned npix)
 {
-    const int ct = cc + cs;
-    const long total = npix * cs;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % cs);
-        const long p = i / cs;
-        dskip[i] = dcat[p * ct + cc + ch];
+    const unsigned g = cs / 8, gt = (cc + cs) / 8, gc = cc / 8;
+    const unsigned total = npix * g;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cg = i % g, p = i / g;
+        st16(dskip + (size_t)i * 8, ld16(dcat + ((size_t)p * gt + gc + cg) * 8));
     }
 }
 
 __global__ void k_pool_backward_combine(const bf16 *dskip, const bf16 *dpooled, const bf16 *e, bf16 *de, int n, int h,
                                         int w, int c)
 {
-    const long total = (long)n * h * w * c;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        const long p = i / c;
-        const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long)w * h));
-        float v = 0.25f * __bfloat162float(dpooled[(((long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch]);
-        if (dskip)
-            v += __bfloat162float(dskip[i]);
-        if (!(__bfloat162float(e[i]) > 0.0f))
-            v = 0.0f;
-        de[i] = __float2bfloat16_rn(v);
+    const unsigned g = c / 8;
+    const unsigned total = (unsigned)n * h * w * g;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cg = i % g, p = i / g;
+        const unsigned x = p % w, y = (p / w) % h, b = p / (w * h);
+        float v[8], t[8], m[8];
+        unpack8(ld16(dpooled + (((size_t)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + 8 * cg), v);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            v[k] *= 0.25f;
+        if (dskip) {
+            unpack8(ld16(dskip + (size_t)i * 8), t);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                v[k] += t[k];
+        }
+        unpack8(ld16(e + (size_t)i * 8), m);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (!(m[k] > 0.0f))
+                v[k] = 0.0f;
+        st16(de + (size_t)i * 8, pack8(v));
     }
 }
 
@@ -484,7 +549,6 @@ int grid_for(long n, int block = 256)
 // kernel records an error, stops issuing and still frees its TMEM.
 constexpr int kTcM = 128, kTcBK = 32, kTcKC = kTcBK / 8, kTcBStages = 4, kTcHaloPx = kTcM + 2;
 constexpr int kTcHaloRow = kTcKC * kTcHaloPx * 16;  // one halo row: 4 channel groups x 130 pixels x 16 B
-constexpr int kTcHaloBytes = 3 * kTcHaloRow;        // 24,960 B
 constexpr int kTcHaloAlloc = 25088;                 // rounded up to 1 KB multiples
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
@@ -520,6 +584,45 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
 {
     return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Epilogue of one pixel row x 16 channels: bias, ReLU, mask, store (bf16, or
+// f32 for the output layer).
+__device__ __forceinline__ void store_row16(const ConvArgs &a, long p, int c, const uint32_t (&r)[16])
+{
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        v[k] = __uint_as_float(r[k]);
+        if (a.bias)
+            v[k] += a.bias[c + k];
+        if (a.relu)
+            v[k] = fmaxf(v[k], 0.0f);
+    }
+    const long o = p * a.cout + c;
+    if (a.mask) {
+        __align__(16) bf16 m[16];
+        *reinterpret_cast<uint4 *>(&m[0]) = *reinterpret_cast<const uint4 *>(a.mask + o);
+        *reinterpret_cast<uint4 *>(&m[8]) = *reinterpret_cast<const uint4 *>(a.mask + o + 8);
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (!(__bfloat162float(m[k]) > 0.0f))
+                v[k] = 0.0f;
+    }
+    if (a.out_f32) {
+        float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + o);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+        __align__(16) __nv_bfloat162 hh[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            hh[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+        uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(a.out) + o);
+        dst[0] = *reinterpret_cast<const uint4 *>(&hh[0]);
+        dst[1] = *reinterpret_cast<const uint4 *>(&hh[4]);
+    }
 }
 
 __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint32_t *err)
@@ -646,39 +749,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
             asm volatile("tcgen05.wait::ld.sync.aligned;");
             if (x >= a.wd || c >= a.cout)
                 continue;
-            float v[16];
-#pragma unroll
-            for (int k = 0; k < 16; k++) {
-                v[k] = __uint_as_float(r[k]);
-                if (a.bias)
-                    v[k] += a.bias[c + k];
-                if (a.relu)
-                    v[k] = fmaxf(v[k], 0.0f);
-            }
-            const long o = p * a.cout + c;
-            if (a.mask) {
-                __align__(16) bf16 m[16];
-                *reinterpret_cast<uint4 *>(&m[0]) = *reinterpret_cast<const uint4 *>(a.mask + o);
-                *reinterpret_cast<uint4 *>(&m[8]) = *reinterpret_cast<const uint4 *>(a.mask + o + 8);
-#pragma unroll
-                for (int k = 0; k < 16; k++)
-                    if (!(__bfloat162float(m[k]) > 0.0f))
-                        v[k] = 0.0f;
-            }
-            if (a.out_f32) {
-                float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.out) + o);
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-            } else {
-                __align__(16) __nv_bfloat162 hh[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++)
-                    hh[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
-                uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(a.out) + o);
-                dst[0] = *reinterpret_cast<const uint4 *>(&hh[0]);
-                dst[1] = *reinterpret_cast<const uint4 *>(&hh[4]);
-            }
+            store_row16(a, p, c, r);
         }
     } else if (tid == 0) {
         atomicOr(err, 1u);
@@ -689,15 +760,489 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
+// Chunk-batched variant for N <= 128 output channels: a stage holds the halo
+// and the weights of all 9 taps of one 32-channel chunk, so a chunk is one
+// barrier and 18 back-to-back MMAs; two stages alternate (the next chunk's
+// copies overlap this chunk's MMAs). Same layouts, waits and error handling
+// as k_conv3x3_tc.
+
+// one stage when the layer has a single chunk, else two
+__host__ __device__ constexpr int tc_chunk_smem_bytes(int N, int nchunks)
+{
+    return (nchunks > 1 ? 2 : 1) * (kTcHaloAlloc + 9 * N * kTcBK * 2);
+}
+
+__global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols, uint32_t *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint32_t tmem_holder;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (a.wd + kTcM - 1) / kTcM;
+    const int tx = blockIdx.x % tiles_x;
+    const int y = (blockIdx.x / tiles_x) % a.h;
+    const int nb = blockIdx.x / (tiles_x * a.h);
+    const int x0 = tx * kTcM;
+    const int N = (a.cout + 15) & ~15;
+    const int tap_bytes = N * kTcBK * 2;
+    const int stage_bytes = kTcHaloAlloc + 9 * tap_bytes;
+    const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
+    const uint32_t sbase = smem_addr(smem);
+
+    if (tid == 0) {
+        for (int st = 0; st < 2; st++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[st])));
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_holder)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_holder;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+
+    auto load_chunk = [&](int c) {
+        uint8_t *h = smem + (c & 1) * stage_bytes;
+        uint8_t *bw = h + kTcHaloAlloc;
+        const int ci0 = c * kTcBK;
+        for (int i = tid; i < 3 * kTcKC * kTcHaloPx; i += 128) {
+            const int px = i % kTcHaloPx, kc = (i / kTcHaloPx) % kTcKC, hr = i / (kTcHaloPx * kTcKC);
+            const int yy = y + hr - 1, xx = x0 - 1 + px, ci = ci0 + 8 * kc;
+            const bool ok = yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd && ci < a.cin;
+            const bf16 *src = ok ? a.in + (((long)nb * a.h + yy) * a.wd + xx) * a.cin + ci : a.in;
+            cp_async16(h + ((hr * kTcKC + kc) * kTcHaloPx + px) * 16, src, ok);
+        }
+        for (int i = tid; i < 9 * N * kTcKC; i += 128) {
+            const int kc = i % kTcKC, n = (i / kTcKC) % N, tap = i / (kTcKC * N), ci = ci0 + 8 * kc;
+            const bool ok = n < a.cout && ci < a.cin;
+            const bf16 *src = ok ? a.wgt + ((long)n * 9 + tap) * a.cin + ci : a.wgt;
+            cp_async16(bw + tap * tap_bytes + (n >> 3) * (kTcKC * 128) + kc * 128 + (n & 7) * 16, src, ok);
+        }
+    };
+
+    load_chunk(0);
+    cp_async_commit();
+    for (int c = 0; c < nchunks; c++) {
+        cp_async_wait<0>(); // this thread's copies of chunk c landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (abort_flag)
+            break;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t h_addr = sbase + (c & 1) * stage_bytes, b_addr = h_addr + kTcHaloAlloc;
+            for (int tap = 0; tap < 9; tap++) {
+                const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+                for (int j = 0; j < kTcBK / 16; j++) {
+                    const uint64_t ad =
+                        umma_desc(h_addr + dy * kTcHaloRow + dx * 16 + j * 2 * kTcHaloPx * 16, kTcHaloPx * 16, 128);
+                    const uint64_t bd = umma_desc(b_addr + tap * tap_bytes + j * 2 * 128, 128, kTcKC * 128);
+                    const uint32_t accumulate = (c > 0 || tap > 0 || j > 0) ? 1u : 0u;
+                    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                                 "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&mbar[c & 1])));
+        }
+        // chunk c + 1 goes to the stage chunk c - 1 was read from; the MMAs of
+        // chunk c are queued behind it meanwhile
+        if (c + 1 < nchunks) {
+            if (c >= 1 && !mbar_wait(smem_addr(&mbar[(c - 1) & 1]), ((c - 1) >> 1) & 1))
+                atomicOr(&abort_flag, 1);
+            load_chunk(c + 1);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    if (!abort_flag && nchunks > 0) {
+        const int last = nchunks - 1;
+        if (!mbar_wait(smem_addr(&mbar[last & 1]), (last >> 1) & 1))
+            atomicOr(&abort_flag, 1);
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!abort_flag) {
+        const int x = x0 + warp * 32 + lane;
+        const long p = ((long)nb * a.h + y) * a.wd + x;
+        for (int c = 0; c < N; c += 16) {
+            uint32_t r[16];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                         "%12, %13, %14, %15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15])
+                         : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (x >= a.wd || c >= a.cout)
+                continue;
+            store_row16(a, p, c, r);
+        }
+    } else if (tid == 0) {
+        atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// Strip kernel: TMA-fed, weights resident, persistent over runs of rows.
+//
+// A unit of work is a 128-pixel-wide column of one image and a run of
+// consecutive output rows (a segment); a CTA runs its units one after the
+// other. The weights of the whole layer (9 x N x cin bf16) are loaded once and
+// stay in shared memory. Input rows arrive by TMA into a ring of `ring` slots,
+// each one halo row of 130 pixels x cin channels; the tensor map zero-fills
+// pixels and rows outside the image, which is the convolution's zero padding.
+// Output row i of a segment reads halo rows i, i + 1, i + 2, so every output
+// row needs one new halo row (the input is read once, not three times).
+// Slot layout (K-major, no swizzle): per 8-channel group the 130 pixels are
+// consecutive 16-byte rows (one TMA box of 8 channels x 130 pixels), groups
+// kStKCBytes apart; a tap (dy, dx) of output row i is the operand starting at
+// slot(i + dy) + 16 dx (SBO 128 B between 8-pixel groups, LBO kStKCBytes
+// between channel groups). Two TMEM accumulators alternate: one thread issues
+// the MMAs of row i (9 taps x cin / 16 steps) and commits them to the row's
+// mbarrier while all four warps drain row i - 1 (TMEM lane = pixel). The slot
+// of halo row i - 1 is refilled once the MMAs of row i - 1 are complete.
+// Halo rows and output rows are counted over the CTA's whole run, so slot
+// and accumulator phases carry across units. Every wait is bounded by the
+// global timer; on a timeout the kernel records an error, stops issuing,
+// waits (bounded) for its copies and MMAs in flight and frees its TMEM.
+constexpr int kStKCBytes = 2176; // 130 pixels x 16 B, padded to a multiple of 128 B
+constexpr int kStHaloPx = kTcM + 2;
+constexpr int kStMaxRing = 8, kStMinRing = 4;
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap, int ncols,
+                                                        int ring, int segs, int seg_rows, uint32_t *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    __shared__ uint32_t tmem_holder;
+    __shared__ __align__(8) uint64_t full[kStMaxRing];
+    __shared__ __align__(8) uint64_t mma_done[2];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (a.wd + kTcM - 1) / kTcM;
+    const int units = a.n * tiles_x * segs;
+    const int KC = a.cin >> 3;
+    const int N = (a.cout + 15) & ~15;
+    const int slot_bytes = KC * kStKCBytes;
+    const int tap_bytes = N * a.cin * 2;
+    const uint32_t half_cols = (uint32_t)ncols >> 1;
+    const uint32_t raw = smem_addr(smem_raw);
+    const uint32_t ring_base = (raw + 1023u) & ~1023u;
+    const uint32_t w_base = ring_base + (uint32_t)(ring * slot_bytes);
+    uint8_t *w_ptr = smem_raw + (w_base - raw);
+    const uint64_t tmap_ptr = reinterpret_cast<uint64_t>(&tmap);
+    const uint32_t row_tx = (uint32_t)(KC * kStHaloPx * 16);
+
+    if (tid == 0) {
+        for (int r = 0; r < ring; r++)
+            mbar_init(&full[r], 1);
+        mbar_init(&mma_done[0], 1);
+        mbar_init(&mma_done[1], 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_holder)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    for (int i = tid; i < 9 * N * KC; i += 128) {
+        const int kc = i % KC, n = (i / KC) % N, tap = i / (KC * N);
+        const bool ok = n < a.cout;
+        const bf16 *src = ok ? a.wgt + ((long)n * 9 + tap) * a.cin + 8 * kc : a.wgt;
+        cp_async16(w_ptr + tap * tap_bytes + (n >> 3) * (KC * 128) + kc * 128 + (n & 7) * 16, src, ok);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_holder;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+
+    // descriptor fields other than the start address (16-byte units in the
+    // low 14 bits; shared addresses stay below 256 KB, so adding an offset to
+    // a descriptor adds it to the address field)
+    const uint64_t a_hi = umma_desc(0, kStKCBytes, 128), b_hi = umma_desc(0, 128, (uint32_t)(KC * 128));
+    const uint32_t a_lo_base = ring_base >> 4, a_lo_slot = (uint32_t)slot_bytes >> 4;
+    const uint32_t b_lo_base = w_base >> 4, b_lo_tap = (uint32_t)tap_bytes >> 4;
+
+    // thread 0's view of the pipeline, counted over the CTA's run
+    int g_issued = 0, g_waited = 0;  // halo rows loaded / seen complete
+    int issue_slot = 0;              // ring slot of halo row g_issued
+    int wait_slot = 0, wait_phase = 0; // ring slot and parity of halo row g_waited
+    int g_mma = -1;                  // last output row whose MMAs were committed
+    int g_row = 0;                   // output rows of earlier units
+    int g_halo = 0;                  // halo rows of earlier units
+
+    for (int u = blockIdx.x; u < units && !abort_flag; u += gridDim.x) {
+        const int sg = u % segs, tx = (u / segs) % tiles_x, nb = u / (segs * tiles_x);
+        const int x0 = tx * kTcM, ya = sg * seg_rows;
+        const int nout = min(a.h, ya + seg_rows) - ya;
+        if (nout <= 0)
+            continue;
+        const int nh = nout + 2;
+        // halo rows are issued in order, one slot after the other
+        auto issue_row = [&](int) {
+            const int slot = issue_slot;
+            issue_slot = slot + 1 == ring ? 0 : slot + 1;
+            const int h = g_issued - g_halo;
+            const uint32_t bar = smem_addr(&full[slot]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(row_tx) : "memory");
+            const uint32_t dst = ring_base + (uint32_t)(slot * slot_bytes);
+            for (int kc = 0; kc < KC; kc++)
+                asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                             "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst + (uint32_t)(kc * kStKCBytes)),
+                             "l"(tmap_ptr), "r"(8 * kc), "r"(x0 - 1), "r"(ya - 1 + h), "r"(nb), "r"(bar)
+                             : "memory");
+            g_issued++;
+        };
+        auto drain = [&](int gi, int i) {
+            // output row i of this unit, accumulator gi & 1
+            const int x = x0 + warp * 32 + lane;
+            const long p = ((long)nb * a.h + ya + i) * a.wd + x;
+            const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(gi & 1) * half_cols;
+            for (int c = 0; c < N; c += 16) {
+                uint32_t r[16];
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+                             "%11, %12, %13, %14, %15}, [%16];"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                               "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                             : "r"(acc + (uint32_t)c));
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (x < a.wd && c < a.cout)
+                    store_row16(a, p, c, r);
+            }
+        };
+        // every halo row of earlier units has been consumed: this unit's halo
+        // row 0 goes to the next slot
+        int row_slot = issue_slot; // slot of this unit's halo row i
+        if (tid == 0)
+            for (int h = 0; h < min(ring, nh); h++)
+                issue_row(h);
+        for (int i = 0; i < nout; i++) {
+            const int gi = g_row + i;
+            if (tid == 0) {
+                bool ok = true;
+                while (ok && g_waited < g_halo + i + 3) {
+                    ok = mbar_wait(smem_addr(&full[wait_slot]), (uint32_t)wait_phase);
+                    if (ok) {
+                        g_waited++;
+                        if (++wait_slot == ring) {
+                            wait_slot = 0;
+                            wait_phase ^= 1;
+                        }
+                    }
+                }
+                if (!ok) {
+                    abort_flag = 1;
+                } else {
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t acc = tmem + (uint32_t)(gi & 1) * half_cols;
+#pragma unroll
+                    for (int tap = 0; tap < 9; tap++) {
+                        const int dy = tap / 3, dx = tap % 3;
+                        int sl = row_slot + dy;
+                        sl = sl >= ring ? sl - ring : sl;
+                        const uint32_t a_lo = a_lo_base + (uint32_t)sl * a_lo_slot + (uint32_t)dx;
+                        const uint32_t b_lo = b_lo_base + (uint32_t)tap * b_lo_tap;
+                        for (int j = 0; j < KC / 2; j++) {
+                            const uint64_t ad = a_hi | (uint64_t)(a_lo + (uint32_t)j * (2 * kStKCBytes / 16));
+                            const uint64_t bd = b_hi | (uint64_t)(b_lo + (uint32_t)j * (2 * 128 / 16));
+                            const uint32_t accumulate = (tap > 0 || j > 0) ? 1u : 0u;
+                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(acc),
+                                         "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+                        }
+                    }
+                    asm volatile(
+                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                            smem_addr(&mma_done[gi & 1])));
+                    g_mma = gi;
+                }
+            }
+            if (i >= 1) {
+                const int gp = gi - 1;
+                bool ok = mbar_wait(smem_addr(&mma_done[gp & 1]), (uint32_t)((gp >> 1) & 1));
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
+                    abort_flag = 1;
+                if (ok) {
+                    // the slot of halo row i - 1 is free once the MMAs of row i - 1 are done
+                    if (tid == 0 && !abort_flag && i - 1 + ring < nh)
+                        issue_row(i - 1 + ring);
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    drain(gp, i - 1);
+                }
+            }
+            row_slot = row_slot + 1 == ring ? 0 : row_slot + 1;
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            if (abort_flag)
+                break;
+        }
+        if (!abort_flag) {
+            const int gl = g_row + nout - 1;
+            bool ok = mbar_wait(smem_addr(&mma_done[gl & 1]), (uint32_t)((gl >> 1) & 1));
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok)
+                abort_flag = 1;
+            else {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                drain(gl, nout - 1);
+            }
+        }
+        g_row += nout;
+        g_halo += nh;
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    }
+    if (abort_flag && tid == 0) {
+        atomicOr(err, 1u);
+        // let copies and MMAs still in flight land before the CTA exits
+        for (int g = g_waited; g < g_issued; g++) {
+            if (!mbar_wait(smem_addr(&full[wait_slot]), (uint32_t)wait_phase))
+                break;
+            if (++wait_slot == ring) {
+                wait_slot = 0;
+                wait_phase ^= 1;
+            }
+        }
+        if (g_mma >= 0)
+            mbar_wait(smem_addr(&mma_done[g_mma & 1]), (uint32_t)((g_mma >> 1) & 1));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
 }  // namespace
 
-void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+struct StripPlan {
+    int ring = 0, smem = 0, grid = 0, segs = 0, seg_rows = 0, ncols = 0;
+};
+
+// Occupancy first (up to 4 CTAs per SM, bounded by shared memory and by the
+// 512 TMEM columns of an SM), then the deepest ring that fits; the rows of
+// every 128-pixel column are cut into segments so that one wave of CTAs
+// covers the layer.
+bool plan_strip(const ConvArgs &a, StripPlan &pl)
+{
+    if (a.cin % 16 || a.cin < 16 || a.cout > 256 || a.cout < 1 || (reinterpret_cast<uintptr_t>(a.in) & 15))
+        return false;
+    static int nsm = 0, sm_smem = 0, optin = 0, reserved = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    }
+    if (!tensor_map_encoder())
+        return false;
+    const int N = (a.cout + 15) & ~15;
+    const int wbytes = 9 * N * a.cin * 2, slot = (a.cin / 8) * kStKCBytes;
+    int ncols = 32;
+    while (ncols < 2 * N)
+        ncols <<= 1;
+    constexpr int kStatic = 2048; // mbarriers, TMEM address, flags (1 KB aligned)
+    for (int c = 4; c >= 1; c--) {
+        if (c * ncols > 512)
+            continue;
+        const int dyn = std::min(optin - kStatic, sm_smem / c - reserved - kStatic);
+        const int ring = std::min(kStMaxRing, (dyn - 1024 - wbytes) / slot);
+        if (ring < kStMinRing)
+            continue;
+        const long cols = (long)a.n * ((a.wd + kTcM - 1) / kTcM);
+        const long ctas = (long)nsm * c;
+        int segs = (int)std::max<long>(1, std::min<long>(a.h, ctas / std::max<long>(1, cols)));
+        const int seg_rows = (a.h + segs - 1) / segs;
+        segs = (a.h + seg_rows - 1) / seg_rows;
+        pl.ring = ring;
+        pl.smem = dyn;
+        pl.segs = segs;
+        pl.seg_rows = seg_rows;
+        pl.ncols = ncols;
+        pl.grid = (int)std::min<long>(cols * segs, ctas);
+        return true;
+    }
+    return false;
+}
+
+// rank-4 map over the NHWC input {C, W, H, N}; box = 8 channels x 130 pixels
+bool encode_input_map(const ConvArgs &a, CUtensorMap &m)
+{
+    const cuuint64_t dims[4] = {(cuuint64_t)a.cin, (cuuint64_t)a.wd, (cuuint64_t)a.h, (cuuint64_t)a.n};
+    const cuuint64_t strides[3] = {(cuuint64_t)a.cin * 2, (cuuint64_t)a.wd * a.cin * 2,
+                                   (cuuint64_t)a.h * a.wd * a.cin * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kStHaloPx, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(a.in), dims, strides, box,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
 {
     const long P = (long)a.n * a.h * a.wd;
+    StripPlan pl;
+    CUtensorMap tmap;
+    if (err && kind != kConvTiles && plan_strip(a, pl) && encode_input_map(a, tmap)) {
+        if (kind == kConvPersistent)
+            pl.grid = std::min(pl.grid, 16);
+        static int attr_smem = 0;
+        if (pl.smem > attr_smem) {
+            cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem);
+            cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+            attr_smem = pl.smem;
+        }
+        k_conv3x3_strip<<<pl.grid, 128, pl.smem, s>>>(a, tmap, pl.ncols, pl.ring, pl.segs, pl.seg_rows, err);
+        return;
+    }
     if (err && a.cout <= 256) {
         static bool attr_set = false;
         if (!attr_set) {
             cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes(256));
+            cudaFuncSetAttribute(k_conv3x3_tc_chunk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc_chunk_smem_bytes(128, 2));
             attr_set = true;
         }
         const int N = (a.cout + 15) & ~15;
@@ -705,7 +1250,11 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err)
         while (ncols < N)
             ncols <<= 1;
         const long tiles = (long)a.n * a.h * ((a.wd + kTcM - 1) / kTcM);
-        k_conv3x3_tc<<<(unsigned)tiles, 128, tc_smem_bytes(N), s>>>(a, ncols, err);
+        if (N <= 128)
+            k_conv3x3_tc_chunk<<<(unsigned)tiles, 128, tc_chunk_smem_bytes(N, (a.cin + kTcBK - 1) / kTcBK), s>>>(
+                a, ncols, err);
+        else
+            k_conv3x3_tc<<<(unsigned)tiles, 128, tc_smem_bytes(N), s>>>(a, ncols, err);
         return;
     }
     // 32-wide channel tiles where they leave fewer channels of the last tile
@@ -760,27 +1309,34 @@ void pack_target(const float *target, float *t3, int npix, cudaStream_t s)
     k_pack_target<<<grid_for(npix), 256, 0, s>>>(reinterpret_cast<const float4 *>(target), t3, npix);
 }
 
+// 8-channel groups of a layout kernel, indexed in 32 bits by the kernels: the
+// denoiser's batch limit (n x h x w <= 2^27 pixels, at most 80 channels at
+// full resolution) keeps every count below 2^31
+static long groups8(long pixels, int c) { return pixels * (c / 8); }
+
 void avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c, cudaStream_t s)
 {
-    k_avgpool2<<<grid_for((long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(in, out, n, h, w, c);
+    k_avgpool2<<<grid_for(groups8((long)n * (h / 2) * (w / 2), c)), 256, 0, s>>>(in, out, n, h, w, c);
 }
 
 void upcat(const bf16 *coarse, int cc, const bf16 *skip, int cs, bf16 *out, int n, int h, int w, cudaStream_t s)
 {
-    k_upcat<<<grid_for((long)n * h * w * (cc + cs)), 256, 0, s>>>(coarse, cc, skip, cs, out, n, h, w);
+    k_upcat<<<grid_for(groups8((long)n * h * w, cc + cs)), 256, 0, s>>>(coarse, cc, skip, cs, out, n, h, w);
 }
 
 void upcat_backward(const bf16 *dcat, int cc, int cs, bf16 *dcoarse, bf16 *dskip, int n, int h, int w, cudaStream_t s)
 {
-    k_upcat_backward_coarse<<<grid_for((long)n * (h / 2) * (w / 2) * cc), 256, 0, s>>>(dcat, cc, cs, dcoarse, n, h, w);
+    k_upcat_backward_coarse<<<grid_for(groups8((long)n * (h / 2) * (w / 2), cc)), 256, 0, s>>>(dcat, cc, cs, dcoarse,
+                                                                                                n, h, w);
     if (dskip)
-        k_upcat_backward_skip<<<grid_for((long)n * h * w * cs), 256, 0, s>>>(dcat, cc, cs, dskip, (long)n * h * w);
+        k_upcat_backward_skip<<<grid_for(groups8((long)n * h * w, cs + cc)), 256, 0, s>>>(dcat, cc, cs, dskip,
+                                                                                          (unsigned)((long)n * h * w));
 }
 
 void pool_backward_combine(const bf16 *dskip, const bf16 *dpooled, const bf16 *e, bf16 *de, int n, int h, int w, int c,
                            cudaStream_t s)
 {
-    k_pool_backward_combine<<<grid_for((long)n * h * w * c), 256, 0, s>>>(dskip, dpooled, e, de, n, h, w, c);
+    k_pool_backward_combine<<<grid_for(groups8((long)n * h * w, c)), 256, 0, s>>>(dskip, dpooled, e, de, n, h, w, c);
 }
 
 void l1_loss(const float *out, int cout, const float *t3, bf16 *dout, float *loss_sum, int npix, cudaStream_t s)

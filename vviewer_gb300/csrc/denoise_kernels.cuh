@@ -26,12 +26,18 @@ struct ConvArgs {
     int n, h, wd;      // P = n * h * wd
 };
 
+enum ConvKernels {
+    kConvAuto = 0,       // tcgen05: strip kernel where the weights fit, else per-tile
+    kConvTiles = 1,      // tcgen05 per-tile kernels only
+    kConvPersistent = 2, // strip kernel on a grid of 16 CTAs (several segments each)
+};
+
 // out = act(conv3x3(in, w) + bias) (zero padding); with transformed weights
 // (w_t[ci][8 - tap][co]) and a mask the same kernel is the input gradient.
 // With `err` set (and cout <= 256) it runs on the tcgen05 tensor cores and
 // `err` receives a status bit if one of its waits timed out; with err null
 // it runs the warp-level mma.sync kernel.
-void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err);
+void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind = kConvAuto);
 
 // dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
 // dbias[co] += sum_p dout[p][co] (dbias may be null).

@@ -465,7 +465,7 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
 #define VVPT_TRACE_MIN_BLOCKS 4
 #endif
 #ifndef VVPT_SHADE_MIN_BLOCKS
-#define VVPT_SHADE_MIN_BLOCKS 1
+#define VVPT_SHADE_MIN_BLOCKS 2
 #endif
 __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {

@@ -31,9 +31,14 @@ class Denoiser:
         except Exception:
             pass
 
+    KERNELS = {"tcgen05": 0, "mma_sync": 1, "tcgen05_tiles": 2, "tcgen05_persistent": 3}
+
     def set_kernels(self, kind: str) -> None:
-        """'tcgen05' (default) or 'mma_sync' convolution kernels."""
-        self.ctx.check(self.ctx.lib.vvpt_denoiser_set_kernels(self.handle, {"tcgen05": 0, "mma_sync": 1}[kind]))
+        """Convolution kernels: 'tcgen05' (default: strip kernel where the
+        weights fit in shared memory, per-tile kernels elsewhere),
+        'mma_sync', 'tcgen05_tiles' (per-tile tcgen05 kernels only) or
+        'tcgen05_persistent' (strip kernel on a 16-CTA grid)."""
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_set_kernels(self.handle, self.KERNELS[kind]))
 
     def params(self) -> np.ndarray:
         out = np.zeros(self.num_params, dtype=np.float32)
