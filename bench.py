@@ -541,9 +541,10 @@ def denoiser_flops(h: int, w: int, n: int = 1) -> float:
 
 
 def run_denoise(args) -> None:
-    """Denoiser inference at 3840 x 2160 (one frame) and one training step on
-    8 crops of 256^2, CUDA events on the library stream; roofline against the
-    measured dense BF16 peak."""
+    """Denoiser inference at 3840 x 2160 (one frame; --width/--height for
+    another size, multiples of 16) and one training step on 8 crops of 256^2,
+    CUDA events on the library stream; roofline against the measured dense
+    BF16 peak."""
     import torch
 
     from vviewer_gb300 import Context
@@ -552,7 +553,9 @@ def run_denoise(args) -> None:
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     dn = Denoiser(ctx, seed=1)
-    H, W = 2160, 3840
+    H, W = (args.height or 2160), (args.width or 3840)
+    if H % 16 or W % 16:
+        raise SystemExit("denoise: width and height must be multiples of 16")
     g = torch.Generator(device="cuda").manual_seed(1)
     rad = torch.rand((H, W, 4), device="cuda", generator=g) * 4
     alb = torch.rand((H, W, 4), device="cuda", generator=g)
@@ -587,8 +590,10 @@ def run_denoise(args) -> None:
     line = {"metric": "denoised frames/s", "value": 1e3 / infer_ms, "unit": "frames/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": infer_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic inputs",
-            "config": {"workload": "denoise_3840x2160", "network": "U-Net 5 levels 32/48/64/96/128, 3x3",
-                       "train_batch": "8 x 256^2"},
+            "config": {"workload": f"denoise_{W}x{H}", "network": "U-Net 5 levels 32/48/64/96/128, 3x3",
+                       "train_batch": "8 x 256^2",
+                       "l2": "inputs (3 RGBA32F images, 133 MB each at 3840x2160) and every activation larger "
+                             "than L2"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None, "flops_per_frame": flops},
             "train_step_ms": train_ms, "train_tflops": 3 * denoiser_flops(256, 256, 8) / (train_ms / 1e3) / 1e12}

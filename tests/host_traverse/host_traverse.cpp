@@ -21,6 +21,19 @@ static inline double __dsub_rn(double a, double b) { return a - b; }
 static inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
 static inline unsigned __float_as_uint(float f) { unsigned i; std::memcpy(&i, &f, 4); return i; }
 static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline float __uint_as_float(unsigned i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
+static inline int __ffs(int x) { return x ? __builtin_ctz((unsigned)x) + 1 : 0; }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
+// byte i of the result = byte (s >> 4i) & 7 of the pair {y, x} (x bytes 0-3)
+static inline unsigned __byte_perm(unsigned x, unsigned y, unsigned s)
+{
+    const unsigned long long pool = ((unsigned long long)y << 32) | x;
+    unsigned r = 0;
+    for (int i = 0; i < 4; i++)
+        r |= (unsigned)((pool >> (8 * ((s >> (4 * i)) & 7u))) & 0xffu) << (8 * i);
+    return r;
+}
 template <class T>
 static inline T __ldg(const T *p) { return *p; }
 // one lane per "warp": the speculative-traversal vote sees only this ray
@@ -51,6 +64,7 @@ extern "C" int host_trace_closest(const vvpt_scene_desc *desc, const vvpt_ray *r
     }
     SceneView v{};
     v.nodes = pk.nodes.data();
+    v.wnodes = pk.wnodes.data();
     v.tris = pk.tris.data();
     v.verts = pk.verts.data();
     v.indices = pk.indices.data();

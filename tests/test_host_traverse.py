@@ -21,6 +21,10 @@ HARNESS = Path(__file__).resolve().parent / "host_traverse" / "host_traverse.cpp
 OUT = Path(__file__).resolve().parent / "_build" / "libhost_traverse.so"
 
 
+def _lib_path(wide):
+    return OUT.with_name(f"libhost_traverse_{'wide' if wide else 'binary'}.so")
+
+
 def _cuda_include():
     for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
         if cand and (Path(cand) / "include" / "vector_types.h").exists():
@@ -28,16 +32,21 @@ def _cuda_include():
     pytest.skip("CUDA headers (vector_types.h) not found")
 
 
-@pytest.fixture(scope="module")
-def host_lib():
-    srcs = [HARNESS, CSRC / "scene_pack.cpp", CSRC / "bvh_build.cpp"]
+@pytest.fixture(scope="module", params=[True, False], ids=["wide_blas", "binary_blas"])
+def host_lib(request):
+    """The harness built for both BLAS layouts: compressed 8-wide nodes (the
+    default) and binary nodes (VVPT_BLAS_WIDE=0)."""
+    wide = request.param
+    out = _lib_path(wide)
+    srcs = [HARNESS, CSRC / "scene_pack.cpp", CSRC / "bvh_build.cpp", CSRC / "bvh_wide.cpp"]
     deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "vvpt.h"]
-    if not OUT.exists() or OUT.stat().st_mtime < max(p.stat().st_mtime for p in deps):
-        OUT.parent.mkdir(exist_ok=True)
+    if not out.exists() or out.stat().st_mtime < max(p.stat().st_mtime for p in deps):
+        out.parent.mkdir(exist_ok=True)
         cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
-               "-I", _cuda_include(), "-I", str(ROOT / "include"), "-I", str(CSRC), *map(str, srcs), "-o", str(OUT)]
+               f"-DVVPT_BLAS_WIDE={int(wide)}", "-I", _cuda_include(), "-I", str(ROOT / "include"), "-I", str(CSRC),
+               *map(str, srcs), "-o", str(out)]
         subprocess.run(cmd, check=True, capture_output=True)
-    lib = C.CDLL(str(OUT))
+    lib = C.CDLL(str(out))
     lib.host_trace_closest.restype = C.c_int
     lib.host_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32),
                                        C.c_char_p, C.c_int]

@@ -42,20 +42,25 @@ def _newest_input() -> float:
     return max(f.stat().st_mtime for f in files if f.is_file())
 
 
-def _compile(src: Path, nvcc: str, extra: list[str]) -> Path:
+def _compile(src: Path, nvcc: str, extra: list[str], defines: list[str]) -> Path:
     obj = BUILD_DIR / (src.stem + src.suffix.replace(".", "_") + ".o")
+    dflags = [f"-D{d}" for d in defines]
     if src.suffix == ".cu":
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *dflags, *extra, "-c", str(src), "-o", str(obj)]
     else:
-        cmd = ["g++", *CXX_FLAGS, "-I", str(Path(nvcc).parent.parent / "include"), "-c", str(src), "-o", str(obj)]
+        cmd = ["g++", *CXX_FLAGS, *dflags, "-I", str(Path(nvcc).parent.parent / "include"), "-c", str(src), "-o",
+               str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     return obj
 
 
-def build(force: bool = False, verbose: bool = False, extra_nvcc: list[str] | None = None) -> Path:
-    """Compiles and links libvvpt.so if it is missing or stale; returns its path."""
+def build(force: bool = False, verbose: bool = False, extra_nvcc: list[str] | None = None,
+          defines: list[str] | None = None) -> Path:
+    """Compiles and links libvvpt.so if it is missing or stale; returns its path.
+    `defines` (NAME=VALUE) reach both compilers, e.g. VVPT_BLAS_WIDE=0 for the
+    binary BLAS layout; `extra_nvcc` only nvcc."""
     if LIB.exists() and not force and LIB.stat().st_mtime >= _newest_input():
         return LIB
     nvcc = _nvcc()
@@ -63,7 +68,7 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc: list[str] | No
     BUILD_DIR.mkdir(exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, extra_nvcc or []), srcs))
+        objs = list(ex.map(lambda s: _compile(s, nvcc, extra_nvcc or [], defines or []), srcs))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)

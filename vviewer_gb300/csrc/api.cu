@@ -306,6 +306,8 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     uint64_t bytes = 0;
     if ((st = upload(ctx, scene->nodes, pk.nodes, bytes)) != VVPT_OK)
         return st;
+    if ((st = upload(ctx, scene->wnodes, pk.wnodes, bytes)) != VVPT_OK)
+        return st;
     if ((st = upload(ctx, scene->tris, pk.tris, bytes)) != VVPT_OK)
         return st;
     if ((st = upload(ctx, scene->verts, pk.verts, bytes)) != VVPT_OK)
@@ -330,6 +332,7 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
 
     SceneView &v = scene->view;
     v.nodes = scene->nodes.as<BVHNode>();
+    v.wnodes = scene->wnodes.as<WideNode>();
     v.tris = scene->tris.as<TriVerts>();
     v.verts = scene->verts.as<ShadeVertex>();
     v.indices = scene->indices.as<uint32_t>();

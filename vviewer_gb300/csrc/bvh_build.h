@@ -40,6 +40,16 @@ struct BVHBuildResult {
 // input gives a root with two empty children).
 BVHBuildResult build_bvh2(const std::vector<Box3> &boxes, const BVHBuildOptions &opt = BVHBuildOptions());
 
+// Compressed 8-wide BVH collapsed from a binary one (bvh_wide.cpp): node 0 is
+// the root; `order` lists the primitives in the wide leaf order (each wide
+// node's leaf triangles contiguous from its tri_base).
+struct WideBuildResult {
+    std::vector<WideNode> nodes;
+    std::vector<uint32_t> order;
+    int depth = 0;
+};
+WideBuildResult collapse_to_wide(const BVHBuildResult &bin, const std::vector<Box3> &boxes);
+
 // The same BVH built on the GPU (bvh_gpu.cu), one tree level per round of
 // kernels on `stream`; node and order arrays come back to the host. Returns
 // false (err set, or err empty for trees the host builds trivially: at most

@@ -586,6 +586,17 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                 "%14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+}
+
 // Epilogue of one pixel row x 16 channels: bias, ReLU, mask, store (bf16, or
 // f32 for the output layer).
 __device__ __forceinline__ void store_row16(const ConvArgs &a, long p, int c, const uint32_t (&r)[16])
@@ -772,7 +783,7 @@ __host__ __device__ constexpr int tc_chunk_smem_bytes(int N, int nchunks)
     return (nchunks > 1 ? 2 : 1) * (kTcHaloAlloc + 9 * N * kTcBK * 2);
 }
 
-__global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols, uint32_t *err)
+__global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols, int nacc, uint32_t *err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_holder;
@@ -836,16 +847,19 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t h_addr = sbase + (c & 1) * stage_bytes, b_addr = h_addr + kTcHaloAlloc;
-            for (int tap = 0; tap < 9; tap++) {
-                const int dy = tap / 3, dx = tap % 3;
+            // tap t accumulates into accumulator t % nacc (independent chains)
 #pragma unroll
-                for (int j = 0; j < kTcBK / 16; j++) {
+            for (int j = 0; j < kTcBK / 16; j++) {
+#pragma unroll
+                for (int tap = 0; tap < 9; tap++) {
+                    const int dy = tap / 3, dx = tap % 3;
                     const uint64_t ad =
                         umma_desc(h_addr + dy * kTcHaloRow + dx * 16 + j * 2 * kTcHaloPx * 16, kTcHaloPx * 16, 128);
                     const uint64_t bd = umma_desc(b_addr + tap * tap_bytes + j * 2 * 128, 128, kTcKC * 128);
-                    const uint32_t accumulate = (c > 0 || tap > 0 || j > 0) ? 1u : 0u;
+                    const uint32_t accumulate = (c > 0 || j > 0 || tap >= nacc) ? 1u : 0u;
+                    const uint32_t dst = tmem + (uint32_t)((tap & (nacc - 1)) * N);
                     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dst),
                                  "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
                 }
             }
@@ -872,15 +886,17 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
     if (!abort_flag) {
         const int x = x0 + warp * 32 + lane;
         const long p = ((long)nb * a.h + y) * a.wd + x;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
         for (int c = 0; c < N; c += 16) {
             uint32_t r[16];
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                         "%12, %13, %14, %15}, [%16];"
-                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                           "=r"(r[14]), "=r"(r[15])
-                         : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            tmem_ld16(lane_base + (uint32_t)c, r);
+            for (int q = 1; q < nacc; q++) {
+                uint32_t t[16];
+                tmem_ld16(lane_base + (uint32_t)(q * N + c), t);
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
+            }
             if (x >= a.wd || c >= a.cout)
                 continue;
             store_row16(a, p, c, r);
@@ -926,7 +942,7 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 }
 
 __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap, int ncols,
-                                                        int ring, int segs, int seg_rows, uint32_t *err)
+                                                        int nacc, int ring, int segs, int seg_rows, uint32_t *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     __shared__ uint32_t tmem_holder;
@@ -1020,13 +1036,14 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
             const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(gi & 1) * half_cols;
             for (int c = 0; c < N; c += 16) {
                 uint32_t r[16];
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-                             "%11, %12, %13, %14, %15}, [%16];"
-                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-                               "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                             : "r"(acc + (uint32_t)c));
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                tmem_ld16(acc + (uint32_t)c, r);
+                for (int q = 1; q < nacc; q++) {
+                    uint32_t t[16];
+                    tmem_ld16(acc + (uint32_t)(q * N + c), t);
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
+                }
                 if (x < a.wd && c < a.cout)
                     store_row16(a, p, c, r);
             }
@@ -1055,20 +1072,28 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
                     abort_flag = 1;
                 } else {
                     asm volatile("tcgen05.fence::after_thread_sync;");
+                    // tap t accumulates into accumulator t % nacc: consecutive
+                    // MMAs go to different accumulators (independent chains)
                     const uint32_t acc = tmem + (uint32_t)(gi & 1) * half_cols;
+                    uint32_t slot_lo[3];
 #pragma unroll
-                    for (int tap = 0; tap < 9; tap++) {
-                        const int dy = tap / 3, dx = tap % 3;
+                    for (int dy = 0; dy < 3; dy++) {
                         int sl = row_slot + dy;
                         sl = sl >= ring ? sl - ring : sl;
-                        const uint32_t a_lo = a_lo_base + (uint32_t)sl * a_lo_slot + (uint32_t)dx;
-                        const uint32_t b_lo = b_lo_base + (uint32_t)tap * b_lo_tap;
-                        for (int j = 0; j < KC / 2; j++) {
-                            const uint64_t ad = a_hi | (uint64_t)(a_lo + (uint32_t)j * (2 * kStKCBytes / 16));
-                            const uint64_t bd = b_hi | (uint64_t)(b_lo + (uint32_t)j * (2 * 128 / 16));
-                            const uint32_t accumulate = (tap > 0 || j > 0) ? 1u : 0u;
+                        slot_lo[dy] = a_lo_base + (uint32_t)sl * a_lo_slot;
+                    }
+                    for (int j = 0; j < KC / 2; j++) {
+#pragma unroll
+                        for (int tap = 0; tap < 9; tap++) {
+                            const int dy = tap / 3, dx = tap % 3;
+                            const uint64_t ad =
+                                a_hi | (uint64_t)(slot_lo[dy] + (uint32_t)dx + (uint32_t)j * (2 * kStKCBytes / 16));
+                            const uint64_t bd =
+                                b_hi | (uint64_t)(b_lo_base + (uint32_t)tap * b_lo_tap + (uint32_t)j * (2 * 128 / 16));
+                            const uint32_t accumulate = (j > 0 || tap >= nacc) ? 1u : 0u;
+                            const uint32_t dst = acc + (uint32_t)((tap & (nacc - 1)) * N);
                             asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(acc),
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dst),
                                          "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
                         }
                     }
@@ -1153,7 +1178,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 }
 
 struct StripPlan {
-    int ring = 0, smem = 0, grid = 0, segs = 0, seg_rows = 0, ncols = 0;
+    int ring = 0, smem = 0, grid = 0, segs = 0, seg_rows = 0, ncols = 0, nacc = 1;
 };
 
 // Occupancy first (up to 4 CTAs per SM, bounded by shared memory and by the
@@ -1193,11 +1218,25 @@ bool plan_strip(const ConvArgs &a, StripPlan &pl)
         int segs = (int)std::max<long>(1, std::min<long>(a.h, ctas / std::max<long>(1, cols)));
         const int seg_rows = (a.h + segs - 1) / segs;
         segs = (a.h + seg_rows - 1) / seg_rows;
+        // accumulators per row: as many independent MMA chains (1, 2 or 4) as
+        // the SM's TMEM leaves room for at this occupancy
+        int nacc = 1, tcols = ncols;
+        for (int q = 4; q >= 2; q >>= 1) {
+            int cq = 32;
+            while (cq < 2 * q * N)
+                cq <<= 1;
+            if (c * cq <= 512) {
+                nacc = q;
+                tcols = cq;
+                break;
+            }
+        }
         pl.ring = ring;
         pl.smem = dyn;
         pl.segs = segs;
         pl.seg_rows = seg_rows;
-        pl.ncols = ncols;
+        pl.ncols = tcols;
+        pl.nacc = nacc;
         pl.grid = (int)std::min<long>(cols * segs, ctas);
         return true;
     }
@@ -1234,7 +1273,7 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
                                  cudaSharedmemCarveoutMaxShared);
             attr_smem = pl.smem;
         }
-        k_conv3x3_strip<<<pl.grid, 128, pl.smem, s>>>(a, tmap, pl.ncols, pl.ring, pl.segs, pl.seg_rows, err);
+        k_conv3x3_strip<<<pl.grid, 128, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs, pl.seg_rows, err);
         return;
     }
     if (err && a.cout <= 256) {
@@ -1250,9 +1289,23 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
         while (ncols < N)
             ncols <<= 1;
         const long tiles = (long)a.n * a.h * ((a.wd + kTcM - 1) / kTcM);
-        if (N <= 128)
-            k_conv3x3_tc_chunk<<<(unsigned)tiles, 128, tc_chunk_smem_bytes(N, (a.cin + kTcBK - 1) / kTcBK), s>>>(
-                a, ncols, err);
+        if (N <= 128) {
+            // as many accumulators as the TMEM left by co-resident CTAs allows
+            const int smem = tc_chunk_smem_bytes(N, (a.cin + kTcBK - 1) / kTcBK);
+            const int per_sm = std::max(1, 233472 / (smem + 2048));
+            int nacc = 1, cols = ncols;
+            for (int q = 4; q >= 2; q >>= 1) {
+                int cq = 32;
+                while (cq < q * N)
+                    cq <<= 1;
+                if (per_sm * cq <= 512) {
+                    nacc = q;
+                    cols = cq;
+                    break;
+                }
+            }
+            k_conv3x3_tc_chunk<<<(unsigned)tiles, 128, smem, s>>>(a, cols, nacc, err);
+        }
         else
             k_conv3x3_tc<<<(unsigned)tiles, 128, tc_smem_bytes(N), s>>>(a, ncols, err);
         return;

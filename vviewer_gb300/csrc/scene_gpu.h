@@ -27,12 +27,25 @@ struct alignas(16) BVHNode {
 };
 static_assert(sizeof(BVHNode) == 64, "BVHNode must be 64 bytes");
 
-// Compressed 8-wide node (80 bytes). Child boxes are quantised to 8 bits per
-// plane relative to the node origin p with per-axis power-of-two scales e.
-// imask bit i: child slot i is an internal node. Internal children are stored
-// contiguously from child_base; leaf children's triangles contiguously from
-// tri_base. meta[i]: 0 = empty slot; internal: 0b001xxxxx with xxxxx = 24 + slot
-// rank; leaf: (tri count as unary in the top 3 bits) | tri offset (5 bits).
+// Bottom-level acceleration structures use the binary nodes above
+// (VVPT_BLAS_WIDE = 0, the default) or compressed 8-wide nodes
+// (VVPT_BLAS_WIDE = 1, a build option). Both give the same closest hits; on
+// GB300 the binary layout traverses faster (the wide one visits 2.7x fewer
+// BLAS nodes per ray but spends more instructions per visit, and the
+// traversal kernels are issue-bound under divergence).
+#ifndef VVPT_BLAS_WIDE
+#define VVPT_BLAS_WIDE 0
+#endif
+
+// Compressed 8-wide node (80 bytes, five 128-bit loads). Child box planes are
+// p + q * 2^(e - 127) per axis with 8-bit q (qlo, qhi); p is a multiple of the
+// scale and every plane is exactly representable. imask bit i: slot i holds an
+// internal child; internal children are consecutive wide nodes from
+// child_base in slot order (index = child_base + number of internal slots
+// below i). meta[i] of a leaf slot: (triangle count 1..4) << 5 | offset
+// (0..31) of its first triangle from tri_base; 0 for empty and internal
+// slots. child_base and tri_base are relative to the BLAS's first wide node
+// and first triangle.
 struct alignas(16) WideNode {
     float px, py, pz;
     uint8_t ex, ey, ez, imask;
@@ -60,7 +73,7 @@ struct alignas(16) ShadeVertex {
 };
 
 struct MeshInfo {
-    uint32_t node_offset;   // first BVHNode of the BLAS
+    uint32_t node_offset;   // first node of the BLAS (WideNode or BVHNode)
     uint32_t tri_offset;    // first TriVerts (leaf order)
     uint32_t vertex_offset; // first ShadeVertex
     uint32_t index_offset;  // first index triple (in uint32 units / 3)
@@ -113,7 +126,8 @@ struct DevTexture {
 
 // Everything a kernel needs about the scene.
 struct SceneView {
-    const BVHNode *nodes;      // all BLAS nodes, then TLAS nodes
+    const BVHNode *nodes;      // all BLAS nodes (binary layout), then TLAS nodes
+    const WideNode *wnodes;    // all BLAS nodes (wide layout)
     const TriVerts *tris;
     const ShadeVertex *verts;
     const uint32_t *indices;   // 3 per triangle, original order

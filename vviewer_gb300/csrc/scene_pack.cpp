@@ -28,6 +28,7 @@ vvpt_status fail(std::string &err, vvpt_status code, const std::string &msg)
 
 struct MeshBuild {
     BVHBuildResult bvh;
+    WideBuildResult wide; // collapsed from bvh (VVPT_BLAS_WIDE)
     Box3 root{};
 };
 
@@ -243,6 +244,10 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
             }
             if (!built)
                 builds[m].bvh = build_bvh2(boxes, opt);
+#if VVPT_BLAS_WIDE
+            builds[m].wide = collapse_to_wide(builds[m].bvh, boxes);
+            builds[m].bvh.nodes = std::vector<BVHNode>();
+#endif
             Box3 r;
             for (int a = 0; a < 3; a++) {
                 r.lo[a] = INFINITY;
@@ -270,31 +275,45 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
 
     std::vector<MeshInfo> minfo(nm);
     std::vector<BVHNode> &nodes = out.nodes;
+    std::vector<WideNode> &wnodes = out.wnodes;
     std::vector<TriVerts> &tris = out.tris;
     std::vector<ShadeVertex> &verts = out.verts;
     std::vector<uint32_t> &indices = out.indices;
     size_t total_nodes = 0, total_tris = 0, total_verts = 0;
     for (uint32_t m = 0; m < nm; m++) {
-        total_nodes += builds[m].bvh.nodes.size();
+        total_nodes += builds[m].bvh.nodes.size() + builds[m].wide.nodes.size();
         total_tris += desc->meshes[m].num_triangles;
         total_verts += desc->meshes[m].num_vertices;
     }
+#if VVPT_BLAS_WIDE
+    wnodes.reserve(total_nodes);
+    nodes.reserve(2 * desc->num_instances + 2);
+#else
     nodes.reserve(total_nodes + 2 * desc->num_instances + 2);
+#endif
     tris.reserve(total_tris);
     verts.reserve(total_verts);
     indices.reserve(3 * total_tris);
     for (uint32_t m = 0; m < nm; m++) {
         const vvpt_mesh_desc &md = desc->meshes[m];
         MeshInfo &mi = minfo[m];
-        mi.node_offset = (uint32_t)nodes.size();
         mi.tri_offset = (uint32_t)tris.size();
         mi.vertex_offset = (uint32_t)verts.size();
         mi.index_offset = (uint32_t)indices.size();
         mi.num_triangles = md.num_triangles;
+#if VVPT_BLAS_WIDE
+        mi.node_offset = (uint32_t)wnodes.size();
+        mi.num_nodes = (uint32_t)builds[m].wide.nodes.size();
+        wnodes.insert(wnodes.end(), builds[m].wide.nodes.begin(), builds[m].wide.nodes.end());
+        const std::vector<uint32_t> &leaf_order = builds[m].wide.order;
+#else
+        mi.node_offset = (uint32_t)nodes.size();
         mi.num_nodes = (uint32_t)builds[m].bvh.nodes.size();
         nodes.insert(nodes.end(), builds[m].bvh.nodes.begin(), builds[m].bvh.nodes.end());
+        const std::vector<uint32_t> &leaf_order = builds[m].bvh.order;
+#endif
         for (uint32_t k = 0; k < md.num_triangles; k++) {
-            uint32_t prim = builds[m].bvh.order[k];
+            uint32_t prim = leaf_order[k];
             TriVerts tv;
             const float *p0 = md.vertices[md.indices[3 * prim + 0]].position;
             const float *p1 = md.vertices[md.indices[3 * prim + 1]].position;

@@ -16,7 +16,8 @@
 namespace vvpt {
 
 struct PackedScene {
-    std::vector<BVHNode> nodes;       // every BLAS, then the TLAS
+    std::vector<BVHNode> nodes;       // every binary BLAS, then the TLAS
+    std::vector<WideNode> wnodes;     // every wide BLAS (VVPT_BLAS_WIDE)
     std::vector<TriVerts> tris;       // leaf order per BLAS
     std::vector<ShadeVertex> verts;
     std::vector<uint32_t> indices;    // original triangle order

@@ -207,6 +207,87 @@ __device__ __forceinline__ float3 wt_xform_vector(const float4 *rows, const floa
     return r;
 }
 
+#if VVPT_BLAS_WIDE
+// Byte k of w as an exact float: 0x4B0000bb is the float 2^23 + bb.
+__device__ __forceinline__ float byte_as_float(uint32_t w, int k)
+{
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)k)), 8388608.0f);
+}
+
+// Ray against the 8 child boxes of a wide node (five 128-bit words `w`).
+// Per axis the node gives the slab distance of a plane q as one multiply-add,
+// q * A + B with A = scale * invd and B = (p - o) * invd, near and far planes
+// chosen by the sign of the inverse direction. That form rounds relative to
+// |B| + 255 |A| rather than to the distance itself (the two terms cancel near
+// the plane), so each axis carries its own margin, 8 ulps of |B| + 255 |A|
+// (several times the worst-case error of the four roundings), folded into B:
+// near distances move down and far ones up, and no child the ray touches is
+// missed (a zero direction component gives infinities or NaN there, and NaN
+// leaves that axis unconstrained). Outputs: the internal-child hits at bit
+// (slot ^ oct), the node's imask and child_base, and the hit leaf children's
+// triangles as a mask over tri_base + 0..31.
+__device__ __forceinline__ void wide_visit(const float4 (&w)[5], const float3 &o, const float3 &invd, uint32_t oct,
+                                           float tmin, float tmax, uint32_t &node_bits, uint32_t &imask,
+                                           uint32_t &child_base, uint32_t &tri_base, uint32_t &tri_bits)
+{
+    const uint32_t eim = __float_as_uint(w[0].w);
+    const float ax = __fmul_rn(__uint_as_float((eim & 0xffu) << 23), invd.x);
+    const float ay = __fmul_rn(__uint_as_float(((eim >> 8) & 0xffu) << 23), invd.y);
+    const float az = __fmul_rn(__uint_as_float(((eim >> 16) & 0xffu) << 23), invd.z);
+    const float bx = __fmul_rn(__fsub_rn(w[0].x, o.x), invd.x);
+    const float by = __fmul_rn(__fsub_rn(w[0].y, o.y), invd.y);
+    const float bz = __fmul_rn(__fsub_rn(w[0].z, o.z), invd.z);
+    const float kUlps = 8.0f * 5.9604645e-08f; // 8 x 2^-24
+    const float mx = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(ax), fabsf(bx)));
+    const float my = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(ay), fabsf(by)));
+    const float mz = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(az), fabsf(bz)));
+    const float bnx = __fsub_rn(bx, mx), bfx = __fadd_rn(bx, mx);
+    const float bny = __fsub_rn(by, my), bfy = __fadd_rn(by, my);
+    const float bnz = __fsub_rn(bz, mz), bfz = __fadd_rn(bz, mz);
+    imask = eim >> 24;
+    child_base = __float_as_uint(w[1].x);
+    tri_base = __float_as_uint(w[1].y);
+    const uint32_t meta[2] = {__float_as_uint(w[1].z), __float_as_uint(w[1].w)};
+    const bool nx = (oct & 1u) != 0, ny = (oct & 2u) != 0, nz = (oct & 4u) != 0;
+    // near / far plane words per axis: lo (w2.xy, w2.zw, w3.xy), hi (w3.zw, w4.xy, w4.zw)
+    const uint32_t nxw[2] = {__float_as_uint(nx ? w[3].z : w[2].x), __float_as_uint(nx ? w[3].w : w[2].y)};
+    const uint32_t fxw[2] = {__float_as_uint(nx ? w[2].x : w[3].z), __float_as_uint(nx ? w[2].y : w[3].w)};
+    const uint32_t nyw[2] = {__float_as_uint(ny ? w[4].x : w[2].z), __float_as_uint(ny ? w[4].y : w[2].w)};
+    const uint32_t fyw[2] = {__float_as_uint(ny ? w[2].z : w[4].x), __float_as_uint(ny ? w[2].w : w[4].y)};
+    const uint32_t nzw[2] = {__float_as_uint(nz ? w[4].z : w[3].x), __float_as_uint(nz ? w[4].w : w[3].y)};
+    const uint32_t fzw[2] = {__float_as_uint(nz ? w[3].x : w[4].z), __float_as_uint(nz ? w[3].y : w[4].w)};
+    node_bits = 0;
+    tri_bits = 0;
+#pragma unroll 2
+    for (int i = 0; i < 8; i++) {
+        const int h = i >> 2, k = i & 3;
+        const float tnx = __fmaf_rn(byte_as_float(nxw[h], k), ax, bnx);
+        const float tfx = __fmaf_rn(byte_as_float(fxw[h], k), ax, bfx);
+        const float tny = __fmaf_rn(byte_as_float(nyw[h], k), ay, bny);
+        const float tfy = __fmaf_rn(byte_as_float(fyw[h], k), ay, bfy);
+        const float tnz = __fmaf_rn(byte_as_float(nzw[h], k), az, bnz);
+        const float tfz = __fmaf_rn(byte_as_float(fzw[h], k), az, bfz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        if (tn <= tf) {
+            const uint32_t m = (meta[h] >> (8 * k)) & 0xffu;
+            if ((imask >> i) & 1u)
+                node_bits |= 1u << (i ^ (int)oct);
+            else if (m)
+                tri_bits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+        }
+    }
+}
+
+__device__ __forceinline__ void load_wide(const WideNode *nodes, uint32_t idx, float4 (&w)[5])
+{
+    const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+        w[k] = __ldg(p + k);
+}
+#endif
+
 // Top of the TLAS staged in shared memory: a traversal kernel fills it at its
 // start with the first kTlasCacheNodes nodes of one live scene (the scene of
 // its block's first queue entry; launched with kTlasCacheBytes of dynamic
@@ -263,7 +344,7 @@ __device__ __forceinline__ BVHNode load_node_cached(int idx)
 // the two levels in one loop keeps a warp's lanes in step: a lane inside an
 // instance never holds lanes that are still in the TLAS, as nested per-level
 // loops would. `err` receives status bits.
-constexpr int kTagNode = 0, kTagLeaf = 1, kTagInst = 2, kTagReturn = 3;
+constexpr int kTagNode = 0, kTagLeaf = 1, kTagInst = 2, kTagReturn = 3, kTagWide = 4;
 
 __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
                                            const Hit &after, uint32_t &err)
@@ -284,6 +365,12 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     bool in_blas = false;
     int node = 0;                 // inner node to visit (local index), -1 none
     int leaf_first = 0, leaf_count = 0; // triangles still to test (local indices)
+#if VVPT_BLAS_WIDE
+    // BLAS level: the group of wide children still to visit (hits at bit
+    // slot ^ oct, imask, first child) and the triangles still to test (mask
+    // over t_base + 0..31); oct = sign bits of the object-space direction
+    uint32_t w_base = 0, w_bits = 0, w_imask = 0, t_base = 0, t_bits = 0, oct = 0;
+#endif
     int2 stack[kTraversalStack];
     int sp = 0;
     // TLAS nodes below this index come from shared memory when the cache
@@ -296,6 +383,38 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             err |= kErrStackOverflow;
     };
     for (;;) {
+#if VVPT_BLAS_WIDE
+        if (t_bits) {
+            const int b = __ffs((int)t_bits) - 1;
+            t_bits &= t_bits - 1u;
+            const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + t_base + (uint32_t)b);
+            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            const uint32_t prim = __float_as_uint(p0.w);
+            float t, u, v;
+            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
+                is_after(t, inst_id, prim, after)) {
+                best.t = t;
+                best.u = u;
+                best.v = v;
+                best.inst = inst_id;
+                best.prim = prim;
+            }
+            continue;
+        }
+        if (w_bits) {
+            // nearest remaining child of the group (octant order)
+            const int b = __ffs((int)w_bits) - 1;
+            w_bits &= w_bits - 1u;
+            const uint32_t slot = (uint32_t)b ^ oct;
+            const uint32_t child = w_base + (uint32_t)__popc(w_imask & ((1u << slot) - 1u));
+            if (w_bits)
+                push((int)w_base, kTagWide, (int)((w_bits << 8) | w_imask));
+            float4 wn[5];
+            load_wide(s.wnodes, node_base + child, wn);
+            wide_visit(wn, co, cinvd, oct, box_tmin, cull_far(best.t, slack), w_bits, w_imask, w_base, t_base, t_bits);
+            continue;
+        }
+#endif
         if (leaf_count > 0) {
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
             const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
@@ -358,6 +477,12 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
         const int cnt = e.y & 0x0FFFFFFF;
         if (tag == kTagNode) {
             node = e.x;
+#if VVPT_BLAS_WIDE
+        } else if (tag == kTagWide) {
+            w_base = (uint32_t)e.x;
+            w_bits = ((uint32_t)cnt >> 8) & 0xffu;
+            w_imask = (uint32_t)cnt & 0xffu;
+#endif
         } else if (tag == kTagLeaf) {
             leaf_first = e.x;
             leaf_count = cnt;
@@ -375,7 +500,16 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             tri_base = inst.tri_offset;
             in_blas = true;
             push(0, kTagReturn, 0);
+#if VVPT_BLAS_WIDE
+            // the BLAS root as a one-child group
+            oct = (__float_as_uint(cd.x) >> 31) | ((__float_as_uint(cd.y) >> 31) << 1) |
+                  ((__float_as_uint(cd.z) >> 31) << 2);
+            w_base = 0;
+            w_imask = 1u;
+            w_bits = 1u << oct;
+#else
             node = 0;
+#endif
         } else {
             // back to the TLAS
             co = o;
