@@ -218,8 +218,35 @@ enum {
      * last event contributes nothing (the reference never adds environment
      * light from the last event either), so the expected image is the
      * reference estimator's; the variance under bright skies is far lower. */
-    VVPT_RENDER_ENV_IS = 4u
+    VVPT_RENDER_ENV_IS = 4u,
+    /* The reference's low-discrepancy sampler (shaders/include/rng/
+     * rng_pmj.glsl, selected there by SAMPLING_PMJ in pt/defines_pt.glsl:3)
+     * instead of the RTGEMS xorshift stream: 2D draws (pixel jitter, lens,
+     * BSDF/phase directions, triangle points) from 16 progressive
+     * multi-jittered (0,2) sequences, 1D draws from a hashed permutation of
+     * the sample index plus a blue-noise offset; per-sample dimension start
+     * pixel.y * width + pixel.y and sample index batch * batch_size + s as
+     * in raygen.rgen.glsl:57-61. Tables: vvpt_sampler_tables. */
+    VVPT_RENDER_SAMPLER_PMJ = 8u
 };
+
+/* Sizes of the low-discrepancy sampler's tables
+ * (shaders/include/rng/rng_pmj_defines.glsl, bluenoise_defines.glsl). */
+enum {
+    VVPT_PMJ_SEQUENCES = 16,
+    VVPT_PMJ_SAMPLES = 16384,
+    VVPT_BLUE_NOISE_TEXTURES = 48,
+    VVPT_BLUE_NOISE_RES = 128
+};
+
+/* Copies the sampler's tables (generated once per process, deterministic):
+ * pmj [VVPT_PMJ_SEQUENCES][VVPT_PMJ_SAMPLES][2] and blue_noise
+ * [VVPT_BLUE_NOISE_TEXTURES][x][y], floats in [0, 1). Either pointer may be
+ * NULL. The reference ships these as data (math/PMJSequences.hpp,
+ * math/BlueNoise.hpp, uploaded by vulkan/resources/VulkanRandom.cpp); here
+ * they are regenerated: (0,2) sequences as Owen-scrambled Sobol points,
+ * blue noise by void-and-cluster. */
+VVPT_API vvpt_status vvpt_sampler_tables(float *pmj, float *blue_noise);
 
 /* Output images, RGBA32F row-major W*H*4 floats each, A = 1 (the three
  * storage images of raygen.rgen.glsl:131-144). Any pointer may be NULL.

@@ -36,20 +36,42 @@ def load():
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_trace_closest.restype = C.c_int
         lib.oracle_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+        lib.oracle_set_sampler_tables.restype = None
+        lib.oracle_set_sampler_tables.argtypes = [C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
 
+_tables = None
+
+
+def _sampler_tables(lib):
+    """The PMJ sampler's tables, the same data the library renders with
+    (vvpt_sampler_tables), handed to the oracle once and kept alive here."""
+    global _tables
+    if _tables is None:
+        from vviewer_gb300.renderer import sampler_tables
+        _tables = sampler_tables()
+        lib.oracle_set_sampler_tables(_tables[0].ctypes.data, _tables[1].ctypes.data)
+    return _tables
+
+
 def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threads: int = 0, fp64: bool = False,
-           env_is: bool = False):
+           env_is: bool = False, sampler: str = "rtgems"):
     """Renders with the oracle. Returns dict of H x W x 4 float32 arrays
-    (radiance, albedo, normal, radiance_m2); pixels not in `pixels` stay 0."""
+    (radiance, albedo, normal, radiance_m2); pixels not in `pixels` stay 0.
+    sampler: 'rtgems' or 'pmj' (VVPT_RENDER_SAMPLER_PMJ)."""
     from vviewer_gb300 import _native as N
 
     lib = load()
     desc = flat_scene.desc()
-    ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height,
-                      N.RENDER_ENV_IS if env_is else 0)
+    flags = N.RENDER_ENV_IS if env_is else 0
+    if sampler == "pmj":
+        _sampler_tables(lib)
+        flags |= N.RENDER_SAMPLER_PMJ
+    elif sampler != "rtgems":
+        raise ValueError("sampler must be 'rtgems' or 'pmj'")
+    ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
     H, W = info.height, info.width
     out = {k: np.zeros((H, W, 4), dtype=np.float32) for k in ("radiance", "albedo", "normal", "radiance_m2")}
     px = None

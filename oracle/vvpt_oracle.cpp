@@ -899,6 +899,7 @@ struct Params {
     int camVolume;
     uint32_t W, H, batchSize, batches, depth, totalSamples, totalLights;
     uint32_t envLight = 0; // the environment is one more light of the pick
+    uint32_t sampler = 0;  // 0: RTGEMS, 1: PMJ (VVPT_RENDER_SAMPLER_PMJ)
 };
 
 // RayPayloadPrimary, shaders/pt/structs_pt.glsl:4-30
@@ -910,11 +911,95 @@ struct Payload {
     bool stop, insideVolume;
     float vtmin;
     uint32_t volumeMaterialIndex;
-    uint32_t rngState;
+    uint32_t rngState;      // RTGEMS state; the dimension under the PMJ sampler
     bool sampled = false;   // direction drawn by BSDF/phase sampling (env MIS)
     float samplePdf = 0.0f;
+    // PMJ sampler (structs_pt.glsl:24-29)
+    uint32_t pmj = 0;
+    uint32_t pixelX = 0, pixelY = 0, sampleIndex = 0, samplesPerPixel = 0;
 };
-inline float rand1D(Payload &p) { return uintToFloat(xorshift(p.rngState)); }
+
+// ---- PMJ sampler, shaders/include/rng/rng_pmj.glsl:20-107, over the tables
+// set by oracle_set_sampler_tables ([16][16384][2], [48][128][128])
+const float *g_pmj = nullptr, *g_blue_noise = nullptr;
+constexpr uint32_t kPmjSeed = 2873468793u; // rng_pmj_defines.glsl
+constexpr float kOneMinusEps = 0.999999f;  // constants.glsl:2
+
+uint64_t mixBits(uint64_t v) // rng_pmj.glsl:28-35
+{
+    v ^= (v >> 31);
+    v *= 9202493588570546565ULL;
+    v ^= (v >> 27);
+    v *= 9357036318526133325ULL;
+    v ^= (v >> 33);
+    return v;
+}
+
+uint32_t permutationElement(uint32_t i, uint32_t l, uint32_t p) // rng_pmj.glsl:37-64
+{
+    uint32_t w = l - 1;
+    w |= w >> 1;
+    w |= w >> 2;
+    w |= w >> 4;
+    w |= w >> 8;
+    w |= w >> 16;
+    do {
+        i ^= p;
+        i *= 0xe170893du;
+        i ^= p >> 16;
+        i ^= (i & w) >> 4;
+        i ^= p >> 8;
+        i *= 0x0929eb3fu;
+        i ^= p >> 23;
+        i ^= (i & w) >> 1;
+        i *= 1u | p >> 27;
+        i *= 0x6935fa69u;
+        i ^= (i & w) >> 11;
+        i *= 0x74dcb303u;
+        i ^= (i & w) >> 2;
+        i *= 0x9e501cc3u;
+        i ^= (i & w) >> 2;
+        i *= 0xc860a3dfu;
+        i &= w;
+        i ^= i >> 5;
+    } while (i >= l);
+    return (i + p) % l;
+}
+
+uint32_t pmjHash(const Payload &pl)
+{
+    return (uint32_t)mixBits(((uint64_t)pl.pixelX << 48) ^ ((uint64_t)pl.pixelY << 32) ^
+                             ((uint64_t)pl.rngState << 16) ^ (uint64_t)kPmjSeed);
+}
+
+inline float rand1D(Payload &p)
+{
+    if (!p.pmj)
+        return uintToFloat(xorshift(p.rngState));
+    // rng_pmj.glsl:66-78
+    uint32_t index = permutationElement(p.sampleIndex, p.samplesPerPixel, pmjHash(p));
+    float delta = g_blue_noise[((size_t)(p.rngState % 48u) * 128u + p.pixelX % 128u) * 128u + p.pixelY % 128u];
+    p.rngState++;
+    return std::min(((float)index + delta) / (float)p.samplesPerPixel, kOneMinusEps);
+}
+
+// rand2D: rng_def.glsl (two rand1D draws) or rng_pmj.glsl:80-107
+inline void rand2D(Payload &p, float &u0, float &u1)
+{
+    if (!p.pmj) {
+        u0 = rand1D(p);
+        u1 = rand1D(p);
+        return;
+    }
+    uint32_t index = p.sampleIndex;
+    const uint32_t inst = p.rngState / 2;
+    if (inst >= 16)
+        index = permutationElement(p.sampleIndex, p.samplesPerPixel, pmjHash(p));
+    const float *u = g_pmj + ((size_t)(inst % 16u) * 16384u + index % 16384u) * 2;
+    p.rngState += 2;
+    u0 = std::min(u[0], kOneMinusEps);
+    u1 = std::min(u[1], kOneMinusEps);
+}
 
 struct HitInfo { // process_hit.glsl + construct_frame.glsl
     const vvpt_material *material;
@@ -1099,8 +1184,8 @@ LSR sampleLight(const Ctx &c, Payload &pl, V3 originPosition, bool allowEnv)
         lsr.isDeltaLight = false;
         if (!allowEnv)
             return lsr;
-        float uRow = rand1D(pl);
-        float uCol = rand1D(pl);
+        float uRow, uCol;
+        rand2D(pl, uRow, uCol);
         float epdf;
         lsr.direction = envSampleDir(c.s, uRow, uCol, epdf);
         tmax = c.p.zfar;
@@ -1145,8 +1230,8 @@ LSR sampleLight(const Ctx &c, Payload &pl, V3 originPosition, bool allowEnv)
             randomTriangle = ntri - 1;
         const uint32_t *ix = m.idx + 3 * randomTriangle;
         float trianglePdf = 1.0f / (float)ntri;
-        float r0 = rand1D(pl);
-        float r1 = rand1D(pl);
+        float r0, r1;
+        rand2D(pl, r0, r1);
         float bx, by;
         uniformSampleTriangle(r0, r1, bx, by);
         float bz = 1.0f - bx - by;
@@ -1366,8 +1451,8 @@ bool processVolumeHit(const Ctx &c, Payload &pl, uint32_t vol, float vtstart, fl
             }
         }
         V3 sdir;
-        float r0 = rand1D(pl);
-        float r1 = rand1D(pl);
+        float r0, r1;
+        rand2D(pl, r0, r1);
         float spdf = HG_Sample(wo, sdir, r0, r1, g);
         pl.origin = scatteringPosition;
         pl.direction = sdir;
@@ -1457,15 +1542,15 @@ void closestHit(const Ctx &c, Payload &pl, const Hit &h, V3 rayDir)
         float sampleDirectionPDF;
         V3 sdl;
         if (lambert) {
-            float r0 = rand1D(pl);
-            float r1 = rand1D(pl);
+            float r0, r1;
+            rand2D(pl, r0, r1);
             sdl = cosineSampleHemisphere(r0, r1, sampleDirectionPDF);
             pl.origin = hi.worldPosition;
             pl.direction = localToWorld(hi.frame, sdl);
             pl.beta = pl.beta * albedo;
         } else {
-            float r0 = rand1D(pl);
-            float r1 = rand1D(pl);
+            float r0, r1;
+            rand2D(pl, r0, r1);
             float r2 = rand1D(pl);
             V3 F = samplePBRStandard(sdl, wo, sampleDirectionPDF, pbr, r0, r1, r2);
             pl.origin = hi.worldPosition;
@@ -1542,13 +1627,23 @@ void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, A
     const Params &p = c.p;
     Payload pl{};
     pl.rngState = initRNG(px, py, p.W, batchIndex);
+    // PMJ sampler state, raygen.rgen.glsl:32-43
+    pl.pmj = p.sampler;
+    pl.samplesPerPixel = p.totalSamples;
+    pl.pixelX = px;
+    pl.pixelY = py;
     float lensRadius = p.lensRadius, focalDistance = p.focalDistance;
     bool insideVolume = p.camVolume != -1;
     for (int k = 0; k < 3; k++)
         cum[k] = Acc{0, 0, 0};
     for (uint32_t s = 0; s < p.batchSize; s++) {
-        float ox = rand1D(pl);
-        float oy = rand1D(pl);
+        if (pl.pmj) {
+            // raygen.rgen.glsl:57-61 (dimension start y * width + y, as written there)
+            pl.rngState = py * p.W + py;
+            pl.sampleIndex = batchIndex * p.batchSize + s;
+        }
+        float ox, oy;
+        rand2D(pl, ox, oy);
         float ux = ((float)px + ox) / (float)p.W, uy = ((float)py + oy) / (float)p.H;
         float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
         float target[4];
@@ -1556,8 +1651,8 @@ void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, A
         V3 dcam = normalize(v3(target[0], target[1], target[2]));
         V3 ocam = v3s(0.0f);
         if (lensRadius > 0) {
-            float lx = rand1D(pl);
-            float ly = rand1D(pl);
+            float lx, ly;
+            rand2D(pl, lx, ly);
             float cx, cy;
             concentricSampleDisk(lx, ly, cx, cy);
             float lox = lensRadius * cx, loy = lensRadius * cy;
@@ -1739,6 +1834,7 @@ void make_params(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const v
     p.depth = ri->depth;
     p.totalSamples = p.batchSize * p.batches;
     p.totalLights = desc->num_lights;
+    p.sampler = (ri->flags & VVPT_RENDER_SAMPLER_PMJ) ? 1u : 0u;
 }
 
 void set_env_light(const Scene &s, const vvpt_render_info *ri, Params &p)
@@ -1750,6 +1846,14 @@ void set_env_light(const Scene &s, const vvpt_render_info *ri, Params &p)
 }  // namespace
 
 extern "C" {
+
+// Tables of the PMJ sampler (VVPT_RENDER_SAMPLER_PMJ): [16][16384][2] and
+// [48][128][128] floats, kept by the caller while it renders.
+void oracle_set_sampler_tables(const float *pmj, const float *blue_noise)
+{
+    g_pmj = pmj;
+    g_blue_noise = blue_noise;
+}
 
 // Renders the listed pixels (all pixels when pixels == NULL) over every batch.
 // Outputs are W*H*4 floats (RGBA, A = 1); pixels not listed are left untouched.
@@ -1766,6 +1870,8 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
     Params p;
     make_params(desc, sd, ri, p);
     set_env_light(s, ri, p);
+    if (p.sampler && (!g_pmj || !g_blue_noise))
+        return 3;
     const Ctx c{s, p};
     const uint32_t npix = pixels ? num_pixels : p.W * p.H;
     if (threads <= 0)

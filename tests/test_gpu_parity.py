@@ -75,13 +75,13 @@ def compare_renders(a, b, m2a, batches):
     return rel_mean, close.mean(), outliers.mean()
 
 
-def render_pair(ctx, engine, info, env_is=False, **kw):
+def render_pair(ctx, engine, info, env_is=False, sampler="rtgems", **kw):
     fs = engine.scene.build()
     sd = engine.scene.scene_data(info.width, info.height)
     g = ctx.upload(fs)
-    res = g.render(sd, info, want_m2=True, env_is=env_is)
+    res = g.render(sd, info, want_m2=True, env_is=env_is, sampler=sampler)
     g.release()
-    ref = oracle.render(fs, sd, info, env_is=env_is, **kw)
+    ref = oracle.render(fs, sd, info, env_is=env_is, sampler=sampler, **kw)
     return res, ref
 
 
@@ -140,6 +140,23 @@ def test_environment_importance_sampling_matches_oracle(ctx, mode):
     e.scene.environment_type = mode
     e.scene.background_color = [0.2, 0.3, 0.4]
     res, ref = render_pair(ctx, e, info, env_is=True)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+
+
+@pytest.mark.parametrize("scene", ["cornell", "medium_thin_lens"])
+def test_pmj_sampler_matches_oracle(ctx, scene):
+    """The low-discrepancy sampler (VVPT_RENDER_SAMPLER_PMJ) against the
+    oracle's restatement of rng_pmj.glsl over the same tables: pixel jitter,
+    lens, light and BSDF/phase draws from the (0,2) sequences or the hashed
+    permutation plus blue noise, per-sample dimension restart."""
+    if scene == "cornell":
+        e, info = scenes.cornell_box(1, 96, 64, 32, 8, 4)
+    else:
+        e, info = scenes.cornell_medium(2, 64, 48, 32, 8, 4, freq=12, spheres=2)
+        e.scene.camera.lens_radius = 0.02
+        e.scene.camera.focal_distance = 2.0
+    res, ref = render_pair(ctx, e, info, sampler="pmj")
     rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
     assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
 

@@ -31,6 +31,11 @@ TEXTURE_RGBA8_SRGB = 1
 TEXTURE_RGBA32F = 2
 RENDER_WANT_BATCH_M2 = 1
 RENDER_ENV_IS = 4
+RENDER_SAMPLER_PMJ = 8
+PMJ_SEQUENCES = 16
+PMJ_SAMPLES = 16384
+BLUE_NOISE_TEXTURES = 48
+BLUE_NOISE_RES = 128
 
 
 class VvptError(RuntimeError):
@@ -192,6 +197,7 @@ _SIGNATURES = {
                                       C.c_uint32]),
     "vvpt_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(SceneData),
                                     C.POINTER(RenderInfo), C.POINTER(Outputs)]),
+    "vvpt_sampler_tables": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

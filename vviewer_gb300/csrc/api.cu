@@ -15,6 +15,7 @@
 #include "../../include/vvpt.h"
 #include "internal.h"
 #include "bvh_build.h"
+#include "sampler_tables.h"
 #include "scene_pack.h"
 #include "scene_gpu.h"
 #include "traverse.cuh"
@@ -65,6 +66,23 @@ vvpt_status make_render_params(vvpt_ctx *ctx, const vvpt_scene *scene, const vvp
     hp.env_light = ((info->flags & VVPT_RENDER_ENV_IS) && scene->view.env_func_int > 0.0f && (mode == 1 || mode == 2))
                        ? 1u
                        : 0u;
+    if (info->flags & VVPT_RENDER_SAMPLER_PMJ) {
+        std::lock_guard<std::mutex> lk(ctx->sampler_mu);
+        if (!ctx->pmj_table.ptr) {
+            const SamplerTables &t = sampler_tables();
+            cudaSetDevice(ctx->device);
+            VV_CUDA(ctx->pmj_table.alloc(t.pmj.size() * sizeof(float)), "cudaMalloc sampler tables");
+            VV_CUDA(ctx->blue_noise_table.alloc(t.blue_noise.size() * sizeof(float)), "cudaMalloc sampler tables");
+            VV_CUDA(cudaMemcpy(ctx->pmj_table.ptr, t.pmj.data(), t.pmj.size() * sizeof(float), cudaMemcpyHostToDevice),
+                    "upload sampler tables");
+            VV_CUDA(cudaMemcpy(ctx->blue_noise_table.ptr, t.blue_noise.data(), t.blue_noise.size() * sizeof(float),
+                               cudaMemcpyHostToDevice),
+                    "upload sampler tables");
+        }
+        hp.sampler = 1u;
+        hp.pmj = ctx->pmj_table.as<float>();
+        hp.blue_noise = ctx->blue_noise_table.as<float>();
+    }
     return VVPT_OK;
 }
 
@@ -870,6 +888,8 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
         return fail(ctx, VVPT_ERR_INVALID_ARG, "null argument");
     if (!out->on_device)
         return fail(ctx, VVPT_ERR_INVALID_ARG, "vvpt_render_noalloc writes device buffers only (outputs.on_device = 1)");
+    if (info->flags & VVPT_RENDER_SAMPLER_PMJ)
+        return fail(ctx, VVPT_ERR_UNSUPPORTED, "vvpt_render_noalloc renders with the RTGEMS sampler only");
     if (info->width == 0 || info->height == 0 || info->batch_size == 0)
         return fail(ctx, VVPT_ERR_INVALID_ARG, "width, height and batch_size must be positive");
     const uint64_t npix64 = (uint64_t)info->width * info->height;
@@ -1020,3 +1040,13 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
 }
 
 }  // extern "C"
+
+VVPT_API vvpt_status vvpt_sampler_tables(float *pmj, float *blue_noise)
+{
+    const SamplerTables &t = sampler_tables();
+    if (pmj)
+        std::memcpy(pmj, t.pmj.data(), t.pmj.size() * sizeof(float));
+    if (blue_noise)
+        std::memcpy(blue_noise, t.blue_noise.data(), t.blue_noise.size() * sizeof(float));
+    return VVPT_OK;
+}

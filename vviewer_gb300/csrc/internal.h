@@ -88,6 +88,9 @@ struct vvpt_ctx {
     vvpt::Engine *engine = nullptr;
     uint64_t budget_bytes = 0; // 0: no limit beyond the device's memory
     int bvh_builder = 0;       // VVPT_BVH_BUILDER_*
+    // low-discrepancy sampler tables (VVPT_RENDER_SAMPLER_PMJ), uploaded on first use
+    std::mutex sampler_mu;
+    vvpt::DevBuf pmj_table, blue_noise_table;
     std::chrono::steady_clock::time_point created = std::chrono::steady_clock::now();
 };
 

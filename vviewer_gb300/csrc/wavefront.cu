@@ -123,6 +123,115 @@ __device__ __forceinline__ float material_alpha(const SceneView &s, const DevMat
 // Light sampling (shaders/pt/lightSampling.glsl:1-106), without the shadow
 // trace, which `connect` performs.
 
+// ---- Sampler. RTGEMS (default): the xorshift stream of
+// shaders/include/rng/rng_def.glsl:4-36, rand2D = two rand1D draws.
+// PMJ (VVPT_RENDER_SAMPLER_PMJ): shaders/include/rng/rng_pmj.glsl:20-107,
+// whose state is the pixel, the sample index and a dimension counter.
+struct PathRng {
+    uint32_t s;     // RTGEMS xorshift state, or the PMJ dimension
+    uint32_t pix;   // PMJ: pixel x | y << 16
+    uint32_t index; // PMJ: sample index within the pixel
+};
+
+// 64-bit finaliser, rng_pmj.glsl:28-35
+__device__ __forceinline__ uint64_t pmj_mix_bits(uint64_t v)
+{
+    v ^= v >> 31;
+    v *= 9202493588570546565ull;
+    v ^= v >> 27;
+    v *= 9357036318526133325ull;
+    v ^= v >> 33;
+    return v;
+}
+
+// Element i of a pseudo-random permutation of [0, l) keyed by p (cycle
+// walking over the next power of two), rng_pmj.glsl:37-64. The walk ends
+// within a few steps; the cap only guards the loop.
+__device__ __forceinline__ uint32_t pmj_permutation_element(uint32_t i, uint32_t l, uint32_t p)
+{
+    uint32_t w = l - 1;
+    w |= w >> 1;
+    w |= w >> 2;
+    w |= w >> 4;
+    w |= w >> 8;
+    w |= w >> 16;
+    for (int it = 0; it < 1024; it++) {
+        i ^= p;
+        i *= 0xe170893du;
+        i ^= p >> 16;
+        i ^= (i & w) >> 4;
+        i ^= p >> 8;
+        i *= 0x0929eb3fu;
+        i ^= p >> 23;
+        i ^= (i & w) >> 1;
+        i *= 1u | p >> 27;
+        i *= 0x6935fa69u;
+        i ^= (i & w) >> 11;
+        i *= 0x74dcb303u;
+        i ^= (i & w) >> 2;
+        i *= 0x9e501cc3u;
+        i ^= (i & w) >> 2;
+        i *= 0xc860a3dfu;
+        i &= w;
+        i ^= i >> 5;
+        if (i < l)
+            break;
+    }
+    return (i + p) % l;
+}
+
+constexpr uint32_t kPmjSeed = 2873468793u;
+constexpr float kOneMinusEpsilon = 0.999999f; // ONEMINUSEPSILON, shaders/include/constants.glsl:2
+
+__device__ __forceinline__ uint32_t pmj_hash(const PathRng &r)
+{
+    const uint64_t px = r.pix & 0xFFFFu, py = r.pix >> 16;
+    return (uint32_t)pmj_mix_bits((px << 48) ^ (py << 32) ^ ((uint64_t)r.s << 16) ^ (uint64_t)kPmjSeed);
+}
+
+__device__ __forceinline__ float rnd1(const RenderParams &p, PathRng &r)
+{
+    if (!p.sampler)
+        return rand1(r.s);
+    const uint32_t index = pmj_permutation_element(r.index, p.total_samples, pmj_hash(r));
+    const uint32_t px = (r.pix & 0xFFFFu) % 128u, py = (r.pix >> 16) % 128u;
+    const float delta = __ldg(p.blue_noise + ((size_t)(r.s % 48u) * 128u + px) * 128u + py);
+    r.s++;
+    return fminf(__fdiv_rn(__fadd_rn((float)index, delta), (float)p.total_samples), kOneMinusEpsilon);
+}
+
+__device__ __forceinline__ float2 rnd2(const RenderParams &p, PathRng &r)
+{
+    if (!p.sampler) {
+        const float a = rand1(r.s);
+        const float b = rand1(r.s);
+        return make_float2(a, b);
+    }
+    uint32_t index = r.index;
+    const uint32_t inst = r.s / 2u;
+    if (inst >= 16u)
+        index = pmj_permutation_element(r.index, p.total_samples, pmj_hash(r));
+    const float2 u = __ldg(reinterpret_cast<const float2 *>(p.pmj) + (size_t)(inst % 16u) * 16384u + index % 16384u);
+    r.s += 2u;
+    return make_float2(fminf(u.x, kOneMinusEpsilon), fminf(u.y, kOneMinusEpsilon));
+}
+
+// The path's sampler state as the shade kernels use it.
+__device__ __forceinline__ PathRng load_rng(const RenderParams &p, const PathState &ps, uint32_t slot)
+{
+    PathRng r;
+    r.s = ps.rng[slot];
+    r.pix = 0;
+    r.index = 0;
+    if (p.sampler) {
+        const uint32_t npix = p.width * p.height, item = ps.item[slot];
+        const uint32_t batch = item / npix, pix = item - batch * npix;
+        r.pix = (pix % p.width) | ((pix / p.width) << 16);
+        r.index = batch * p.batch_size + ps.sample[slot];
+    }
+    return r;
+}
+
 struct LightSample {
     float3 dir;
     float3 radiance;
@@ -136,7 +245,7 @@ struct LightSample {
 // that pick contribute nothing (the last event of a path, whose environment
 // contribution the reference's estimator never adds either).
 __device__ __forceinline__ LightSample sample_light(const SceneView &s, const RenderParams &p, const float3 &origin,
-                                                    uint32_t &rng, bool allow_env)
+                                                    PathRng &rng, bool allow_env)
 {
     LightSample ls;
     ls.delta = true;
@@ -148,15 +257,15 @@ __device__ __forceinline__ LightSample sample_light(const SceneView &s, const Re
     if (total == 0)
         return ls;
     float pdf = 1.0f / (float)total;
-    uint32_t li = (uint32_t)(rand1(rng) * (float)total);
+    uint32_t li = (uint32_t)(rnd1(p, rng) * (float)total);
     if (li >= total)
         li = total - 1;
     if (li == p.num_lights) {
         ls.delta = false;
         if (!allow_env)
             return ls;
-        const float u_row = rand1(rng);
-        const float u_col = rand1(rng);
+        const float2 uv = rnd2(p, rng);
+        const float u_row = uv.x, u_col = uv.y;
         float epdf;
         ls.dir = sample_env(s, u_row, u_col, epdf);
         ls.tmax = p.zfar;
@@ -188,13 +297,12 @@ __device__ __forceinline__ LightSample sample_light(const SceneView &s, const Re
         const uint32_t mesh_inst = L.info[1];
         const DevInstance &inst = s.instances[mesh_inst];
         const DevMaterial &m = s.materials[inst.material];
-        uint32_t tri = (uint32_t)(rand1(rng) * (float)inst.num_triangles);
+        uint32_t tri = (uint32_t)(rnd1(p, rng) * (float)inst.num_triangles);
         if (tri >= inst.num_triangles)
             tri = inst.num_triangles - 1;
         float tri_pdf = 1.0f / (float)inst.num_triangles;
-        float u0 = rand1(rng);
-        float u1 = rand1(rng);
-        float2 bc = uniform_sample_triangle(u0, u1);
+        const float2 uu = rnd2(p, rng);
+        float2 bc = uniform_sample_triangle(uu.x, uu.y);
         float b0 = bc.x, b1 = bc.y, b2 = 1.0f - bc.x - bc.y;
         ShadeVertex a, b, c;
         fetch_triangle(s, inst, tri, a, b, c);
@@ -387,19 +495,23 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
         const uint32_t batch = item / npix;
         const uint32_t pix = item - batch * npix;
         const uint32_t px = pix % p.width, py = pix / p.width;
-        uint32_t rng;
+        PathRng rng;
         float3 alb, nrm;
         if (fresh) {
-            rng = init_rng(px, py, p.width, batch);
+            rng.s = init_rng(px, py, p.width, batch);
             alb = nrm = f3(0.0f);
         } else {
-            rng = ps.rng[slot];
+            rng.s = ps.rng[slot];
             alb = f3(ps.alb[slot]);
             nrm = f3(ps.nrm[slot]);
         }
+        rng.pix = px | (py << 16);
+        rng.index = batch * p.batch_size + sample;
+        if (p.sampler)
+            rng.s = py * p.width + py; // dimension start of every sample, raygen.rgen.glsl:57-60
         // camera ray, raygen.rgen.glsl:63-91
-        float ox = rand1(rng);
-        float oy = rand1(rng);
+        const float2 oxy = rnd2(p, rng);
+        const float ox = oxy.x, oy = oxy.y;
         float uvx = ((float)px + ox) / (float)p.width;
         float uvy = ((float)py + oy) / (float)p.height;
         float dx = uvx * 2.0f - 1.0f, dy = uvy * 2.0f - 1.0f;
@@ -407,8 +519,8 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
         float3 dcam = normalize3(f3(target.x, target.y, target.z));
         float3 ocam = f3(0.0f);
         if (p.lens_radius > 0.0f) {
-            float lx = rand1(rng);
-            float ly = rand1(rng);
+            const float2 lxy = rnd2(p, rng);
+            const float lx = lxy.x, ly = lxy.y;
             float2 disk = concentric_sample_disk(lx, ly);
             float2 lens = make_float2(p.lens_radius * disk.x, p.lens_radius * disk.y);
             float ft = p.focal_distance / (-dcam.z);
@@ -427,7 +539,7 @@ __global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues
         ps.cum_rad[slot] = f4(cr, 0.0f);
         ps.cum_alb[slot] = f4(ca, 0.0f);
         ps.cum_nrm[slot] = f4(cn, 0.0f);
-        ps.rng[slot] = rng;
+        ps.rng[slot] = rng.s;
         uint32_t nf = F_ITEM;
         if (p.cam_volume != -1)
             nf |= F_INSIDE;
@@ -581,16 +693,16 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_walk(JobTable jt
 
 // Volume free flight on the current segment; returns true when the path
 // scattered in the medium (sampledMedium) and writes the scatter point.
-__device__ __forceinline__ bool medium_event(const SceneView &s, uint32_t vol, float vtstart, float vtend,
-                                             const float3 &origin, const float3 &raydir, float3 &beta, uint32_t &rng,
-                                             float3 &scatter_pos, float &g)
+__device__ __forceinline__ bool medium_event(const SceneView &s, const RenderParams &p, uint32_t vol, float vtstart,
+                                             float vtend, const float3 &origin, const float3 &raydir, float3 &beta,
+                                             PathRng &rng, float3 &scatter_pos, float &g)
 {
     Medium md = load_medium(s, vol);
     g = md.g;
     float3 dirn = normalize3(raydir);
     float dist_in = fmaxf(vtend - vtstart, kEps);
-    uint32_t channel = min((uint32_t)(rand1(rng) * 3.0f), 2u);
-    float u = rand1(rng);
+    uint32_t channel = min((uint32_t)(rnd1(p, rng) * 3.0f), 2u);
+    float u = rnd1(p, rng);
     float hit_dist = -logf(1.0f - u) / comp(md.sigma_t, channel);
     bool sampled = hit_dist < dist_in;
     float td = fminf(hit_dist, dist_in);
@@ -647,7 +759,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         const RenderParams &p = J.params;
 
         uint32_t flags = ps.flags[slot];
-        uint32_t rng = ps.rng[slot];
+        PathRng rng = load_rng(p, ps, slot);
         float3 beta = f3(ps.beta[slot]);
         float3 rad = f3(ps.rad[slot]);
         float3 origin = f3(ps.o[slot]);
@@ -686,7 +798,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         float g = 0.0f;
         if (inside && vol < s.num_materials) {
             float vtend = is_hit ? hv.x : fminf(p.zfar_trunc, kExtTmax);
-            sampled_medium = medium_event(s, vol, kExtTmin, vtend, origin, dir, beta, rng, scatter_pos, g);
+            sampled_medium = medium_event(s, p, vol, kExtTmin, vtend, origin, dir, beta, rng, scatter_pos, g);
         }
         if (sampled_medium) {
             // light sample at the scatter point with the HG phase function
@@ -707,8 +819,8 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
                 }
             }
             float3 wi;
-            float u0 = rand1(rng);
-            float u1 = rand1(rng);
+            const float2 uu = rnd2(p, rng);
+            const float u0 = uu.x, u1 = uu.y;
             float spdf = hg_sample(wo, wi, u0, u1, g);
             origin = scatter_pos;
             dir = wi;
@@ -761,7 +873,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
             bool passthrough = false;
             if (m.mrao.w > 0.0f) {
                 float alpha = material_alpha(s, m, tuv);
-                float r = rand1(rng);
+                float r = rnd1(p, rng);
                 if (alpha < kEps || r > alpha) {
                     if (h.front_volume != h.back_volume) {
                         inside = false;
@@ -831,13 +943,13 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
                     bool black_f = false;
                     float3 Fs;
                     if (lambert) {
-                        float u0 = rand1(rng);
-                        float u1 = rand1(rng);
+                        const float2 uu = rnd2(p, rng);
+                        const float u0 = uu.x, u1 = uu.y;
                         sdir_local = cosine_sample_hemisphere(u0, u1, spdf);
                     } else {
-                        float u0 = rand1(rng);
-                        float u1 = rand1(rng);
-                        float r = rand1(rng);
+                        const float2 uu = rnd2(p, rng);
+                        const float u0 = uu.x, u1 = uu.y;
+                        float r = rnd1(p, rng);
                         Fs = sample_pbr(sdir_local, wo, spdf, pbr, u0, u1, r);
                         black_f = is_black(Fs);
                     }
@@ -862,7 +974,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         }
         // Russian roulette (russian_roulette.glsl:1-11) for events that reach it
         if (!terminal_no_rr) {
-            float rr = rand1(rng);
+            float rr = rnd1(p, rng);
             if (d > kRussianRouletteDepth) {
                 float mb = fmaxf(beta.x, fmaxf(beta.y, beta.z));
                 if (rr >= mb)
@@ -892,7 +1004,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         if (has_nee)
             nf |= fuse ? F_NEE_FUSED : F_NEE;
         ps.flags[slot] = nf;
-        ps.rng[slot] = rng;
+        ps.rng[slot] = rng.s;
         ps.beta[slot] = f4(beta, 0.0f);
         ps.rad[slot] = f4(rad, 0.0f);
         ps.o[slot] = f4(origin, 0.0f);

@@ -27,6 +27,9 @@ struct RenderParams {
     uint32_t total_items; // width * height * batches
     uint32_t want_m2;
     uint32_t env_light;   // 1: the environment is sampled as one more light (VVPT_RENDER_ENV_IS)
+    uint32_t sampler;     // 0: RTGEMS stream, 1: PMJ (VVPT_RENDER_SAMPLER_PMJ)
+    const float *pmj;        // [16][16384][2] (sampler 1)
+    const float *blue_noise; // [48][128][128] (sampler 1)
 };
 
 // Structure-of-arrays path state, one entry per slot. A slot runs one

@@ -21,6 +21,24 @@ from .assets import srgb_encode, write_hdr
 from .scene import Engine, FlatScene
 
 
+def _sampler_flag(sampler: str) -> int:
+    if sampler not in ("rtgems", "pmj"):
+        raise ValueError("sampler must be 'rtgems' or 'pmj'")
+    return N.RENDER_SAMPLER_PMJ if sampler == "pmj" else 0
+
+
+def sampler_tables() -> tuple[np.ndarray, np.ndarray]:
+    """The PMJ sampler's tables (vvpt_sampler_tables): (16, 16384, 2) (0,2)
+    sequence points and (48, 128, 128) blue-noise values, float32."""
+    lib = N.load()
+    pmj = np.zeros((N.PMJ_SEQUENCES, N.PMJ_SAMPLES, 2), dtype=np.float32)
+    bn = np.zeros((N.BLUE_NOISE_TEXTURES, N.BLUE_NOISE_RES, N.BLUE_NOISE_RES), dtype=np.float32)
+    st = lib.vvpt_sampler_tables(pmj.ctypes.data, bn.ctypes.data)
+    if st != 0:
+        raise N.VvptError(st, "vvpt_sampler_tables failed")
+    return pmj, bn
+
+
 @dataclass
 class RenderInfo:
     samples: int = 256
@@ -136,13 +154,16 @@ class GpuScene:
 
     def render(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
                outputs: dict | None = None, profile: bool = False,
-               host_outputs: dict | None = None, env_is: bool = False) -> RenderResult | None:
+               host_outputs: dict | None = None, env_is: bool = False,
+               sampler: str = "rtgems") -> RenderResult | None:
         """Renders into new host arrays, into caller-provided host arrays
         (`host_outputs`), or into device pointers when `outputs` maps
         radiance/albedo/normal/radiance_m2 to device addresses. env_is: the
-        environment is importance sampled as a light (VVPT_RENDER_ENV_IS)."""
+        environment is importance sampled as a light (VVPT_RENDER_ENV_IS).
+        sampler: 'rtgems' (the reference's default xorshift stream) or 'pmj'
+        (its low-discrepancy sampler, VVPT_RENDER_SAMPLER_PMJ)."""
         flags = ((N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_PROFILE_KERNELS if profile else 0) |
-                 (N.RENDER_ENV_IS if env_is else 0))
+                 (N.RENDER_ENV_IS if env_is else 0) | _sampler_flag(sampler))
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         if host_outputs is not None:
             o = N.Outputs(host_outputs.get("radiance"), host_outputs.get("albedo"), host_outputs.get("normal"),
@@ -167,11 +188,11 @@ class GpuScene:
         return RenderResult(rad, alb, nrm, m2, self.ctx.stats(), info.samples // info.batch_size)
 
     def submit(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
-               outputs: dict | None = None, env_is: bool = False) -> "Job":
+               outputs: dict | None = None, env_is: bool = False, sampler: str = "rtgems") -> "Job":
         """Queues a render on the context's job engine (vvpt_submit). Outputs go
         to new host arrays, or to device pointers when `outputs` maps
         radiance/albedo/normal/radiance_m2 to device addresses."""
-        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_ENV_IS if env_is else 0)
+        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_ENV_IS if env_is else 0) | _sampler_flag(sampler)
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         job = Job(self, info, want_m2)
         if outputs is not None:
