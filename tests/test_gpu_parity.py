@@ -161,6 +161,35 @@ def test_pmj_sampler_matches_oracle(ctx, scene):
     assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
 
 
+def test_converged_render_matches_fp64_oracle(ctx):
+    """A converged GPU image (4096 spp) against the oracle's FP64-accumulated
+    render at 4x the samples: per pixel within 3 Monte Carlo standard errors
+    (the standard errors of both images from their batch sums, at least 99 %
+    of the pixels) and the image means within 1e-3 relative."""
+    e, info = scenes.cornell_box(1, 32, 32, 4096, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(info.width, info.height)
+    g = ctx.upload(fs)
+    res = g.render(sd, info, want_m2=True)
+    g.release()
+    batches = info.samples // info.batch_size
+    info.samples *= 4
+    ref = oracle.render(fs, sd, info, fp64=True)
+    rb = info.samples // info.batch_size
+
+    def mean_and_se(img, m2, nb):
+        # the image is the sum of nb batch contributions; m2 sums their squares
+        x = img[..., :3].astype(np.float64)
+        var = np.maximum(nb * m2[..., :3].astype(np.float64) - x * x, 0.0) / max(nb - 1, 1)
+        return x, np.sqrt(var)
+
+    a, sa = mean_and_se(res.radiance, res.radiance_m2, batches)
+    b, sb = mean_and_se(ref["radiance"], ref["radiance_m2"], rb)
+    z = np.abs(a - b) / np.sqrt(sa ** 2 + sb ** 2 + 1e-30)
+    assert (z <= 3.0).all(-1).mean() >= 0.99, np.sort(z.ravel())[-10:]
+    assert abs(a.mean() - b.mean()) <= 1e-3 * b.mean(), (a.mean(), b.mean())
+
+
 def test_instanced_sky_scene_matches_oracle(ctx):
     """512 rigid instances of 8 displaced meshes (20.7M instanced
     triangles), 32 mesh lights, thin lens, procedural sky with the

@@ -941,13 +941,52 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
 }
 
-__global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap, int ncols,
-                                                        int nacc, int ring, int segs, int seg_rows, uint32_t *err)
+// Bounded wait that also gives up once another role has aborted.
+__device__ __forceinline__ bool mbar_wait_role(uint32_t bar, uint32_t parity, const volatile int *abort_flag)
+{
+    const unsigned long long t0 = globaltimer();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+        if (*abort_flag || globaltimer() - t0 > kTcWaitNs)
+            return false;
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+}
+
+// 192 threads: warps 0-3 drain accumulators (TMEM lane quarter = warp),
+// warp 4 loads halo rows by TMA, warp 5 issues the MMAs. The roles run
+// ahead of each other as far as the ring (`ring` halo-row slots) and the two
+// accumulators allow, synchronised only by mbarriers:
+//   full[s]   TMA bytes of the halo row in slot s landed (producer -> MMA)
+//   empty[s]  the MMAs that read slot s completed (MMA commit -> producer)
+//   acc_full[b]  row accumulator b is complete (MMA commit -> drain)
+//   acc_empty[b] the four drain warps have read accumulator b (drain -> MMA)
+constexpr int kStThreads = 192;
+
+__global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                              int ncols, int nacc, int ring, int segs, int seg_rows,
+                                                              uint32_t *err)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     __shared__ uint32_t tmem_holder;
-    __shared__ __align__(8) uint64_t full[kStMaxRing];
-    __shared__ __align__(8) uint64_t mma_done[2];
+    __shared__ __align__(8) uint64_t full[kStMaxRing], empty[kStMaxRing];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2];
     __shared__ int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.wd + kTcM - 1) / kTcM;
@@ -961,14 +1000,17 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
     const uint32_t ring_base = (raw + 1023u) & ~1023u;
     const uint32_t w_base = ring_base + (uint32_t)(ring * slot_bytes);
     uint8_t *w_ptr = smem_raw + (w_base - raw);
-    const uint64_t tmap_ptr = reinterpret_cast<uint64_t>(&tmap);
-    const uint32_t row_tx = (uint32_t)(KC * kStHaloPx * 16);
+    const volatile int *abort_v = &abort_flag;
 
     if (tid == 0) {
-        for (int r = 0; r < ring; r++)
+        for (int r = 0; r < ring; r++) {
             mbar_init(&full[r], 1);
-        mbar_init(&mma_done[0], 1);
-        mbar_init(&mma_done[1], 1);
+            mbar_init(&empty[r], 1);
+        }
+        for (int k = 0; k < 2; k++) {
+            mbar_init(&acc_full[k], 1);
+            mbar_init(&acc_empty[k], 4);
+        }
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -977,7 +1019,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
                      "r"(ncols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    for (int i = tid; i < 9 * N * KC; i += 128) {
+    for (int i = tid; i < 9 * N * KC; i += kStThreads) {
         const int kc = i % KC, n = (i / KC) % N, tap = i / (KC * N);
         const bool ok = n < a.cout;
         const bf16 *src = ok ? a.wgt + ((long)n * 9 + tap) * a.cin + 8 * kc : a.wgt;
@@ -990,91 +1032,86 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_holder;
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
 
-    // descriptor fields other than the start address (16-byte units in the
-    // low 14 bits; shared addresses stay below 256 KB, so adding an offset to
-    // a descriptor adds it to the address field)
-    const uint64_t a_hi = umma_desc(0, kStKCBytes, 128), b_hi = umma_desc(0, 128, (uint32_t)(KC * 128));
-    const uint32_t a_lo_base = ring_base >> 4, a_lo_slot = (uint32_t)slot_bytes >> 4;
-    const uint32_t b_lo_base = w_base >> 4, b_lo_tap = (uint32_t)tap_bytes >> 4;
-
-    // thread 0's view of the pipeline, counted over the CTA's run
-    int g_issued = 0, g_waited = 0;  // halo rows loaded / seen complete
-    int issue_slot = 0;              // ring slot of halo row g_issued
-    int wait_slot = 0, wait_phase = 0; // ring slot and parity of halo row g_waited
-    int g_mma = -1;                  // last output row whose MMAs were committed
-    int g_row = 0;                   // output rows of earlier units
-    int g_halo = 0;                  // halo rows of earlier units
-
-    for (int u = blockIdx.x; u < units && !abort_flag; u += gridDim.x) {
-        const int sg = u % segs, tx = (u / segs) % tiles_x, nb = u / (segs * tiles_x);
-        const int x0 = tx * kTcM, ya = sg * seg_rows;
-        const int nout = min(a.h, ya + seg_rows) - ya;
-        if (nout <= 0)
-            continue;
-        const int nh = nout + 2;
-        // halo rows are issued in order, one slot after the other
-        auto issue_row = [&](int) {
-            const int slot = issue_slot;
-            issue_slot = slot + 1 == ring ? 0 : slot + 1;
-            const int h = g_issued - g_halo;
-            const uint32_t bar = smem_addr(&full[slot]);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(row_tx) : "memory");
-            const uint32_t dst = ring_base + (uint32_t)(slot * slot_bytes);
-            for (int kc = 0; kc < KC; kc++)
-                asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-                             "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst + (uint32_t)(kc * kStKCBytes)),
-                             "l"(tmap_ptr), "r"(8 * kc), "r"(x0 - 1), "r"(ya - 1 + h), "r"(nb), "r"(bar)
-                             : "memory");
-            g_issued++;
-        };
-        auto drain = [&](int gi, int i) {
-            // output row i of this unit, accumulator gi & 1
-            const int x = x0 + warp * 32 + lane;
-            const long p = ((long)nb * a.h + ya + i) * a.wd + x;
-            const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(gi & 1) * half_cols;
-            for (int c = 0; c < N; c += 16) {
-                uint32_t r[16];
-                tmem_ld16(acc + (uint32_t)c, r);
-                for (int q = 1; q < nacc; q++) {
-                    uint32_t t[16];
-                    tmem_ld16(acc + (uint32_t)(q * N + c), t);
-#pragma unroll
-                    for (int k = 0; k < 16; k++)
-                        r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
-                }
-                if (x < a.wd && c < a.cout)
-                    store_row16(a, p, c, r);
-            }
-        };
-        // every halo row of earlier units has been consumed: this unit's halo
-        // row 0 goes to the next slot
-        int row_slot = issue_slot; // slot of this unit's halo row i
-        if (tid == 0)
-            for (int h = 0; h < min(ring, nh); h++)
-                issue_row(h);
-        for (int i = 0; i < nout; i++) {
-            const int gi = g_row + i;
-            if (tid == 0) {
-                bool ok = true;
-                while (ok && g_waited < g_halo + i + 3) {
-                    ok = mbar_wait(smem_addr(&full[wait_slot]), (uint32_t)wait_phase);
-                    if (ok) {
-                        g_waited++;
-                        if (++wait_slot == ring) {
-                            wait_slot = 0;
-                            wait_phase ^= 1;
-                        }
+    if (warp == 4) {
+        // ---- producer: one TMA row (KC boxes of 8 channels x 130 pixels) per halo row
+        if (lane == 0) {
+            const uint64_t tmap_ptr = reinterpret_cast<uint64_t>(&tmap);
+            const uint32_t row_tx = (uint32_t)(KC * kStHaloPx * 16);
+            int slot = 0, phase = 0, issued = 0;
+            int last_phase[kStMaxRing];
+            for (int r = 0; r < kStMaxRing; r++)
+                last_phase[r] = -1;
+            for (int u = blockIdx.x; u < units && !*abort_v; u += gridDim.x) {
+                const int sg = u % segs, tx = (u / segs) % tiles_x, nb = u / (segs * tiles_x);
+                const int x0 = tx * kTcM, ya = sg * seg_rows;
+                const int nout = min(a.h, ya + seg_rows) - ya;
+                if (nout <= 0)
+                    continue;
+                for (int h = 0; h < nout + 2; h++) {
+                    if (!mbar_wait_role(smem_addr(&empty[slot]), (uint32_t)(phase ^ 1), abort_v)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    const uint32_t bar = smem_addr(&full[slot]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(row_tx)
+                                 : "memory");
+                    const uint32_t dst = ring_base + (uint32_t)(slot * slot_bytes);
+                    for (int kc = 0; kc < KC; kc++)
+                        asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                                     "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst + (uint32_t)(kc * kStKCBytes)),
+                                     "l"(tmap_ptr), "r"(8 * kc), "r"(x0 - 1), "r"(ya - 1 + h), "r"(nb), "r"(bar)
+                                     : "memory");
+                    last_phase[slot] = phase;
+                    issued++;
+                    if (++slot == ring) {
+                        slot = 0;
+                        phase ^= 1;
                     }
                 }
-                if (!ok) {
+            }
+            // every copy issued has landed before the CTA exits
+            for (int r = 0; r < ring; r++)
+                if (last_phase[r] >= 0 && !mbar_wait(smem_addr(&full[r]), (uint32_t)last_phase[r]))
                     abort_flag = 1;
-                } else {
+        }
+    } else if (warp == 5) {
+        // ---- MMA issue: 9 taps x cin / 16 steps per output row
+        if (lane == 0) {
+            const uint32_t idesc =
+                (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+            const uint64_t a_hi = umma_desc(0, kStKCBytes, 128), b_hi = umma_desc(0, 128, (uint32_t)(KC * 128));
+            const uint32_t a_lo_base = ring_base >> 4, a_lo_slot = (uint32_t)slot_bytes >> 4;
+            const uint32_t b_lo_base = w_base >> 4, b_lo_tap = (uint32_t)tap_bytes >> 4;
+            int row_slot = 0;            // slot of the unit's halo row i
+            int wait_slot = 0, wait_phase = 0, waited = 0; // next halo row to see complete
+            int gi = 0;                  // output rows so far
+            int halo = 0;                // halo rows of earlier units
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                const int sg = u % segs;
+                const int ya = sg * seg_rows;
+                const int nout = min(a.h, ya + seg_rows) - ya;
+                if (nout <= 0)
+                    continue;
+                for (int i = 0; i < nout && ok; i++, gi++) {
+                    while (ok && waited < halo + i + 3) {
+                        ok = mbar_wait_role(smem_addr(&full[wait_slot]), (uint32_t)wait_phase, abort_v);
+                        if (ok) {
+                            waited++;
+                            if (++wait_slot == ring) {
+                                wait_slot = 0;
+                                wait_phase ^= 1;
+                            }
+                        }
+                    }
+                    const int b = gi & 1;
+                    if (ok)
+                        ok = mbar_wait_role(smem_addr(&acc_empty[b]), (uint32_t)(((gi >> 1) & 1) ^ 1), abort_v);
+                    if (!ok)
+                        break;
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    // tap t accumulates into accumulator t % nacc: consecutive
-                    // MMAs go to different accumulators (independent chains)
-                    const uint32_t acc = tmem + (uint32_t)(gi & 1) * half_cols;
+                    const uint32_t acc = tmem + (uint32_t)b * half_cols;
                     uint32_t slot_lo[3];
 #pragma unroll
                     for (int dy = 0; dy < 3; dy++) {
@@ -1097,64 +1134,75 @@ __global__ void __launch_bounds__(128) k_conv3x3_strip(ConvArgs a, const __grid_
                                          "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
                         }
                     }
-                    asm volatile(
-                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                            smem_addr(&mma_done[gi & 1])));
-                    g_mma = gi;
+                    umma_commit(smem_addr(&acc_full[b]));
+                    // halo row i is not read by later rows of the unit
+                    umma_commit(smem_addr(&empty[row_slot]));
+                    row_slot = row_slot + 1 == ring ? 0 : row_slot + 1;
                 }
-            }
-            if (i >= 1) {
-                const int gp = gi - 1;
-                bool ok = mbar_wait(smem_addr(&mma_done[gp & 1]), (uint32_t)((gp >> 1) & 1));
-                ok = __all_sync(0xffffffffu, ok);
                 if (!ok)
-                    abort_flag = 1;
-                if (ok) {
-                    // the slot of halo row i - 1 is free once the MMAs of row i - 1 are done
-                    if (tid == 0 && !abort_flag && i - 1 + ring < nh)
-                        issue_row(i - 1 + ring);
-                    asm volatile("tcgen05.fence::after_thread_sync;");
-                    drain(gp, i - 1);
+                    break;
+                // the unit's last two halo rows
+                for (int k = 0; k < 2; k++) {
+                    umma_commit(smem_addr(&empty[row_slot]));
+                    row_slot = row_slot + 1 == ring ? 0 : row_slot + 1;
                 }
+                halo += nout + 2;
             }
-            row_slot = row_slot + 1 == ring ? 0 : row_slot + 1;
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncthreads();
-            if (abort_flag)
-                break;
-        }
-        if (!abort_flag) {
-            const int gl = g_row + nout - 1;
-            bool ok = mbar_wait(smem_addr(&mma_done[gl & 1]), (uint32_t)((gl >> 1) & 1));
-            ok = __all_sync(0xffffffffu, ok);
             if (!ok)
                 abort_flag = 1;
-            else {
+            // the MMAs of the last row issued are complete before TMEM is freed
+            if (gi > 0 && !mbar_wait(smem_addr(&acc_full[(gi - 1) & 1]), (uint32_t)(((gi - 1) >> 1) & 1)))
+                abort_flag = 1;
+        }
+    } else {
+        // ---- drain: warp w reads TMEM lanes 32w..32w+31 (pixels x0 + 32w + lane)
+        int gi = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            const int sg = u % segs, tx = (u / segs) % tiles_x, nb = u / (segs * tiles_x);
+            const int x0 = tx * kTcM, ya = sg * seg_rows;
+            const int nout = min(a.h, ya + seg_rows) - ya;
+            if (nout <= 0)
+                continue;
+            for (int i = 0; i < nout; i++, gi++) {
+                const int b = gi & 1;
+                ok = mbar_wait_role(smem_addr(&acc_full[b]), (uint32_t)((gi >> 1) & 1), abort_v);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
+                    break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                drain(gl, nout - 1);
+                const int x = x0 + warp * 32 + lane;
+                const long p = ((long)nb * a.h + ya + i) * a.wd + x;
+                const uint32_t acc = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)b * half_cols;
+                for (int c = 0; c < N; c += 16) {
+                    uint32_t r[16];
+                    tmem_ld16(acc + (uint32_t)c, r);
+                    for (int q = 1; q < nacc; q++) {
+                        uint32_t t[16];
+                        tmem_ld16(acc + (uint32_t)(q * N + c), t);
+#pragma unroll
+                        for (int k = 0; k < 16; k++)
+                            r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
+                    }
+                    if (c + 16 >= N) {
+                        // the accumulator is read: hand it back to the MMA warp
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            mbar_arrive(smem_addr(&acc_empty[b]));
+                    }
+                    if (x < a.wd && c < a.cout)
+                        store_row16(a, p, c, r);
+                }
             }
         }
-        g_row += nout;
-        g_halo += nh;
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-    }
-    if (abort_flag && tid == 0) {
-        atomicOr(err, 1u);
-        // let copies and MMAs still in flight land before the CTA exits
-        for (int g = g_waited; g < g_issued; g++) {
-            if (!mbar_wait(smem_addr(&full[wait_slot]), (uint32_t)wait_phase))
-                break;
-            if (++wait_slot == ring) {
-                wait_slot = 0;
-                wait_phase ^= 1;
-            }
-        }
-        if (g_mma >= 0)
-            mbar_wait(smem_addr(&mma_done[g_mma & 1]), (uint32_t)((g_mma >> 1) & 1));
+        if (!ok)
+            abort_flag = 1;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    if (abort_flag && tid == 0)
+        atomicOr(err, 1u);
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
@@ -1273,7 +1321,8 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
                                  cudaSharedmemCarveoutMaxShared);
             attr_smem = pl.smem;
         }
-        k_conv3x3_strip<<<pl.grid, 128, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs, pl.seg_rows, err);
+        k_conv3x3_strip<<<pl.grid, kStThreads, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs,
+                                                             pl.seg_rows, err);
         return;
     }
     if (err && a.cout <= 256) {
