@@ -1,7 +1,8 @@
 // Denoiser kernels (denoise_kernels.cuh). The convolutions are implicit GEMMs
-// on the BF16 tensor cores through warp-level mma.sync m16n8k16 with FP32
-// accumulators; operand tiles are staged in shared memory and read with
-// ldmatrix.
+// on the BF16 tensor cores with FP32 accumulators: tcgen05 MMAs into TMEM
+// (the strip kernel, TMA-fed, for layers whose weights fit in shared memory;
+// per-tile kernels for the rest), and the warp-level mma.sync m16n8k16 kernels
+// (operand tiles read with ldmatrix) kept as a cross-check.
 #include <algorithm>
 
 #include <cuda.h>
@@ -924,14 +925,15 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
 // consecutive 16-byte rows (one TMA box of 8 channels x 130 pixels), groups
 // kStKCBytes apart; a tap (dy, dx) of output row i is the operand starting at
 // slot(i + dy) + 16 dx (SBO 128 B between 8-pixel groups, LBO kStKCBytes
-// between channel groups). Two TMEM accumulators alternate: one thread issues
-// the MMAs of row i (9 taps x cin / 16 steps) and commits them to the row's
-// mbarrier while all four warps drain row i - 1 (TMEM lane = pixel). The slot
-// of halo row i - 1 is refilled once the MMAs of row i - 1 are complete.
-// Halo rows and output rows are counted over the CTA's whole run, so slot
-// and accumulator phases carry across units. Every wait is bounded by the
-// global timer; on a timeout the kernel records an error, stops issuing,
-// waits (bounded) for its copies and MMAs in flight and frees its TMEM.
+// between channel groups). Two TMEM accumulators alternate between output
+// rows; each holds `nacc` partial sums (taps spread over independent MMA
+// chains) that the drain adds. The roles (k_conv3x3_strip below) are warp
+// specialised: a producer warp, an MMA warp and four drain warps, linked by
+// mbarriers only. Halo rows and output rows are counted over the CTA's whole
+// run, so slot and accumulator phases carry across units. Every wait is
+// bounded by the global timer; on a timeout the kernel records an error, the
+// other roles stop at their next wait, copies and MMAs in flight are waited
+// for (bounded) and the TMEM is freed.
 constexpr int kStKCBytes = 2176; // 130 pixels x 16 B, padded to a multiple of 128 B
 constexpr int kStHaloPx = kTcM + 2;
 constexpr int kStMaxRing = 8, kStMinRing = 4;
