@@ -56,6 +56,21 @@ def test_jobs_in_a_mix_equal_single_renders(ctx, mixed_jobs):
         j.release()
 
 
+def test_jobs_with_different_samplers_in_one_mix(ctx, mixed_jobs):
+    """Jobs of both samplers (RTGEMS and PMJ) and with the environment as a
+    light share the fused queues: each job's sampler and estimator travel
+    with its parameters, so every image still equals its single render."""
+    flavours = [dict(sampler="pmj"), dict(sampler="rtgems"), dict(sampler="pmj", env_is=True)]
+    alone = [g.render(sd, info, **kw) for (g, sd, info), kw in zip(mixed_jobs, flavours)]
+    jobs = [g.submit(sd, info, **kw) for (g, sd, info), kw in zip(mixed_jobs, flavours)]
+    for k, j in enumerate(jobs):
+        _same(j.result(), alone[k])
+        j.release()
+    # and the PMJ images differ from the RTGEMS ones of the same requests
+    g, sd, info = mixed_jobs[0]
+    assert not np.array_equal(g.render(sd, info).radiance, alone[0].radiance)
+
+
 def test_many_small_jobs_and_device_outputs(ctx, mixed_jobs):
     torch = pytest.importorskip("torch")
     g, sd, info = mixed_jobs[0]

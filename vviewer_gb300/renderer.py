@@ -192,7 +192,8 @@ class GpuScene:
         """Queues a render on the context's job engine (vvpt_submit). Outputs go
         to new host arrays, or to device pointers when `outputs` maps
         radiance/albedo/normal/radiance_m2 to device addresses."""
-        flags = (N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_ENV_IS if env_is else 0) | _sampler_flag(sampler)
+        flags = ((N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_ENV_IS if env_is else 0) |
+                 _sampler_flag(sampler))
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         job = Job(self, info, want_m2)
         if outputs is not None:
