@@ -779,12 +779,19 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(ConvArgs a, int ncols, uint3
 // as k_conv3x3_tc.
 
 // one stage when the layer has a single chunk, else two
-__host__ __device__ constexpr int tc_chunk_smem_bytes(int N, int nchunks)
+// halo of `rows` output rows: rows + 2 halo rows, rounded up to 1 KB
+__host__ __device__ constexpr int tc_chunk_halo_bytes(int rows) { return ((rows + 2) * kTcHaloRow + 1023) / 1024 * 1024; }
+
+__host__ __device__ constexpr int tc_chunk_smem_bytes(int N, int nchunks, int rows)
 {
-    return (nchunks > 1 ? 2 : 1) * (kTcHaloAlloc + 9 * N * kTcBK * 2);
+    return (nchunks > 1 ? 2 : 1) * (tc_chunk_halo_bytes(rows) + 9 * N * kTcBK * 2);
 }
 
-__global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols, int nacc, uint32_t *err)
+// output rows per CTA of the chunk kernel: the chunk's weights are staged once
+// for all of them (4 rows up to 64 output channels, else 2: two stages fit)
+inline int tc_chunk_rows(int N) { return N <= 64 ? 4 : 2; }
+
+__global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols, int nacc, int rows, uint32_t *err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_holder;
@@ -792,13 +799,15 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
     __shared__ int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.wd + kTcM - 1) / kTcM;
+    const int yblocks = (a.h + rows - 1) / rows;
     const int tx = blockIdx.x % tiles_x;
-    const int y = (blockIdx.x / tiles_x) % a.h;
-    const int nb = blockIdx.x / (tiles_x * a.h);
+    const int y0 = (blockIdx.x / tiles_x) % yblocks * rows;
+    const int nb = blockIdx.x / (tiles_x * yblocks);
     const int x0 = tx * kTcM;
     const int N = (a.cout + 15) & ~15;
     const int tap_bytes = N * kTcBK * 2;
-    const int stage_bytes = kTcHaloAlloc + 9 * tap_bytes;
+    const int halo_alloc = tc_chunk_halo_bytes(rows);
+    const int stage_bytes = halo_alloc + 9 * tap_bytes;
     const int nchunks = (a.cin + kTcBK - 1) / kTcBK;
     const uint32_t sbase = smem_addr(smem);
 
@@ -820,11 +829,11 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
 
     auto load_chunk = [&](int c) {
         uint8_t *h = smem + (c & 1) * stage_bytes;
-        uint8_t *bw = h + kTcHaloAlloc;
+        uint8_t *bw = h + halo_alloc;
         const int ci0 = c * kTcBK;
-        for (int i = tid; i < 3 * kTcKC * kTcHaloPx; i += 128) {
+        for (int i = tid; i < (rows + 2) * kTcKC * kTcHaloPx; i += 128) {
             const int px = i % kTcHaloPx, kc = (i / kTcHaloPx) % kTcKC, hr = i / (kTcHaloPx * kTcKC);
-            const int yy = y + hr - 1, xx = x0 - 1 + px, ci = ci0 + 8 * kc;
+            const int yy = y0 + hr - 1, xx = x0 - 1 + px, ci = ci0 + 8 * kc;
             const bool ok = yy >= 0 && yy < a.h && xx >= 0 && xx < a.wd && ci < a.cin;
             const bf16 *src = ok ? a.in + (((long)nb * a.h + yy) * a.wd + xx) * a.cin + ci : a.in;
             cp_async16(h + ((hr * kTcKC + kc) * kTcHaloPx + px) * 16, src, ok);
@@ -847,21 +856,25 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
             break;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t h_addr = sbase + (c & 1) * stage_bytes, b_addr = h_addr + kTcHaloAlloc;
-            // tap t accumulates into accumulator t % nacc (independent chains)
+            const uint32_t h_addr = sbase + (c & 1) * stage_bytes, b_addr = h_addr + halo_alloc;
+            // output row r of the block, tap t: accumulator r * nacc + t % nacc
+            // (independent chains); the chunk's weights serve all rows
+            for (int r = 0; r < rows; r++) {
 #pragma unroll
-            for (int j = 0; j < kTcBK / 16; j++) {
+                for (int j = 0; j < kTcBK / 16; j++) {
 #pragma unroll
-                for (int tap = 0; tap < 9; tap++) {
-                    const int dy = tap / 3, dx = tap % 3;
-                    const uint64_t ad =
-                        umma_desc(h_addr + dy * kTcHaloRow + dx * 16 + j * 2 * kTcHaloPx * 16, kTcHaloPx * 16, 128);
-                    const uint64_t bd = umma_desc(b_addr + tap * tap_bytes + j * 2 * 128, 128, kTcKC * 128);
-                    const uint32_t accumulate = (c > 0 || j > 0 || tap >= nacc) ? 1u : 0u;
-                    const uint32_t dst = tmem + (uint32_t)((tap & (nacc - 1)) * N);
-                    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dst),
-                                 "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+                    for (int tap = 0; tap < 9; tap++) {
+                        const int dy = tap / 3, dx = tap % 3;
+                        const uint64_t ad = umma_desc(h_addr + (r + dy) * kTcHaloRow + dx * 16 +
+                                                          j * 2 * kTcHaloPx * 16,
+                                                      kTcHaloPx * 16, 128);
+                        const uint64_t bd = umma_desc(b_addr + tap * tap_bytes + j * 2 * 128, 128, kTcKC * 128);
+                        const uint32_t accumulate = (c > 0 || j > 0 || tap >= nacc) ? 1u : 0u;
+                        const uint32_t dst = tmem + (uint32_t)((r * nacc + (tap & (nacc - 1))) * N);
+                        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dst),
+                                     "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+                    }
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -886,21 +899,23 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!abort_flag) {
         const int x = x0 + warp * 32 + lane;
-        const long p = ((long)nb * a.h + y) * a.wd + x;
-        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c = 0; c < N; c += 16) {
-            uint32_t r[16];
-            tmem_ld16(lane_base + (uint32_t)c, r);
-            for (int q = 1; q < nacc; q++) {
-                uint32_t t[16];
-                tmem_ld16(lane_base + (uint32_t)(q * N + c), t);
+        for (int rr = 0; rr < rows && y0 + rr < a.h; rr++) {
+            const long p = ((long)nb * a.h + y0 + rr) * a.wd + x;
+            const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(rr * nacc * N);
+            for (int c = 0; c < N; c += 16) {
+                uint32_t r[16];
+                tmem_ld16(lane_base + (uint32_t)c, r);
+                for (int q = 1; q < nacc; q++) {
+                    uint32_t t[16];
+                    tmem_ld16(lane_base + (uint32_t)(q * N + c), t);
 #pragma unroll
-                for (int k = 0; k < 16; k++)
-                    r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
+                    for (int k = 0; k < 16; k++)
+                        r[k] = __float_as_uint(__uint_as_float(r[k]) + __uint_as_float(t[k]));
+                }
+                if (x >= a.wd || c >= a.cout)
+                    continue;
+                store_row16(a, p, c, r);
             }
-            if (x >= a.wd || c >= a.cout)
-                continue;
-            store_row16(a, p, c, r);
         }
     } else if (tid == 0) {
         atomicOr(err, 1u);
@@ -936,7 +951,9 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc_chunk(ConvArgs a, int ncols,
 // for (bounded) and the TMEM is freed.
 constexpr int kStKCBytes = 2176; // 130 pixels x 16 B, padded to a multiple of 128 B
 constexpr int kStHaloPx = kTcM + 2;
-constexpr int kStMaxRing = 8, kStMinRing = 4;
+// at least the three halo rows one output row reads; three slots (no row
+// prefetched ahead) are taken when they let more CTAs share an SM
+constexpr int kStMaxRing = 8, kStMinRing = 3;
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 {
@@ -1332,7 +1349,8 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
         if (!attr_set) {
             cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem_bytes(256));
             cudaFuncSetAttribute(k_conv3x3_tc_chunk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tc_chunk_smem_bytes(128, 2));
+                                 std::max(tc_chunk_smem_bytes(128, 2, tc_chunk_rows(128)),
+                                          tc_chunk_smem_bytes(64, 2, tc_chunk_rows(64))));
             attr_set = true;
         }
         const int N = (a.cout + 15) & ~15;
@@ -1341,21 +1359,15 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
             ncols <<= 1;
         const long tiles = (long)a.n * a.h * ((a.wd + kTcM - 1) / kTcM);
         if (N <= 128) {
-            // as many accumulators as the TMEM left by co-resident CTAs allows
-            const int smem = tc_chunk_smem_bytes(N, (a.cin + kTcBK - 1) / kTcBK);
-            const int per_sm = std::max(1, 233472 / (smem + 2048));
-            int nacc = 1, cols = ncols;
-            for (int q = 4; q >= 2; q >>= 1) {
-                int cq = 32;
-                while (cq < q * N)
-                    cq <<= 1;
-                if (per_sm * cq <= 512) {
-                    nacc = q;
-                    cols = cq;
-                    break;
-                }
-            }
-            k_conv3x3_tc_chunk<<<(unsigned)tiles, 128, smem, s>>>(a, cols, nacc, err);
+            // several output rows per CTA, one accumulator (one MMA chain)
+            // per row
+            const int rows = tc_chunk_rows(N);
+            const int smem = tc_chunk_smem_bytes(N, (a.cin + kTcBK - 1) / kTcBK, rows);
+            int cols = 32;
+            while (cols < rows * N)
+                cols <<= 1;
+            const long blocks = (long)a.n * ((a.h + rows - 1) / rows) * ((a.wd + kTcM - 1) / kTcM);
+            k_conv3x3_tc_chunk<<<(unsigned)blocks, 128, smem, s>>>(a, cols, 1, rows, err);
         }
         else
             k_conv3x3_tc<<<(unsigned)tiles, 128, tc_smem_bytes(N), s>>>(a, ncols, err);
