@@ -105,7 +105,7 @@ def test_training_on_tracer_pairs_beats_the_noisy_render(ctx):
     dn.close()
 
 
-@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_tiles", "tcgen05_persistent"])
+@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_tiles", "tcgen05_persistent", "tcgen05_unfused"])
 @pytest.mark.parametrize("n,h,w", [(2, 64, 48), (1, 48, 272)])
 def test_tcgen05_and_mma_sync_kernels_agree(ctx, kind, n, h, w):
     """The tcgen05 convolutions (TMEM accumulators) against the warp-level
@@ -133,4 +133,27 @@ def test_tcgen05_and_mma_sync_kernels_agree(ctx, kind, n, h, w):
     assert abs(l0 - l1) <= 1e-3 * l0
     assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0)
     assert np.allclose(o1, o0, rtol=2e-2, atol=1e-3)
+    dn.close()
+
+
+@pytest.mark.parametrize("n,h,w", [(1, 64, 48), (1, 48, 272)])
+def test_fused_upsample_concat_is_exact(ctx, n, h, w):
+    """Inference reads the decoder's upsample + concat input straight from the
+    coarse and skip tensors (an extra warp writes the upsampled channels into
+    the strip kernel's ring); the convolution sees the same BF16 values in the
+    same order, so the image is bit-identical to the unfused path's."""
+    import torch
+    rng = np.random.default_rng(8)
+    ins = [_cuda(rng.gamma(1.0, 0.5, (h, w, 4))), _cuda(rng.uniform(0, 1, (h, w, 4))),
+           _cuda(rng.uniform(0, 1, (h, w, 4)))]
+    dn = Denoiser(ctx, seed=4)
+    outs = {}
+    for kind in ("tcgen05", "tcgen05_unfused", "tcgen05_persistent"):
+        dn.set_kernels(kind)
+        o = torch.zeros((h, w, 4), device="cuda")
+        dn.apply(*ins, o)
+        torch.cuda.synchronize()
+        outs[kind] = o.cpu().numpy()
+    assert np.array_equal(outs["tcgen05"], outs["tcgen05_unfused"])
+    assert np.array_equal(outs["tcgen05_persistent"], outs["tcgen05_unfused"])
     dn.close()

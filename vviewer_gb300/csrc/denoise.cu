@@ -188,6 +188,30 @@ void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, b
     vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>(), dn->conv_kind);
 }
 
+// layer li over concat(upsample2(coarse), skip) without the concatenated
+// tensor; false when only the unfused path takes the layer
+bool conv_fwd_concat(vvpt_denoiser *dn, int li, const bf16 *coarse, int cc, const bf16 *skip, bf16 *out, int level,
+                     cudaStream_t s)
+{
+    if (dn->mma_sync)
+        return false;
+    const Layer &L = dn->layers[li];
+    vvdn::ConvArgs a{};
+    a.in = skip;
+    a.cin = L.cin;
+    a.coarse = coarse;
+    a.cc = cc;
+    a.wgt = dn->w16.as<bf16>() + L.w16_off;
+    a.bias = dn->params.as<float>() + L.b_off;
+    a.out = out;
+    a.cout = L.cout;
+    a.relu = L.relu ? 1 : 0;
+    a.n = dn->n;
+    a.h = dn->h >> level;
+    a.wd = dn->w >> level;
+    return vvdn::conv3x3_concat(a, s, dn->err.as<uint32_t>(), dn->conv_kind);
+}
+
 // input gradient of layer li: din = conv(dout, w_t) * (mask > 0)
 void conv_dgrad(vvpt_denoiser *dn, int li, const bf16 *dout, bf16 *din, const bf16 *mask, int level, cudaStream_t s)
 {
@@ -215,7 +239,12 @@ void conv_wgrad(vvpt_denoiser *dn, int li, const bf16 *dout, const bf16 *in, int
                         dn->grads.as<float>() + L.w_off, dn->grads.as<float>() + L.b_off, s);
 }
 
-void forward(vvpt_denoiser *dn, const float *rad, const float *alb, const float *nrm, cudaStream_t s)
+// inference (fuse_concat): the decoder's first convolution of a level reads
+// concat(upsample(coarse), skip) straight from both tensors where the strip
+// kernel takes it; training keeps the concatenated tensor for the weight
+// gradient
+void forward(vvpt_denoiser *dn, const float *rad, const float *alb, const float *nrm, cudaStream_t s,
+             bool fuse_concat = false)
 {
     refresh_weights(dn, s);
     const int n = dn->n;
@@ -229,10 +258,13 @@ void forward(vvpt_denoiser *dn, const float *rad, const float *alb, const float 
     }
     for (int l = kLevels - 2; l >= 0; l--) {
         const Tensor &coarse = l == kLevels - 2 ? dn->e[kLevels - 1] : dn->d[l + 1];
-        vvdn::upcat(act(dn, coarse), kCh[l + 1], act(dn, dn->e[l]), kCh[l], act(dn, dn->u[l]), n, dn->h >> l,
-                    dn->w >> l, s);
         const int li = 10 + 2 * (kLevels - 2 - l);
-        conv_fwd(dn, li, act(dn, dn->u[l]), act(dn, dn->b[l]), l, false, s);
+        if (!(fuse_concat && conv_fwd_concat(dn, li, act(dn, coarse), kCh[l + 1], act(dn, dn->e[l]),
+                                             act(dn, dn->b[l]), l, s))) {
+            vvdn::upcat(act(dn, coarse), kCh[l + 1], act(dn, dn->e[l]), kCh[l], act(dn, dn->u[l]), n, dn->h >> l,
+                        dn->w >> l, s);
+            conv_fwd(dn, li, act(dn, dn->u[l]), act(dn, dn->b[l]), l, false, s);
+        }
         conv_fwd(dn, li + 1, act(dn, dn->b[l]), act(dn, dn->d[l]), l, false, s);
     }
     conv_fwd(dn, kLayers - 1, act(dn, dn->d[0]), dn->out_f32.as<float>(), 0, true, s);
@@ -444,11 +476,12 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *dn, const vvpt_deno
 
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *dn, int kind)
 {
-    if (!dn || kind < VVPT_DENOISER_TCGEN05 || kind > VVPT_DENOISER_TCGEN05_PERSISTENT)
+    if (!dn || kind < VVPT_DENOISER_TCGEN05 || kind > VVPT_DENOISER_TCGEN05_UNFUSED)
         return VVPT_ERR_INVALID_ARG;
     dn->mma_sync = kind == VVPT_DENOISER_MMA_SYNC;
     dn->conv_kind = kind == VVPT_DENOISER_TCGEN05_TILES        ? vvdn::kConvTiles
                     : kind == VVPT_DENOISER_TCGEN05_PERSISTENT ? vvdn::kConvPersistent
+                    : kind == VVPT_DENOISER_TCGEN05_UNFUSED    ? vvdn::kConvNoFusion
                                                                : vvdn::kConvAuto;
     return VVPT_OK;
 }
@@ -467,7 +500,7 @@ VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *dn, const float *radianc
     if ((st = ensure_shape(dn, 1, (int)height, (int)width, false)) != VVPT_OK)
         return st;
     cudaStream_t s = vv_stream(ctx);
-    forward(dn, radiance, albedo, normal, s);
+    forward(dn, radiance, albedo, normal, s, true);
     vvdn::unpack_output(dn->out_f32.as<float>(), kOutCh, out, (int)(width * height), s);
     VV_CUDA(cudaGetLastError(), "denoiser kernels");
     return check_device_status(dn, s);

@@ -988,15 +988,17 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
 }
 
-// 192 threads: warps 0-3 drain accumulators (TMEM lane quarter = warp),
-// warp 4 loads halo rows by TMA, warp 5 issues the MMAs. The roles run
-// ahead of each other as far as the ring (`ring` halo-row slots) and the two
-// accumulators allow, synchronised only by mbarriers:
-//   full[s]   TMA bytes of the halo row in slot s landed (producer -> MMA)
+// 224 threads: warps 0-3 drain accumulators (TMEM lane quarter = warp),
+// warp 4 loads halo rows by TMA, warp 5 issues the MMAs, warp 6 fills the
+// upsampled channels of a fused upsample + concat input (a.coarse). The roles
+// run ahead of each other as far as the ring (`ring` halo-row slots) and the
+// two accumulators allow, synchronised only by mbarriers:
+//   full[s]   the halo row in slot s is complete: TMA bytes landed (producer)
+//             and, fused, the upsampled channels stored (warp 6) -> MMA
 //   empty[s]  the MMAs that read slot s completed (MMA commit -> producer)
 //   acc_full[b]  row accumulator b is complete (MMA commit -> drain)
 //   acc_empty[b] the four drain warps have read accumulator b (drain -> MMA)
-constexpr int kStThreads = 192;
+constexpr int kStThreads = 224;
 
 __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap,
                                                               int ncols, int nacc, int ring, int segs, int seg_rows,
@@ -1021,9 +1023,10 @@ __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const 
     uint8_t *w_ptr = smem_raw + (w_base - raw);
     const volatile int *abort_v = &abort_flag;
 
+    const int CG = a.cc >> 3;  // channel groups filled by warp 6 (upsampled coarse input)
     if (tid == 0) {
         for (int r = 0; r < ring; r++) {
-            mbar_init(&full[r], 1);
+            mbar_init(&full[r], CG ? 2 : 1);
             mbar_init(&empty[r], 1);
         }
         for (int k = 0; k < 2; k++) {
@@ -1052,11 +1055,87 @@ __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const 
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_holder;
 
-    if (warp == 4) {
-        // ---- producer: one TMA row (KC boxes of 8 channels x 130 pixels) per halo row
+    if (warp == 6) {
+        // ---- upsampled channels of a fused concat input: fine pixel x of
+        // halo row y reads coarse pixel (x >> 1, y >> 1). 16-byte cp.async
+        // copies (consecutive lanes on consecutive channel groups of a coarse
+        // pixel), one commit group per row; a row is published (fence to the
+        // async proxy, arrive on its full barrier) once `lag` newer rows are
+        // in flight, lag <= ring - 3 so the MMA warp can always release the
+        // slot this warp waits for.
+        if (CG) {
+            const int hc = a.h >> 1, wc = a.wd >> 1;
+            const int npc = kStHaloPx * CG, dp = 32 / CG, dg = 32 % CG;
+            const int lag = min(2, ring - 3);
+            int slot = 0, phase = 0, pub_slot = 0, pending = 0;
+            auto publish = [&]() {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    mbar_arrive(smem_addr(&full[pub_slot]));
+                pub_slot = pub_slot + 1 == ring ? 0 : pub_slot + 1;
+                pending--;
+            };
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                const int sg = u % segs, tx = (u / segs) % tiles_x, nb = u / (segs * tiles_x);
+                const int x0 = tx * kTcM, ya = sg * seg_rows;
+                const int nout = min(a.h, ya + seg_rows) - ya;
+                if (nout <= 0)
+                    continue;
+                for (int h = 0; h < nout + 2 && ok; h++) {
+                    bool w = true;
+                    if (lane == 0)
+                        w = mbar_wait_role(smem_addr(&empty[slot]), (uint32_t)(phase ^ 1), abort_v);
+                    ok = __shfl_sync(0xffffffffu, w, 0);
+                    if (!ok)
+                        break;
+                    const int yy = ya - 1 + h;
+                    const bool row_ok = yy >= 0 && yy < a.h;
+                    const bf16 *crow = a.coarse + ((long)nb * hc + (row_ok ? yy >> 1 : 0)) * wc * a.cc;
+                    uint8_t *dst = smem_raw + (ring_base - raw) + slot * slot_bytes;
+                    int pp = lane / CG, g = lane - (lane / CG) * CG;
+                    for (int idx = lane; idx < npc; idx += 32) {
+                        const int xx = x0 - 1 + pp;
+                        const bool in = row_ok && xx >= 0 && xx < a.wd;
+                        cp_async16(dst + g * kStKCBytes + pp * 16, in ? crow + (long)(xx >> 1) * a.cc + 8 * g : a.coarse,
+                                   in);
+                        g += dg;
+                        pp += dp;
+                        if (g >= CG) {
+                            g -= CG;
+                            pp++;
+                        }
+                    }
+                    cp_async_commit();
+                    pending++;
+                    if (++slot == ring) {
+                        slot = 0;
+                        phase ^= 1;
+                    }
+                    if (pending > lag) {
+                        if (lag <= 0)
+                            cp_async_wait<0>();
+                        else if (lag == 1)
+                            cp_async_wait<1>();
+                        else
+                            cp_async_wait<2>();
+                        publish();
+                    }
+                }
+            }
+            cp_async_wait<0>();
+            while (pending > 0)
+                publish();
+            if (!ok)
+                abort_flag = 1;
+        }
+    } else if (warp == 4) {
+        // ---- producer: one TMA row (the KC - CG boxes of 8 channels x 130
+        // pixels of `in`) per halo row
         if (lane == 0) {
             const uint64_t tmap_ptr = reinterpret_cast<uint64_t>(&tmap);
-            const uint32_t row_tx = (uint32_t)(KC * kStHaloPx * 16);
+            const uint32_t row_tx = (uint32_t)((KC - CG) * kStHaloPx * 16);
             int slot = 0, phase = 0, issued = 0;
             int last_phase[kStMaxRing];
             for (int r = 0; r < kStMaxRing; r++)
@@ -1076,10 +1155,11 @@ __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const 
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(row_tx)
                                  : "memory");
                     const uint32_t dst = ring_base + (uint32_t)(slot * slot_bytes);
-                    for (int kc = 0; kc < KC; kc++)
+                    for (int kc = CG; kc < KC; kc++)
                         asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
                                      "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst + (uint32_t)(kc * kStKCBytes)),
-                                     "l"(tmap_ptr), "r"(8 * kc), "r"(x0 - 1), "r"(ya - 1 + h), "r"(nb), "r"(bar)
+                                     "l"(tmap_ptr), "r"(8 * (kc - CG)), "r"(x0 - 1), "r"(ya - 1 + h), "r"(nb),
+                                     "r"(bar)
                                      : "memory");
                     last_phase[slot] = phase;
                     issued++;
@@ -1245,7 +1325,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 }
 
 struct StripPlan {
-    int ring = 0, smem = 0, grid = 0, segs = 0, seg_rows = 0, ncols = 0, nacc = 1;
+    int ring = 0, smem = 0, grid = 0, segs = 0, seg_rows = 0, ncols = 0, nacc = 1, per_sm = 1;
 };
 
 // Occupancy first (up to 4 CTAs per SM, bounded by shared memory and by the
@@ -1255,6 +1335,8 @@ struct StripPlan {
 bool plan_strip(const ConvArgs &a, StripPlan &pl)
 {
     if (a.cin % 16 || a.cin < 16 || a.cout > 256 || a.cout < 1 || (reinterpret_cast<uintptr_t>(a.in) & 15))
+        return false;
+    if (a.cc && (a.cc % 8 || a.cc >= a.cin || a.h % 2 || a.wd % 2 || (reinterpret_cast<uintptr_t>(a.coarse) & 15)))
         return false;
     static int nsm = 0, sm_smem = 0, optin = 0, reserved = 0;
     if (!nsm) {
@@ -1304,18 +1386,20 @@ bool plan_strip(const ConvArgs &a, StripPlan &pl)
         pl.seg_rows = seg_rows;
         pl.ncols = tcols;
         pl.nacc = nacc;
+        pl.per_sm = c;
         pl.grid = (int)std::min<long>(cols * segs, ctas);
         return true;
     }
     return false;
 }
 
-// rank-4 map over the NHWC input {C, W, H, N}; box = 8 channels x 130 pixels
+// rank-4 map over the NHWC input {C, W, H, N} (the cin - cc channels of `in`);
+// box = 8 channels x 130 pixels
 bool encode_input_map(const ConvArgs &a, CUtensorMap &m)
 {
-    const cuuint64_t dims[4] = {(cuuint64_t)a.cin, (cuuint64_t)a.wd, (cuuint64_t)a.h, (cuuint64_t)a.n};
-    const cuuint64_t strides[3] = {(cuuint64_t)a.cin * 2, (cuuint64_t)a.wd * a.cin * 2,
-                                   (cuuint64_t)a.h * a.wd * a.cin * 2};
+    const int c = a.cin - a.cc;
+    const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)a.wd, (cuuint64_t)a.h, (cuuint64_t)a.n};
+    const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)a.wd * c * 2, (cuuint64_t)a.h * a.wd * c * 2};
     const cuuint32_t box[4] = {8, (cuuint32_t)kStHaloPx, 1, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     return tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(a.in), dims, strides, box,
@@ -1325,25 +1409,48 @@ bool encode_input_map(const ConvArgs &a, CUtensorMap &m)
 
 }  // namespace
 
-void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
+namespace {
+
+// The strip kernel for `a` when it takes the layer; false (nothing launched)
+// otherwise. A fused upsample + concat input is taken only where two or more
+// CTAs share an SM: the warp that copies the upsampled channels keeps up
+// there, while with one CTA per SM (level 1, 219 KB of weights and ring) the
+// unfused path measured faster (0.47 vs 0.57 ms at 1920 x 1080).
+bool launch_strip(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
 {
-    const long P = (long)a.n * a.h * a.wd;
     StripPlan pl;
     CUtensorMap tmap;
-    if (err && kind != kConvTiles && plan_strip(a, pl) && encode_input_map(a, tmap)) {
-        if (kind == kConvPersistent)
-            pl.grid = std::min(pl.grid, 16);
-        static int attr_smem = 0;
-        if (pl.smem > attr_smem) {
-            cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem);
-            cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
-            attr_smem = pl.smem;
-        }
-        k_conv3x3_strip<<<pl.grid, kStThreads, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs,
-                                                             pl.seg_rows, err);
-        return;
+    if (!err || kind == kConvTiles || !plan_strip(a, pl) || (a.cc && pl.per_sm < 2) || !encode_input_map(a, tmap))
+        return false;
+    if (kind == kConvPersistent)
+        pl.grid = std::min(pl.grid, 16);
+    static int attr_smem = 0;
+    if (pl.smem > attr_smem) {
+        cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem);
+        cudaFuncSetAttribute(k_conv3x3_strip, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        attr_smem = pl.smem;
     }
+    k_conv3x3_strip<<<pl.grid, kStThreads, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs, pl.seg_rows,
+                                                         err);
+    return true;
+}
+
+}  // namespace
+
+bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
+{
+    return kind != kConvNoFusion && a.coarse && a.cc > 0 && launch_strip(a, s, err, kind);
+}
+
+void conv3x3(const ConvArgs &a_in, cudaStream_t s, uint32_t *err, ConvKernels kind)
+{
+    ConvArgs a = a_in;
+    a.coarse = nullptr;
+    a.cc = 0;
+    const long P = (long)a.n * a.h * a.wd;
+    if (launch_strip(a, s, err, kind))
+        return;
     if (err && a.cout <= 256) {
         static bool attr_set = false;
         if (!attr_set) {

@@ -24,12 +24,18 @@ struct ConvArgs {
     int relu;
     const bf16 *mask;  // [P][cout] or null: output *= (mask > 0)
     int n, h, wd;      // P = n * h * wd
+    // Fused nearest-upsample + concat input (conv3x3_concat): channels
+    // [0, cc) come from `coarse` ([n][h/2][wd/2][cc]) upsampled by 2, channels
+    // [cc, cin) from `in` ([P][cin - cc]). cc = 0: `in` holds all cin.
+    const bf16 *coarse;
+    int cc;
 };
 
 enum ConvKernels {
     kConvAuto = 0,       // tcgen05: strip kernel where the weights fit, else per-tile
     kConvTiles = 1,      // tcgen05 per-tile kernels only
     kConvPersistent = 2, // strip kernel on a grid of 16 CTAs (several segments each)
+    kConvNoFusion = 3,   // as kConvAuto, but no fused upsample + concat inputs
 };
 
 // out = act(conv3x3(in, w) + bias) (zero padding); with transformed weights
@@ -38,6 +44,11 @@ enum ConvKernels {
 // `err` receives a status bit if one of its waits timed out; with err null
 // it runs the warp-level mma.sync kernel.
 void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind = kConvAuto);
+
+// The same convolution over concat(upsample2(coarse), in) without writing the
+// concatenated tensor (a.coarse, a.cc set): runs only on the strip kernel and
+// returns false, launching nothing, when that kernel does not take the layer.
+bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind = kConvAuto);
 
 // dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
 // dbias[co] += sum_p dout[p][co] (dbias may be null).
