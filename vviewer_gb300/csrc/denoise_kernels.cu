@@ -44,18 +44,6 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1
                  : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// 16 bf16 (two 16-byte vectors) or zeros
-__device__ __forceinline__ void load16(const bf16 *src, bool ok, bf16 *dst)
-{
-    uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-    if (ok) {
-        v0 = *reinterpret_cast<const uint4 *>(src);
-        v1 = *reinterpret_cast<const uint4 *>(src + 8);
-    }
-    *reinterpret_cast<uint4 *>(dst) = v0;
-    *reinterpret_cast<uint4 *>(dst + 8) = v1;
-}
-
 // Asynchronous 16-byte global -> shared copy; src_bytes = 0 writes zeros
 // (padding, channels past cin, rows past cout).
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid)
@@ -208,33 +196,42 @@ __global__ void __launch_bounds__(256) k_conv3x3(ConvArgs a)
         }
 }
 
-// Weight gradient for one tap: block tile 64 output channels x 64 input
-// channels, K = a slice of pixels in steps of 32. Warp w owns output
-// channels [16w, 16w + 16). Partial sums are added to dw with atomics.
-constexpr int kWgK = 32;
+// Weight gradient for one tap: block tile BM output channels x 64 input
+// channels, K = a slice of pixels in steps of 32 through a 3-stage cp.async
+// pipeline. BM = 64: warp w owns output channels [16w, 16w + 16) and all 64
+// input channels; BM = 32 (layers of at most 32 output channels): warp w
+// owns output channels 16 (w & 1) and input channels 32 (w >> 1). Partial
+// sums are added to dw with atomics.
+constexpr int kWgK = 32, kWgStages = 3;
+template <int BM>
 __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const bf16 *__restrict__ dout, int cout,
                                                        const bf16 *__restrict__ in, int cin, int n, int h, int w,
                                                        float *dw, long slice)
 {
-    __shared__ __align__(16) bf16 Ds[kWgK][kTileC + 8]; // [pixel][cout]
-    __shared__ __align__(16) bf16 Xs[kWgK][kTileC + 8]; // [pixel][cin]
+    constexpr int NT = BM == 64 ? 8 : 4; // n-tiles of 8 input channels per warp
+    __shared__ __align__(16) bf16 Ds[kWgStages][kWgK][kTileC + 8]; // [pixel][cout]
+    __shared__ __align__(16) bf16 Xs[kWgStages][kWgK][kTileC + 8]; // [pixel][cin]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tap = blockIdx.y % 9;
     const int tiles_ci = (cin + kTileC - 1) / kTileC;
     const int ct = blockIdx.y / 9;
-    const int co0 = (ct / tiles_ci) * kTileC, ci0 = (ct % tiles_ci) * kTileC;
+    const int co0 = (ct / tiles_ci) * BM, ci0 = (ct % tiles_ci) * kTileC;
     const long P = (long)n * h * w;
     const long pbeg = (long)blockIdx.x * slice, pend = min(P, pbeg + slice);
     const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int wm = BM == 64 ? warp * 16 : (warp & 1) * 16; // warp's output-channel offset in the tile
+    const int wn = BM == 64 ? 0 : (warp >> 1) * 32;        // warp's input-channel offset in the tile
     // load mapping: row = tid / 4 (pixel), group = (tid % 4) * 16 channels
     const int lr = tid >> 2, lg = (tid & 3) * 16;
-    float acc[8][4];
+    float acc[NT][4];
 #pragma unroll
-    for (int j = 0; j < 8; j++)
+    for (int j = 0; j < NT; j++)
         acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    for (long pb = pbeg; pb < pend; pb += kWgK) {
-        const long p = pb + lr;
-        bool ok = p < pend;
+    const int nsteps = (int)((pend - pbeg + kWgK - 1) / kWgK);
+    auto load = [&](int step) {
+        const int st = step % kWgStages;
+        const long p = pbeg + (long)step * kWgK + lr;
+        const bool ok = p < pend;
         int pn = 0, py = 0, px = 0;
         if (ok) {
             pn = (int)(p / ((long)h * w));
@@ -243,38 +240,57 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const bf16 *__restrict__ 
             px = rem - py * w;
         }
         const int co = co0 + lg, ci = ci0 + lg;
-        load16(dout + p * cout + co, ok && co < cout, &Ds[lr][lg]);
+        const bool dok = ok && co < cout && lg < BM;
+        const bf16 *ds = dok ? dout + p * cout + co : dout;
+        cp_async16(&Ds[st][lr][lg], ds, dok);
+        cp_async16(&Ds[st][lr][lg + 8], dok ? ds + 8 : dout, dok);
         const int yy = py + dy, xx = px + dx;
         const bool xok = ok && yy >= 0 && yy < h && xx >= 0 && xx < w && ci < cin;
-        load16(in + (((long)pn * h + yy) * w + xx) * cin + ci, xok, &Xs[lr][lg]);
+        const bf16 *xs = xok ? in + (((long)pn * h + yy) * w + xx) * cin + ci : in;
+        cp_async16(&Xs[st][lr][lg], xs, xok);
+        cp_async16(&Xs[st][lr][lg + 8], xok ? xs + 8 : in, xok);
+    };
+    for (int st = 0; st < kWgStages - 1; st++) {
+        if (st < nsteps)
+            load(st);
+        cp_async_commit();
+    }
+    for (int step = 0; step < nsteps; step++) {
+        cp_async_wait<kWgStages - 2>();
         __syncthreads();
+        const int st = step % kWgStages;
 #pragma unroll
         for (int ks = 0; ks < kWgK; ks += 16) {
             // A[m = cout][k = pixel] from Ds[k][m] (transposed load)
             uint32_t a0, a1, a2, a3;
-            ldsm_x4_t(smem_addr(&Ds[ks + (lane & 7) + ((lane >> 4) << 3)][warp * 16 + ((lane >> 3) & 1) * 8]), a0, a1,
+            ldsm_x4_t(smem_addr(&Ds[st][ks + (lane & 7) + ((lane >> 4) << 3)][wm + ((lane >> 3) & 1) * 8]), a0, a1,
                       a2, a3);
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < NT / 2; j++) {
                 // B[k = pixel][n = cin] from Xs[k][n] (transposed load): two n-tiles
                 uint32_t b0, b1, b2, b3;
-                ldsm_x4_t(smem_addr(&Xs[ks + (lane & 7) + ((lane >> 3) & 1) * 8][16 * j + (lane >> 4) * 8]), b0, b1,
-                          b2, b3);
+                ldsm_x4_t(smem_addr(&Xs[st][ks + (lane & 7) + ((lane >> 3) & 1) * 8][wn + 16 * j + (lane >> 4) * 8]),
+                          b0, b1, b2, b3);
                 mma_bf16(acc[2 * j], a0, a1, a2, a3, b0, b1);
                 mma_bf16(acc[2 * j + 1], a0, a1, a2, a3, b2, b3);
             }
         }
-        __syncthreads();
+        // the stage refilled next was read two steps ago; the barrier above
+        // ordered those reads
+        if (step + kWgStages - 1 < nsteps)
+            load(step + kWgStages - 1);
+        cp_async_commit();
     }
+    cp_async_wait<0>();
     const int g = lane >> 2, t = lane & 3;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        const int co = co0 + warp * 16 + g + half * 8;
+        const int co = co0 + wm + g + half * 8;
         if (co >= cout)
             continue;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int ci = ci0 + 8 * j + 2 * t;
+        for (int j = 0; j < NT; j++) {
+            const int ci = ci0 + wn + 8 * j + 2 * t;
             if (ci >= cin)
                 continue;
             float *d = dw + ((long)co * 9 + tap) * cin + ci;
@@ -284,16 +300,63 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const bf16 *__restrict__ 
     }
 }
 
-__global__ void k_bias_grad(const bf16 *dout, int cout, long P, float *dbias)
+// The layout kernels below move 8 channels (16 bytes) per thread: channel
+// counts are multiples of 8, so every access is one aligned 128-bit load or
+// store and a warp covers 512 consecutive bytes. Index arithmetic is 32-bit
+// (element counts stay below 2^31; the host checks).
+__device__ __forceinline__ void unpack8(const uint4 &v, float (&f)[8])
 {
-    // one block per 8 channels-group x pixel slice; simple strided sums
-    const int c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= cout)
-        return;
-    float s = 0.0f;
-    for (long p = blockIdx.x; p < P; p += gridDim.x)
-        s += __bfloat162float(dout[p * cout + c]);
-    atomicAdd(dbias + c, s);
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float2 t = __bfloat1622float2(h[k]);
+        f[2 * k] = t.x;
+        f[2 * k + 1] = t.y;
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8])
+{
+    uint4 v;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    return v;
+}
+
+__device__ __forceinline__ uint4 ld16(const bf16 *p) { return __ldg(reinterpret_cast<const uint4 *>(p)); }
+__device__ __forceinline__ void st16(bf16 *p, const uint4 &v) { *reinterpret_cast<uint4 *>(p) = v; }
+
+// dbias[c] += sum_p dout[p][c]: a thread sums 8 channels (one 16-byte load
+// per pixel) over a strided set of pixels, the block reduces its pixel lanes
+// in shared memory and adds one value per channel.
+constexpr int kBiasThreads = 256;
+__global__ void __launch_bounds__(kBiasThreads) k_bias_grad(const bf16 *dout, int cout, long P, float *dbias)
+{
+    __shared__ float red[kBiasThreads * 8];
+    const int G = cout >> 3, lanes = kBiasThreads / G;
+    const int g = threadIdx.x % G, r = threadIdx.x / G;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (r < lanes) {
+        for (long p = (long)blockIdx.x * lanes + r; p < P; p += (long)gridDim.x * lanes) {
+            float v[8];
+            unpack8(ld16(dout + p * cout + 8 * g), v);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                acc[k] += v[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        red[threadIdx.x * 8 + k] = acc[k];
+    __syncthreads();
+    for (int c = threadIdx.x; c < cout; c += kBiasThreads) {
+        float sum = 0.0f;
+        for (int q = 0; q < lanes; q++)
+            sum += red[(q * G + (c >> 3)) * 8 + (c & 7)];
+        atomicAdd(dbias + c, sum);
+    }
 }
 
 __global__ void k_transform_weights(const bf16 *w, bf16 *wt, int cout, int cin)
@@ -345,34 +408,6 @@ __global__ void k_pack_target(const float4 *t, float *t3, int npix)
         t3[3 * p + 2] = log1pf(fmaxf(v.z, 0.0f));
     }
 }
-
-// The layout kernels below move 8 channels (16 bytes) per thread: channel
-// counts are multiples of 8, so every access is one aligned 128-bit load or
-// store and a warp covers 512 consecutive bytes. Index arithmetic is 32-bit
-// (element counts stay below 2^31; the host checks).
-__device__ __forceinline__ void unpack8(const uint4 &v, float (&f)[8])
-{
-    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const float2 t = __bfloat1622float2(h[k]);
-        f[2 * k] = t.x;
-        f[2 * k + 1] = t.y;
-    }
-}
-
-__device__ __forceinline__ uint4 pack8(const float (&f)[8])
-{
-    uint4 v;
-    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-        h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
-    return v;
-}
-
-__device__ __forceinline__ uint4 ld16(const bf16 *p) { return __ldg(reinterpret_cast<const uint4 *>(p)); }
-__device__ __forceinline__ void st16(bf16 *p, const uint4 &v) { *reinterpret_cast<uint4 *>(p) = v; }
 
 __global__ void k_avgpool2(const bf16 *in, bf16 *out, int n, int h, int w, int c)
 {
@@ -1496,17 +1531,23 @@ void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, i
                    cudaStream_t s)
 {
     const long P = (long)n * h * w;
-    const int tiles = ((cout + kTileC - 1) / kTileC) * ((cin + kTileC - 1) / kTileC);
+    const int bm = cout <= 32 ? 32 : 64;
+    const int tiles = ((cout + bm - 1) / bm) * ((cin + kTileC - 1) / kTileC);
     // about 4 blocks per SM over all taps and tiles
     long slices = std::max<long>(1, (152L * 4) / (9L * tiles));
     long slice = (P + slices - 1) / slices;
     slice = std::max<long>(kWgK, (slice + kWgK - 1) / kWgK * kWgK);
     slices = (P + slice - 1) / slice;
     dim3 grid((unsigned)slices, (unsigned)(9 * tiles));
-    k_conv3x3_wgrad<<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
+    if (bm == 32)
+        k_conv3x3_wgrad<32><<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
+    else
+        k_conv3x3_wgrad<64><<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
     if (dbias) {
-        dim3 gb((unsigned)std::min<long>(P, 1024), (unsigned)((cout + 127) / 128));
-        k_bias_grad<<<gb, 128, 0, s>>>(dout, cout, P, dbias);
+        // channel counts are multiples of 8 up to 256: 1-32 groups per pixel lane
+        const int lanes = kBiasThreads / (cout / 8);
+        const long blocks = std::min<long>(152L * 4, (P + 16L * lanes - 1) / (16L * lanes));
+        k_bias_grad<<<(unsigned)std::max<long>(blocks, 1), kBiasThreads, 0, s>>>(dout, cout, P, dbias);
     }
 }
 
