@@ -1533,8 +1533,9 @@ void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, i
     const long P = (long)n * h * w;
     const int bm = cout <= 32 ? 32 : 64;
     const int tiles = ((cout + bm - 1) / bm) * ((cin + kTileC - 1) / kTileC);
-    // about 4 blocks per SM over all taps and tiles
-    long slices = std::max<long>(1, (152L * 4) / (9L * tiles));
+    // about 8 blocks per SM over all taps and tiles (each block's K loop is
+    // latency-bound; more blocks keep more copies and MMAs in flight)
+    long slices = std::max<long>(1, (152L * 8) / (9L * tiles));
     long slice = (P + slices - 1) / slices;
     slice = std::max<long>(kWgK, (slice + kWgK - 1) / kWgK * kWgK);
     slices = (P + slice - 1) / slice;
