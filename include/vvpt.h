@@ -546,14 +546,17 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *denoiser,
  * TCGEN05_PERSISTENT: the strip kernel on a small grid, so that every CTA
  * walks several row segments. TCGEN05_UNFUSED: as TCGEN05, but inference
  * writes the upsample + concat tensor instead of reading both halves in the
- * convolution. All accumulate in FP32; the last four serve as cross-checks
- * of the first. */
+ * convolution. TCGEN05_WGRAD: as TCGEN05, and the weight gradients on the
+ * tcgen05 tensor cores as well (by default they run on the mma.sync kernel,
+ * which is faster for these channel counts). All accumulate in FP32; the
+ * variants serve as cross-checks of the first. */
 enum {
     VVPT_DENOISER_TCGEN05 = 0,
     VVPT_DENOISER_MMA_SYNC = 1,
     VVPT_DENOISER_TCGEN05_TILES = 2,
     VVPT_DENOISER_TCGEN05_PERSISTENT = 3,
-    VVPT_DENOISER_TCGEN05_UNFUSED = 4
+    VVPT_DENOISER_TCGEN05_UNFUSED = 4,
+    VVPT_DENOISER_TCGEN05_WGRAD = 5
 };
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *denoiser, int kind);
 /* Denoises one image: out = exp(network(log1p radiance, albedo, normal)) - 1. */

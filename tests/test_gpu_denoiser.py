@@ -105,7 +105,8 @@ def test_training_on_tracer_pairs_beats_the_noisy_render(ctx):
     dn.close()
 
 
-@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_tiles", "tcgen05_persistent", "tcgen05_unfused"])
+@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_tiles", "tcgen05_persistent", "tcgen05_unfused",
+                                  "tcgen05_wgrad"])
 @pytest.mark.parametrize("n,h,w", [(2, 64, 48), (1, 48, 272)])
 def test_tcgen05_and_mma_sync_kernels_agree(ctx, kind, n, h, w):
     """The tcgen05 convolutions (TMEM accumulators) against the warp-level

@@ -236,7 +236,8 @@ void conv_wgrad(vvpt_denoiser *dn, int li, const bf16 *dout, const bf16 *in, int
 {
     const Layer &L = dn->layers[li];
     vvdn::conv3x3_wgrad(dout, L.cout, in, L.cin, dn->n, dn->h >> level, dn->w >> level,
-                        dn->grads.as<float>() + L.w_off, dn->grads.as<float>() + L.b_off, s);
+                        dn->grads.as<float>() + L.w_off, dn->grads.as<float>() + L.b_off, s,
+                        dn->conv_kind == vvdn::kConvWgradTc ? dn->err.as<uint32_t>() : nullptr);
 }
 
 // inference (fuse_concat): the decoder's first convolution of a level reads
@@ -476,12 +477,13 @@ VVPT_API vvpt_status vvpt_denoiser_train_step(vvpt_denoiser *dn, const vvpt_deno
 
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *dn, int kind)
 {
-    if (!dn || kind < VVPT_DENOISER_TCGEN05 || kind > VVPT_DENOISER_TCGEN05_UNFUSED)
+    if (!dn || kind < VVPT_DENOISER_TCGEN05 || kind > VVPT_DENOISER_TCGEN05_WGRAD)
         return VVPT_ERR_INVALID_ARG;
     dn->mma_sync = kind == VVPT_DENOISER_MMA_SYNC;
     dn->conv_kind = kind == VVPT_DENOISER_TCGEN05_TILES        ? vvdn::kConvTiles
                     : kind == VVPT_DENOISER_TCGEN05_PERSISTENT ? vvdn::kConvPersistent
                     : kind == VVPT_DENOISER_TCGEN05_UNFUSED    ? vvdn::kConvNoFusion
+                    : kind == VVPT_DENOISER_TCGEN05_WGRAD      ? vvdn::kConvWgradTc
                                                                : vvdn::kConvAuto;
     return VVPT_OK;
 }

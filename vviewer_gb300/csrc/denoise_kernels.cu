@@ -1341,6 +1341,161 @@ __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const 
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
+// Weight gradient on the tcgen05 tensor cores, one tap per CTA:
+// dW_tap[co][ci] = sum_p dout[p][co] * in[p shifted by the tap][ci], a GEMM
+// with M = 128 output channels (zero rows past cout), N = up to 128 input
+// channels, K = a slice of pixels. Both operands are MN-major as they lie in
+// NHWC memory (8 consecutive channels of a pixel are 16 contiguous bytes): a
+// K chunk of 64 pixels is staged as [channel group][pixel][16 B], i.e. core
+// matrices of 8 channels x 8 pixels, K groups 128 B apart (LBO) and channel
+// groups 64 x 16 B apart (SBO). Three stages of cp.async copies; thread 0
+// issues four m128 nN k16 MMAs per chunk and commits each stage to its
+// mbarrier, refills wait for the MMAs of the stage's previous chunk. The
+// accumulator (one TMEM column per input channel, lane = output channel) is
+// added to dw with atomics. Waits are bounded as in the other tcgen05
+// kernels.
+constexpr int kWtK = 64, kWtStages = 3, kWtM = 128;
+
+__host__ __device__ constexpr int wt_stage_bytes(int N) { return kWtK * (kWtM + N) * 2; }
+
+__global__ void __launch_bounds__(128) k_conv3x3_wgrad_tc(const bf16 *__restrict__ dout, int cout,
+                                                          const bf16 *__restrict__ in, int cin, int n, int h, int w,
+                                                          float *dw, long slice, int ntile, int ncols, uint32_t *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint32_t tmem_holder;
+    __shared__ __align__(8) uint64_t mbar[kWtStages];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tap = blockIdx.y % 9;
+    const int tiles_ci = (cin + ntile - 1) / ntile;
+    const int ct = blockIdx.y / 9;
+    const int co0 = (ct / tiles_ci) * kWtM, ci0 = (ct % tiles_ci) * ntile;
+    const int N = min(ntile, (cin - ci0 + 15) & ~15);
+    const long P = (long)n * h * w;
+    const long pbeg = (long)blockIdx.x * slice, pend = min(P, pbeg + slice);
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int nchunks = (int)((pend - pbeg + kWtK - 1) / kWtK);
+    const int stage_bytes = wt_stage_bytes(ntile);
+    const uint32_t sbase = smem_addr(smem);
+
+    if (tid == 0) {
+        for (int st = 0; st < kWtStages; st++)
+            mbar_init(&mbar[st], 1);
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_holder)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_holder;
+    // D f32, A/B bf16, A and B MN-major (bits 15, 16), N >> 3, M >> 4
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kWtM >> 4) << 24);
+
+    auto load_chunk = [&](int c) {
+        uint8_t *a_s = smem + (c % kWtStages) * stage_bytes;
+        uint8_t *b_s = a_s + kWtK * kWtM * 2;
+        const long pb = pbeg + (long)c * kWtK;
+        // A: 64 pixels x 16 groups of 8 output channels
+        for (int i = tid; i < kWtK * (kWtM / 8); i += 128) {
+            const int px = i % kWtK, g = i / kWtK;
+            const long p = pb + px;
+            const int co = co0 + 8 * g;
+            const bool ok = p < pend && co < cout;
+            cp_async16(a_s + g * (kWtK * 16) + px * 16, ok ? dout + p * cout + co : dout, ok);
+        }
+        // B: 64 pixels x N / 8 groups of input channels at the tap's offset
+        for (int i = tid; i < kWtK * (N / 8); i += 128) {
+            const int px = i % kWtK, g = i / kWtK;
+            const long p = pb + px;
+            const int ci = ci0 + 8 * g;
+            bool ok = p < pend && ci < cin;
+            long q = 0;
+            if (ok) {
+                const int pn = (int)(p / ((long)h * w));
+                const int rem = (int)(p - (long)pn * h * w);
+                const int yy = rem / w + dy, xx = rem % w + dx;
+                ok = yy >= 0 && yy < h && xx >= 0 && xx < w;
+                q = ((long)pn * h + yy) * w + xx;
+            }
+            cp_async16(b_s + g * (kWtK * 16) + px * 16, ok ? in + q * cin + ci : in, ok);
+        }
+    };
+
+    for (int st = 0; st < kWtStages - 1; st++) {
+        if (st < nchunks)
+            load_chunk(st);
+        cp_async_commit();
+    }
+    for (int c = 0; c < nchunks; c++) {
+        cp_async_wait<kWtStages - 2>(); // this thread's copies of chunk c landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (abort_flag)
+            break;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a_addr = sbase + (uint32_t)((c % kWtStages) * stage_bytes);
+            const uint32_t b_addr = a_addr + (uint32_t)(kWtK * kWtM * 2);
+#pragma unroll
+            for (int j = 0; j < kWtK / 16; j++) {
+                // K step j: pixels 16 j .. 16 j + 15 = two K groups of 8
+                const uint64_t ad = umma_desc(a_addr + (uint32_t)(j * 256), 128, kWtK * 16);
+                const uint64_t bd = umma_desc(b_addr + (uint32_t)(j * 256), 128, kWtK * 16);
+                const uint32_t accumulate = (c > 0 || j > 0) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                             "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+            }
+            umma_commit(smem_addr(&mbar[c % kWtStages]));
+        }
+        // chunk c + 2 reuses the stage of chunk c - 1
+        const int nx = c + kWtStages - 1;
+        if (nx < nchunks) {
+            if (c >= 1) {
+                const int prev = c - 1;
+                if (!mbar_wait(smem_addr(&mbar[prev % kWtStages]), (uint32_t)((prev / kWtStages) & 1)))
+                    atomicOr(&abort_flag, 1);
+            }
+            load_chunk(nx);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    if (!abort_flag && nchunks > 0) {
+        const int last = nchunks - 1;
+        if (!mbar_wait(smem_addr(&mbar[last % kWtStages]), (uint32_t)((last / kWtStages) & 1)))
+            atomicOr(&abort_flag, 1);
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!abort_flag && nchunks > 0) {
+        const int co = co0 + warp * 32 + lane;
+        for (int c = 0; c < N; c += 16) {
+            uint32_t r[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+            if (co >= cout)
+                continue;
+            float *d = dw + ((long)co * 9 + tap) * cin + ci0 + c;
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if (ci0 + c + k < cin)
+                    atomicAdd(d + k, __uint_as_float(r[k]));
+        }
+    } else if (abort_flag && tid == 0) {
+        atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
 }  // namespace
 
 namespace {
@@ -1528,7 +1683,42 @@ void conv3x3(const ConvArgs &a_in, cudaStream_t s, uint32_t *err, ConvKernels ki
 }
 
 void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw, float *dbias,
-                   cudaStream_t s)
+                   cudaStream_t s, uint32_t *err)
+{
+    const long P = (long)n * h * w;
+    if (err) {
+        // tcgen05: 128 output channels x up to 128 input channels per tap and slice
+        const int ntile = std::min(128, (cin + 15) & ~15);
+        int ncols = 32;
+        while (ncols < ntile)
+            ncols <<= 1;
+        const int tiles = ((cout + kWtM - 1) / kWtM) * ((cin + ntile - 1) / ntile);
+        long slices = std::max<long>(1, (152L * 4) / (9L * tiles));
+        long slice = (P + slices - 1) / slices;
+        slice = std::max<long>(kWtK, (slice + kWtK - 1) / kWtK * kWtK);
+        slices = (P + slice - 1) / slice;
+        const int smem = kWtStages * wt_stage_bytes(ntile);
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(k_conv3x3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kWtStages * wt_stage_bytes(128));
+            attr_set = true;
+        }
+        dim3 grid((unsigned)slices, (unsigned)(9 * tiles));
+        k_conv3x3_wgrad_tc<<<grid, 128, smem, s>>>(dout, cout, in, cin, n, h, w, dw, slice, ntile, ncols, err);
+    } else {
+        wgrad_mma_sync(dout, cout, in, cin, n, h, w, dw, s);
+    }
+    if (dbias) {
+        // channel counts are multiples of 8 up to 256: 1-32 groups per pixel lane
+        const int lanes = kBiasThreads / (cout / 8);
+        const long blocks = std::min<long>(152L * 4, (P + 16L * lanes - 1) / (16L * lanes));
+        k_bias_grad<<<(unsigned)std::max<long>(blocks, 1), kBiasThreads, 0, s>>>(dout, cout, P, dbias);
+    }
+}
+
+void wgrad_mma_sync(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw,
+                    cudaStream_t s)
 {
     const long P = (long)n * h * w;
     const int bm = cout <= 32 ? 32 : 64;
@@ -1544,12 +1734,6 @@ void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, i
         k_conv3x3_wgrad<32><<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
     else
         k_conv3x3_wgrad<64><<<grid, 128, 0, s>>>(dout, cout, in, cin, n, h, w, dw, slice);
-    if (dbias) {
-        // channel counts are multiples of 8 up to 256: 1-32 groups per pixel lane
-        const int lanes = kBiasThreads / (cout / 8);
-        const long blocks = std::min<long>(152L * 4, (P + 16L * lanes - 1) / (16L * lanes));
-        k_bias_grad<<<(unsigned)std::max<long>(blocks, 1), kBiasThreads, 0, s>>>(dout, cout, P, dbias);
-    }
 }
 
 void transform_weights(const bf16 *w, bf16 *wt, int cout, int cin, cudaStream_t s)

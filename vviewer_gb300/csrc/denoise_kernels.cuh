@@ -36,6 +36,7 @@ enum ConvKernels {
     kConvTiles = 1,      // tcgen05 per-tile kernels only
     kConvPersistent = 2, // strip kernel on a grid of 16 CTAs (several segments each)
     kConvNoFusion = 3,   // as kConvAuto, but no fused upsample + concat inputs
+    kConvWgradTc = 4,    // as kConvAuto, and the weight gradient on tcgen05 too
 };
 
 // out = act(conv3x3(in, w) + bias) (zero padding); with transformed weights
@@ -52,8 +53,14 @@ bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernel
 
 // dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
 // dbias[co] += sum_p dout[p][co] (dbias may be null).
+// With `err` set it runs on the tcgen05 tensor cores (err receives a status
+// bit if a wait timed out), with err null on the warp-level mma.sync kernel
+// (the faster of the two for this network: training step 3.2 vs 4.5 ms).
 void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw,
-                   float *dbias, cudaStream_t s);
+                   float *dbias, cudaStream_t s, uint32_t *err = nullptr);
+// the mma.sync weight gradient (dw only)
+void wgrad_mma_sync(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw,
+                    cudaStream_t s);
 
 // w_t[ci][8 - tap][co] = w[co][tap][ci]
 void transform_weights(const bf16 *w, bf16 *wt, int cout, int cin, cudaStream_t s);

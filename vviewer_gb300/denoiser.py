@@ -31,14 +31,16 @@ class Denoiser:
         except Exception:
             pass
 
-    KERNELS = {"tcgen05": 0, "mma_sync": 1, "tcgen05_tiles": 2, "tcgen05_persistent": 3, "tcgen05_unfused": 4}
+    KERNELS = {"tcgen05": 0, "mma_sync": 1, "tcgen05_tiles": 2, "tcgen05_persistent": 3, "tcgen05_unfused": 4,
+               "tcgen05_wgrad": 5}
 
     def set_kernels(self, kind: str) -> None:
         """Convolution kernels: 'tcgen05' (default: strip kernel where the
         weights fit in shared memory, per-tile kernels elsewhere),
         'mma_sync', 'tcgen05_tiles' (per-tile tcgen05 kernels only),
-        'tcgen05_persistent' (strip kernel on a 16-CTA grid) or
-        'tcgen05_unfused' (inference writes the upsample + concat tensor)."""
+        'tcgen05_persistent' (strip kernel on a 16-CTA grid),
+        'tcgen05_unfused' (inference writes the upsample + concat tensor) or
+        'tcgen05_wgrad' (weight gradients on tcgen05 as well)."""
         self.ctx.check(self.ctx.lib.vvpt_denoiser_set_kernels(self.handle, self.KERNELS[kind]))
 
     def params(self) -> np.ndarray:
