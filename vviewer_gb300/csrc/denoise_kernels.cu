@@ -1397,33 +1397,39 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad_tc(const bf16 *__restrict
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
                            ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kWtM >> 4) << 24);
 
+    // A rows past cout stay zero: cleared once, never loaded
+    const int ga = (min(cout - co0, kWtM) + 7) / 8; // A channel groups with data
+    for (int i = tid; i < kWtStages * (kWtM / 8 - ga) * kWtK; i += 128) {
+        const int st = i / ((kWtM / 8 - ga) * kWtK), r = i % ((kWtM / 8 - ga) * kWtK);
+        *reinterpret_cast<uint4 *>(smem + st * stage_bytes + (ga * kWtK + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    // thread -> one pixel of the chunk (its position decoded once) and every
+    // other channel group
+    const int lpx = tid & (kWtK - 1), lhalf = tid / kWtK;
     auto load_chunk = [&](int c) {
         uint8_t *a_s = smem + (c % kWtStages) * stage_bytes;
         uint8_t *b_s = a_s + kWtK * kWtM * 2;
-        const long pb = pbeg + (long)c * kWtK;
-        // A: 64 pixels x 16 groups of 8 output channels
-        for (int i = tid; i < kWtK * (kWtM / 8); i += 128) {
-            const int px = i % kWtK, g = i / kWtK;
-            const long p = pb + px;
-            const int co = co0 + 8 * g;
-            const bool ok = p < pend && co < cout;
-            cp_async16(a_s + g * (kWtK * 16) + px * 16, ok ? dout + p * cout + co : dout, ok);
+        const long p = pbeg + (long)c * kWtK + lpx;
+        const bool pok = p < pend;
+        bool xok = false;
+        long q = 0;
+        if (pok) {
+            const int pn = (int)(p / ((long)h * w));
+            const int rem = (int)(p - (long)pn * h * w);
+            const int y = rem / w;
+            const int yy = y + dy, xx = rem - y * w + dx;
+            xok = yy >= 0 && yy < h && xx >= 0 && xx < w;
+            q = ((long)pn * h + yy) * w + xx;
         }
-        // B: 64 pixels x N / 8 groups of input channels at the tap's offset
-        for (int i = tid; i < kWtK * (N / 8); i += 128) {
-            const int px = i % kWtK, g = i / kWtK;
-            const long p = pb + px;
+        for (int g = lhalf; g < ga; g += 2) {
+            const int co = co0 + 8 * g;
+            const bool ok = pok && co < cout;
+            cp_async16(a_s + g * (kWtK * 16) + lpx * 16, ok ? dout + p * cout + co : dout, ok);
+        }
+        for (int g = lhalf; g < N / 8; g += 2) {
             const int ci = ci0 + 8 * g;
-            bool ok = p < pend && ci < cin;
-            long q = 0;
-            if (ok) {
-                const int pn = (int)(p / ((long)h * w));
-                const int rem = (int)(p - (long)pn * h * w);
-                const int yy = rem / w + dy, xx = rem % w + dx;
-                ok = yy >= 0 && yy < h && xx >= 0 && xx < w;
-                q = ((long)pn * h + yy) * w + xx;
-            }
-            cp_async16(b_s + g * (kWtK * 16) + px * 16, ok ? in + q * cin + ci : in, ok);
+            const bool ok = xok && ci < cin;
+            cp_async16(b_s + g * (kWtK * 16) + lpx * 16, ok ? in + q * cin + ci : in, ok);
         }
     };
 

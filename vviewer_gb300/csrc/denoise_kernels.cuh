@@ -55,7 +55,7 @@ bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernel
 // dbias[co] += sum_p dout[p][co] (dbias may be null).
 // With `err` set it runs on the tcgen05 tensor cores (err receives a status
 // bit if a wait timed out), with err null on the warp-level mma.sync kernel
-// (the faster of the two for this network: training step 3.2 vs 4.5 ms).
+// (the faster of the two for this network: training step 3.2 vs 4.1 ms).
 void conv3x3_wgrad(const bf16 *dout, int cout, const bf16 *in, int cin, int n, int h, int w, float *dw,
                    float *dbias, cudaStream_t s, uint32_t *err = nullptr);
 // the mma.sync weight gradient (dw only)
