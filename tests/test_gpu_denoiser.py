@@ -158,3 +158,27 @@ def test_fused_upsample_concat_is_exact(ctx, n, h, w):
     assert np.array_equal(outs["tcgen05"], outs["tcgen05_unfused"])
     assert np.array_equal(outs["tcgen05_persistent"], outs["tcgen05_unfused"])
     dn.close()
+
+
+def test_timed_out_wait_is_reported_and_the_denoiser_recovers(ctx):
+    """Failure handling without a GPU fault: one strip convolution withholds
+    its accumulator-ready signal, the drain warps' bounded waits run out, the
+    kernel frees its tensor memory and records an error status; apply()
+    reports VVPT_ERR_DEVICE and the next apply() gives the normal image."""
+    import torch
+    rng = np.random.default_rng(9)
+    h, w = 32, 48
+    ins = [_cuda(rng.gamma(1.0, 0.5, (h, w, 4))), _cuda(rng.uniform(0, 1, (h, w, 4))),
+           _cuda(rng.uniform(0, 1, (h, w, 4)))]
+    dn = Denoiser(ctx, seed=2)
+    ref = torch.zeros((h, w, 4), device="cuda")
+    dn.apply(*ins, ref)
+    dn.inject_wait_timeout()
+    out = torch.zeros((h, w, 4), device="cuda")
+    with pytest.raises(N.VvptError) as e:
+        dn.apply(*ins, out)
+    assert e.value.status == 5  # VVPT_ERR_DEVICE
+    dn.apply(*ins, out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    dn.close()

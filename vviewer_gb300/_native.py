@@ -193,6 +193,7 @@ _SIGNATURES = {
                                           C.POINTER(C.c_float)]),
     "vvpt_denoiser_train_step": (C.c_int, [C.c_void_p, C.POINTER(DenoiseBatch), C.c_float, C.POINTER(C.c_float)]),
     "vvpt_denoiser_set_kernels": (C.c_int, [C.c_void_p, C.c_int]),
+    "vvpt_denoiser_inject_wait_timeout": (C.c_int, [C.c_void_p]),
     "vvpt_denoiser_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                       C.c_uint32]),
     "vvpt_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(SceneData),

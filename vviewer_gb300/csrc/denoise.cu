@@ -488,6 +488,14 @@ VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *dn, int kind)
     return VVPT_OK;
 }
 
+VVPT_API vvpt_status vvpt_denoiser_inject_wait_timeout(vvpt_denoiser *dn)
+{
+    if (!dn)
+        return VVPT_ERR_INVALID_ARG;
+    vvdn::inject_wait_timeout();
+    return VVPT_OK;
+}
+
 VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *dn, const float *radiance, const float *albedo,
                                          const float *normal, float *out, uint32_t width, uint32_t height)
 {

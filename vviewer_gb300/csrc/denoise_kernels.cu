@@ -4,6 +4,7 @@
 // per-tile kernels for the rest), and the warp-level mma.sync m16n8k16 kernels
 // (operand tiles read with ldmatrix) kept as a cross-check.
 #include <algorithm>
+#include <atomic>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -1037,7 +1038,7 @@ constexpr int kStThreads = 224;
 
 __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const __grid_constant__ CUtensorMap tmap,
                                                               int ncols, int nacc, int ring, int segs, int seg_rows,
-                                                              uint32_t *err)
+                                                              uint32_t *err, int withhold_acc_full)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     __shared__ uint32_t tmem_holder;
@@ -1268,7 +1269,10 @@ __global__ void __launch_bounds__(kStThreads) k_conv3x3_strip(ConvArgs a, const 
                                          "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
                         }
                     }
-                    umma_commit(smem_addr(&acc_full[b]));
+                    // (withhold_acc_full: a diagnostic launch that never signals
+                    // the drain warps, whose bounded waits then run out)
+                    if (!withhold_acc_full)
+                        umma_commit(smem_addr(&acc_full[b]));
                     // halo row i is not read by later rows of the unit
                     umma_commit(smem_addr(&empty[row_slot]));
                     row_slot = row_slot + 1 == ring ? 0 : row_slot + 1;
@@ -1506,6 +1510,8 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad_tc(const bf16 *__restrict
 
 namespace {
 
+std::atomic<bool> g_inject_wait_timeout{false};
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
@@ -1627,12 +1633,15 @@ bool launch_strip(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels 
                              cudaSharedmemCarveoutMaxShared);
         attr_smem = pl.smem;
     }
+    const int withhold = g_inject_wait_timeout.exchange(false) ? 1 : 0;
     k_conv3x3_strip<<<pl.grid, kStThreads, pl.smem, s>>>(a, tmap, pl.ncols, pl.nacc, pl.ring, pl.segs, pl.seg_rows,
-                                                         err);
+                                                         err, withhold);
     return true;
 }
 
 }  // namespace
+
+void inject_wait_timeout() { g_inject_wait_timeout.store(true); }
 
 bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind)
 {

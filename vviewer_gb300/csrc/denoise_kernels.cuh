@@ -51,6 +51,11 @@ void conv3x3(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind 
 // returns false, launching nothing, when that kernel does not take the layer.
 bool conv3x3_concat(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels kind = kConvAuto);
 
+// Diagnostics: the next strip-kernel launch withholds its accumulator-ready
+// signal, so its drain warps' bounded waits run out and the launch records
+// an error status instead of hanging (no GPU fault is involved).
+void inject_wait_timeout();
+
 // dw[co][tap][ci] += sum_p dout[p][co] * in[p shifted by tap][ci];
 // dbias[co] += sum_p dout[p][co] (dbias may be null).
 // With `err` set it runs on the tcgen05 tensor cores (err receives a status

@@ -43,6 +43,11 @@ class Denoiser:
         'tcgen05_wgrad' (weight gradients on tcgen05 as well)."""
         self.ctx.check(self.ctx.lib.vvpt_denoiser_set_kernels(self.handle, self.KERNELS[kind]))
 
+    def inject_wait_timeout(self) -> None:
+        """Diagnostics: the next strip convolution's bounded waits run out
+        (vvpt_denoiser_inject_wait_timeout); the next call reports it."""
+        self.ctx.check(self.ctx.lib.vvpt_denoiser_inject_wait_timeout(self.handle))
+
     def params(self) -> np.ndarray:
         out = np.zeros(self.num_params, dtype=np.float32)
         self.ctx.check(self.ctx.lib.vvpt_denoiser_get_params(self.handle, out.ctypes.data, self.num_params))
