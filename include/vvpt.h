@@ -559,10 +559,11 @@ enum {
     VVPT_DENOISER_TCGEN05_WGRAD = 5
 };
 VVPT_API vvpt_status vvpt_denoiser_set_kernels(vvpt_denoiser *denoiser, int kind);
-/* Diagnostics for failure handling: the next tcgen05 strip convolution
- * withholds its accumulator-ready signal, its drain warps' bounded waits
- * (2 s) run out, and the call that launched it returns VVPT_ERR_DEVICE; the
- * kernel frees its tensor memory and the denoiser stays usable. */
+/* Diagnostics for failure handling: the next tcgen05 strip convolution of
+ * the process (of any denoiser) withholds its accumulator-ready signal, its
+ * drain warps' bounded waits (2 s) run out, and the call that launched it
+ * returns VVPT_ERR_DEVICE; the kernel frees its tensor memory and the
+ * denoiser stays usable. */
 VVPT_API vvpt_status vvpt_denoiser_inject_wait_timeout(vvpt_denoiser *denoiser);
 /* Denoises one image: out = exp(network(log1p radiance, albedo, normal)) - 1. */
 VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *denoiser,
