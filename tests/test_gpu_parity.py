@@ -103,6 +103,23 @@ def test_medium_scene_matches_oracle(ctx):
     assert rel < 1e-3 and close >= 0.9 and z4 < 0.01, (rel, close, z4)
 
 
+def test_gltf_model_scene_matches_oracle(ctx, tmp_path):
+    """A glTF model (indexed meshes, a node tree, an RGBA base colour texture
+    with cut-outs, metallic-roughness, occlusion and normal maps, an emissive
+    quad) placed twice in the Cornell room through addModel3D."""
+    from gltf_files import textured_panel_model
+    from vviewer_gb300.model3d import add_model3d, import_model
+
+    e, info = scenes.cornell_box(3, 96, 72, 32, 8, 4)
+    model = import_model(e, textured_panel_model(tmp_path, "glb"), name="panel")
+    add_model3d(e.scene, None, model, Transform((0.5, 0.45, 0.45), (0.5, 0.5, 0.5)))
+    add_model3d(e.scene, None, model, Transform((0.3, 0.25, 0.7), (0.3, 0.3, 0.3), (0.0, 0.6, 0.0)))
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-3 and close >= 0.9 and z4 < 0.01, (rel, close, z4)
+    assert (res.albedo == ref["albedo"]).all(-1).mean() >= 0.98
+
+
 def test_thin_lens_and_non_square_match_oracle(ctx):
     e, info = scenes.cornell_box(4, 80, 48, 16, 8, 4)
     cam = e.scene.camera

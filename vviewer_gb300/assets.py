@@ -118,27 +118,35 @@ def load_obj(path: str | Path) -> Mesh:
     return mesh_from_obj_arrays(a["name"], a["v"], a["vt"], a["vn"], a["f"].reshape(-1, 3))
 
 
-def calc_tangent_space(pos: np.ndarray, uv: np.ndarray, nrm: np.ndarray, max_angle_deg: float = 45.0):
-    """Per-corner tangents/bitangents (corners grouped in threes), restating
-    assimp 5.2.5's CalcTangentSpace step in float32:
+def calc_tangent_space(pos: np.ndarray, uv: np.ndarray, nrm: np.ndarray, max_angle_deg: float = 45.0,
+                       faces: np.ndarray | None = None):
+    """Per-vertex tangents/bitangents, restating assimp 5.2.5's
+    CalcTangentSpace step in float32:
 
     1. per face, with v = p1 - p0, w = p2 - p0 and UV deltas (sx, sy), (tx, ty):
        tangent = (w*sy - v*ty) * dirCorrection, bitangent = (v*tx - w*sx) * dirCorrection,
        dirCorrection = -1 when tx*sy - ty*sx < 0; degenerate UVs use (0,1),(1,0);
-    2. per corner, both projected onto the plane of the corner's normal and
-       normalised;
-    3. smoothing, visiting corners in index order: a corner not yet assigned
-       gathers every unassigned corner within the position epsilon
+    2. per face corner, both projected onto the plane of that vertex's normal
+       and normalised, and stored at the vertex; faces are visited in order,
+       so a vertex shared by several faces (indexed meshes) keeps the last
+       face's value;
+    3. smoothing, visiting vertices in index order: a vertex not yet assigned
+       gathers every unassigned vertex within the position epsilon
        (1e-4 x bounding-box diagonal) whose normal has a dot product >= 0.9999
        and whose tangent and bitangent are within the smoothing angle of its
-       own. The seed corner is part of the neighbour search as well, so it
+       own. The seed vertex is part of the neighbour search as well, so it
        enters the sum twice. The normalised sums replace all gathered values.
+
+    `faces` (F x 3 vertex indices) describes an indexed mesh (glTF); without
+    it the vertices are face corners grouped in threes (assimp's OBJ output).
+    Vertices no face uses keep zero vectors.
     """
     from scipy.spatial import cKDTree
 
     n = pos.shape[0]
-    p = pos.astype(f32).reshape(-1, 3, 3)
-    t = uv.astype(f32).reshape(-1, 3, 2)
+    faces = (np.arange(n, dtype=np.int64) if faces is None else np.asarray(faces, dtype=np.int64)).reshape(-1, 3)
+    p = pos.astype(f32)[faces]
+    t = uv.astype(f32)[faces]
     v = p[:, 1] - p[:, 0]
     w = p[:, 2] - p[:, 0]
     sx = t[:, 1, 0] - t[:, 0, 0]
@@ -153,30 +161,40 @@ def calc_tangent_space(pos: np.ndarray, uv: np.ndarray, nrm: np.ndarray, max_ang
     ty = np.where(degen, 0, ty).astype(f32)
     tan = np.repeat(((w * sy[:, None] - v * ty[:, None]) * dir_corr[:, None]).astype(f32), 3, axis=0)
     bit = np.repeat(((-w * sx[:, None] + v * tx[:, None]) * dir_corr[:, None]).astype(f32), 3, axis=0)
+    corner_vertex = faces.ravel()
     nn = nrm.astype(f32)
-    lt = (tan - nn * (tan * nn).sum(1, keepdims=True)).astype(f32)
-    lb = (bit - nn * (bit * nn).sum(1, keepdims=True)).astype(f32)
+    nc = nn[corner_vertex]
+    ct = (tan - nc * (tan * nc).sum(1, keepdims=True)).astype(f32)
+    cb = (bit - nc * (bit * nc).sum(1, keepdims=True)).astype(f32)
 
     def _normalize_safe(a):
         ln = np.sqrt((a * a).sum(1, keepdims=True))
         return np.where(ln > 0, a / np.where(ln > 0, ln, 1), a).astype(f32)
 
-    lt = _normalize_safe(lt)
-    lb = _normalize_safe(lb)
+    ct = _normalize_safe(ct)
+    cb = _normalize_safe(cb)
     # non-finite frames: rebuild from the normal
-    bad = ~(np.isfinite(lt).all(1) & np.isfinite(lb).all(1)) | ~(np.abs(lt).sum(1) > 0)
+    bad = ~(np.isfinite(ct).all(1) & np.isfinite(cb).all(1)) | ~(np.abs(ct).sum(1) > 0)
     for i in np.nonzero(bad)[0]:
-        a = np.array([1.0, 0.0, 0.0]) if abs(nn[i, 0]) < 0.9 else np.array([0.0, 1.0, 0.0])
-        tt = np.cross(nn[i], a)
-        lt[i] = tt / np.linalg.norm(tt)
-        lb[i] = np.cross(nn[i], lt[i])
+        a = np.array([1.0, 0.0, 0.0]) if abs(nc[i, 0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        tt = np.cross(nc[i], a)
+        ct[i] = tt / np.linalg.norm(tt)
+        cb[i] = np.cross(nc[i], ct[i])
+    # the last face corner of each vertex wins
+    last = np.full(n, -1, dtype=np.int64)
+    np.maximum.at(last, corner_vertex, np.arange(corner_vertex.size, dtype=np.int64))
+    used = last >= 0
+    lt = np.zeros((n, 3), dtype=f32)
+    lb = np.zeros((n, 3), dtype=f32)
+    lt[used] = ct[last[used]]
+    lb[used] = cb[last[used]]
 
     eps = float(np.linalg.norm(pos.max(0) - pos.min(0))) * 1e-4
     neighbours = cKDTree(pos.astype(np.float64)).query_ball_point(pos.astype(np.float64), r=max(eps, 1e-12))
     limit = f32(math.cos(math.radians(max_angle_deg)))
     T = lt.copy()
     B = lb.copy()
-    done = np.zeros(n, dtype=bool)
+    done = ~used
     for a in range(n):
         if done[a]:
             continue

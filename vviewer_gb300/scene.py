@@ -605,6 +605,7 @@ class Engine:
         self.lights: list[Light] = []
         self.meshes: list[Mesh] = []
         self.textures = default_textures()
+        self.models: dict = {}  # imported models by name (model3d.import_model)
         self._materials_by_name: dict[str, Material] = {}
         self._lights_by_name: dict[str, Light] = {}
         self.scene = Scene(self)

@@ -4,15 +4,16 @@ Follows the reference's format and loading steps:
   * parsing: src/lib/vengine/core/io/Import.cpp:26-566 (vec2/3/4 given as
     {x,y,z[,w]} or {r,g,b[,a]} objects, arrays of 1..4 floats or one float;
     rotations as Euler degrees (vec3) or a quaternion (x, y, z, w); camera by
-    target + up or by rotation; materials LAMBERT / PBR_STANDARD / VOLUME
-    (EMBEDDED materials come with a model and are not supported here);
+    target + up or by rotation; materials LAMBERT / PBR_STANDARD / VOLUME,
+    EMBEDDED ones named "<model file stem>:<name>" coming with their model;
     lights POINT / DIRECTIONAL; scene objects with transform, mesh, material,
     light, volume and children);
   * applying: src/bin/vviewer/UI/MainWindow.cpp:598-672 (camera through
     Transform::setRotation(forward, up), src/lib/vengine/math/Transform.cpp:90-100;
     models, materials, lights, objects; environment map and type);
   * export: src/lib/vengine/core/io/Export.cpp (the same fields).
-Models are Wavefront OBJ files (the reference loads any assimp format);
+Models are glTF 2.0 (.gltf, .glb) or Wavefront OBJ files, imported by
+model3d.import_model with the materials a glTF file carries;
 textures are 8-bit PNG (albedo and emissive sRGB, the rest linear); the
 environment is a Radiance .hdr image used as the equirectangular map.
 """
@@ -27,7 +28,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _native as N
-from .assets import load_obj, read_hdr
+from .assets import read_hdr
 from .scene import (EnvironmentType, Engine, LightType, MaterialLambert, MaterialPBRStandard, MaterialVolume,
                     Transform, quat_from_euler, quat_to_mat3)
 
@@ -39,7 +40,13 @@ f32 = np.float32
 def read_png(path: str | Path) -> np.ndarray:
     """H x W x 4 uint8 RGBA from a PNG file (grey, grey+alpha, RGB, RGBA,
     palette; bit depth 8 or 16; no interlacing)."""
-    data = Path(path).read_bytes()
+    return decode_png(Path(path).read_bytes(), str(path))[0]
+
+
+def decode_png(data: bytes, path: str = "PNG") -> tuple[np.ndarray, int]:
+    """(H x W x 4 uint8 RGBA, channels in the file) of PNG data. The channel
+    count is stb_image's: 1 grey, 2 grey+alpha, 3 RGB, 4 RGBA, and 3 or 4 for
+    a palette image (4 with a transparency chunk)."""
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError(f"{path}: not a PNG file")
     pos, idat, plte, trns = 8, [], None, None
@@ -65,28 +72,32 @@ def read_png(path: str | Path) -> np.ndarray:
     stride = (w * channels * depth + 7) // 8
     raw = zlib.decompress(b"".join(idat))
     out = np.zeros((h, stride), dtype=np.uint8)
-    prev = np.zeros(stride, dtype=np.int32)
+    prev = np.zeros(stride, dtype=np.int64)
     for y in range(h):
         ft = raw[y * (stride + 1)]
-        line = np.frombuffer(raw, dtype=np.uint8, count=stride, offset=y * (stride + 1) + 1).astype(np.int32)
-        cur = np.zeros(stride, dtype=np.int32)
+        line = np.frombuffer(raw, dtype=np.uint8, count=stride, offset=y * (stride + 1) + 1).astype(np.int64)
         if ft == 0:
             cur = line
-        elif ft == 2:
+        elif ft == 2:  # Up
             cur = (line + prev) & 0xFF
-        else:
+        elif ft == 1 and stride % bpp == 0:  # Sub: a running sum per byte lane
+            cur = np.cumsum(line.reshape(-1, bpp), axis=0).ravel() & 0xFF
+        else:  # Average, Paeth: sequential along the row
+            ln, pv = line.tolist(), prev.tolist()
+            cl = [0] * stride
             for i in range(stride):
-                a = cur[i - bpp] if i >= bpp else 0
-                b = prev[i]
-                c = prev[i - bpp] if i >= bpp else 0
+                a = cl[i - bpp] if i >= bpp else 0
+                b = pv[i]
                 if ft == 1:
                     p = a
                 elif ft == 3:
                     p = (a + b) >> 1
                 else:  # Paeth
+                    c = pv[i - bpp] if i >= bpp else 0
                     pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
                     p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
-                cur[i] = (line[i] + p) & 0xFF
+                cl[i] = (ln[i] + p) & 0xFF
+            cur = np.asarray(cl, dtype=np.int64)
         out[y] = cur
         prev = cur
     if depth == 16:
@@ -112,7 +123,8 @@ def read_png(path: str | Path) -> np.ndarray:
             rgba[..., 3] = px[..., 1]
     else:
         rgba[..., :channels] = px
-    return rgba
+    file_channels = (4 if trns is not None else 3) if ctype == 3 else channels
+    return rgba, file_channels
 
 
 # ---------------------------------------------------------------- value parsing (Import.cpp:41-213)
@@ -242,17 +254,17 @@ def import_scene(path: str | Path, engine: Engine | None = None) -> Engine:
     cam.focal_distance = float(c.get("focalDistance", cam.focal_distance))
     camera_volume = c.get("volume", "")
 
-    # models
+    # models, with their embedded materials (MainWindow.cpp:638-642)
+    from .model3d import import_model
+
     models = {}
     for m in doc.get("models", []):
-        fp = folder / m["filepath"]
-        if fp.suffix.lower() != ".obj":
-            raise ValueError(f"model {m['name']}: only OBJ files are supported ({fp.name})")
-        models[m["name"]] = fp
-    meshes: dict = {}
+        models[m["name"]] = import_model(engine, folder / m["filepath"], name=m["name"])
 
-    # materials (Import.cpp:370-432)
+    # materials (Import.cpp:370-432); EMBEDDED ones came with their model
     for m in doc.get("materials", []):
+        if m["type"] == "EMBEDDED":
+            continue
         cls = _MATERIALS.get(m["type"])
         if cls is None:
             raise ValueError(f"material {m['name']}: {m['type']} materials are not supported")
@@ -324,9 +336,12 @@ def import_scene(path: str | Path, engine: Engine | None = None) -> Engine:
             model = o["mesh"]["modelName"]
             if model not in models:
                 raise ValueError(f"object {o['name']}: unknown model {model}")
-            if model not in meshes:
-                meshes[model] = engine.add_mesh(load_obj(models[model]))
-            so.mesh = meshes[model]
+            sub = o["mesh"].get("submesh")
+            candidates = models[model].meshes()
+            mesh = models[model].mesh(sub) if sub is not None else (candidates[0] if len(candidates) == 1 else None)
+            if mesh is None:
+                raise ValueError(f"object {o['name']}: model {model} has no mesh {sub!r}")
+            so.mesh = mesh
         if "material" in o:
             so.material = engine.material(o["material"]["name"])
         if "light" in o:
