@@ -89,3 +89,30 @@ extern "C" int host_trace_closest(const vvpt_scene_desc *desc, const vvpt_ray *r
     *err_bits = e;
     return 0;
 }
+
+// may_reach_emitter for each ray over the packed scene's emissive boxes;
+// also returns the number of boxes.
+extern "C" int host_may_reach_emitter(const vvpt_scene_desc *desc, const vvpt_ray *rays, uint32_t n, uint8_t *out,
+                                      uint32_t *num_boxes, char *msg, int msg_len)
+{
+    PackedScene pk;
+    std::string err;
+    vvpt_status st = pack_scene(desc, pk, err, 1);
+    if (st != VVPT_OK) {
+        std::strncpy(msg, err.c_str(), msg_len - 1);
+        msg[msg_len - 1] = 0;
+        return (int)st;
+    }
+    SceneView v{};
+    v.emit_boxes = pk.emit_boxes.data();
+    v.num_emit_boxes = (uint32_t)(pk.emit_boxes.size() / 2);
+    *num_boxes = v.num_emit_boxes;
+    for (uint32_t i = 0; i < n; i++) {
+        const vvpt_ray &r = rays[i];
+        out[i] = may_reach_emitter(v, f3(r.origin[0], r.origin[1], r.origin[2]),
+                                   f3(r.direction[0], r.direction[1], r.direction[2]))
+                     ? 1
+                     : 0;
+    }
+    return 0;
+}

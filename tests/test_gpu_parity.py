@@ -117,7 +117,8 @@ def test_gltf_model_scene_matches_oracle(ctx, tmp_path):
     res, ref = render_pair(ctx, e, info)
     rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
     assert rel < 1e-3 and close >= 0.9 and z4 < 0.01, (rel, close, z4)
-    assert (res.albedo == ref["albedo"]).all(-1).mean() >= 0.98
+    # textured first-hit albedo: bilinear sRGB lookups agree to rounding
+    assert np.isclose(res.albedo, ref["albedo"], rtol=1e-5, atol=1e-6).all(-1).mean() >= 0.99
 
 
 def test_thin_lens_and_non_square_match_oracle(ctx):

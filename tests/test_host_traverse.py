@@ -50,6 +50,9 @@ def host_lib(request):
     lib.host_trace_closest.restype = C.c_int
     lib.host_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32),
                                        C.c_char_p, C.c_int]
+    lib.host_may_reach_emitter.restype = C.c_int
+    lib.host_may_reach_emitter.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32),
+                                           C.c_char_p, C.c_int]
     return lib
 
 
@@ -98,3 +101,65 @@ def test_hit_just_above_coplanar_faces(host_lib):
     ho = oracle.trace_closest(fs, ray)
     assert_hits_equal(hh, ho)
     assert hh["instance"][0] == 0
+
+
+def _many_lights_scene():
+    """The Cornell box with 40 small emissive quads: more emissive instances
+    than the 32 boxes the prefilter keeps, so the boxes are merged."""
+    from vviewer_gb300 import scenes
+    from vviewer_gb300.scene import MaterialLambert, Transform
+
+    e, _ = scenes.cornell_box(2)
+    lamp = e.create_material(MaterialLambert, "lamp")
+    lamp.emissive = [3.0, 3.0, 3.0, 1.0]
+    quad = next(so.mesh for so in e.scene.objects_flat() if so.name == "light")
+    rng = np.random.default_rng(4)
+    for k in range(40):
+        so = e.scene.add_scene_object(f"lamp{k}", Transform((rng.uniform(-0.4, 0.4), -rng.uniform(0.1, 0.9),
+                                                             rng.uniform(-0.4, 0.4)), (0.3, 0.3, 0.3)))
+        so.mesh = quad
+        so.material = lamp
+    return e
+
+
+def _emissive_instances(fs):
+    out = np.zeros(len(fs.instances), dtype=bool)
+    for k, inst in enumerate(fs.instances):
+        m = fs.materials[inst.material_index]
+        e = [abs(m.emissive[c] * m.emissive[3]) for c in range(3)]
+        out[k] = bool(inst.flags & 1) and max(e) > 0.05
+    return out
+
+
+@pytest.mark.parametrize("name", ["cornell", "two_balls_mesh_light", "displaced_spheres", "many_lights"])
+def test_emitter_prefilter_keeps_every_ray_that_reaches_an_emitter(host_lib, name):
+    """The emitter-ray prefilter (traverse.cuh may_reach_emitter over the
+    packed emissive boxes) must pass every ray whose closest hit is an
+    emissive instance: those are the rays whose emitter contribution can be
+    non-zero. Rays start anywhere, on surfaces, and just off surfaces."""
+    if name == "many_lights":
+        fs, lo, hi = _many_lights_scene().scene.build(), -0.2, 1.2
+    else:
+        build, (lo, hi) = HIT_SCENES[name]
+        fs = build().scene.build()
+    rays = np.concatenate([make_rays(fs, 40_000, 3, lo, hi), make_near_rays(fs, 20_000, 5)])
+    hits = host_trace(host_lib, fs, rays)
+    desc = fs.desc()
+    r = np.ascontiguousarray(rays, dtype=np.float32)
+    may = np.zeros(r.shape[0], dtype=np.uint8)
+    nb = C.c_uint32(0)
+    msg = C.create_string_buffer(256)
+    assert host_lib.host_may_reach_emitter(C.addressof(desc), r.ctypes.data, r.shape[0], may.ctypes.data,
+                                           C.byref(nb), msg, 256) == 0, msg.value
+    emissive = _emissive_instances(fs)
+    hit = hits["instance"] != 0xFFFFFFFF
+    reach = np.zeros(len(hits), dtype=bool)
+    reach[hit] = emissive[hits["instance"][hit].astype(np.int64)]
+    assert reach.sum() > 50, reach.sum()
+    assert may[reach].all(), f"{np.count_nonzero(may[reach] == 0)} rays reach an emitter but were rejected"
+    assert 1 <= nb.value <= 32
+    if name == "many_lights":
+        assert nb.value == 32  # 41 emissive instances merged into 32 boxes
+    if name in ("cornell", "displaced_spheres"):
+        # one small ceiling light: most rays are rejected
+        assert may.mean() < 0.5, may.mean()

@@ -94,7 +94,7 @@ size_t path_state_bytes(size_t slots)
 
 size_t queue_bytes(size_t slots)
 {
-    return 10 * aligned256(slots * sizeof(uint32_t)) + aligned256(C_COUNT * sizeof(uint32_t));
+    return 11 * aligned256(slots * sizeof(uint32_t)) + aligned256(C_COUNT * sizeof(uint32_t));
 }
 
 PathState carve_path_state(char *base, size_t n)
@@ -145,6 +145,7 @@ Queues carve_queues(char *base, size_t n)
     q.shade_p = (uint32_t *)take(u4);
     q.shade_m = (uint32_t *)take(u4);
     q.conn = (uint32_t *)take(u4);
+    q.nee = (uint32_t *)take(u4);
     q.ext_key = (uint32_t *)take(u4);
     q.walk = (uint32_t *)take(u4);
     q.regen[0] = (uint32_t *)take(u4);
@@ -346,6 +347,8 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
         return st;
     if ((st = upload(ctx, scene->env_dist, pk.env_dist, bytes)) != VVPT_OK)
         return st;
+    if ((st = upload(ctx, scene->emit_boxes, pk.emit_boxes, bytes)) != VVPT_OK)
+        return st;
     VV_CUDA(cudaStreamSynchronize(vv_stream(ctx)), "scene upload");
 
     SceneView &v = scene->view;
@@ -376,6 +379,8 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     v.env_func = scene->env_dist.as<float>();
     v.env_cond_cdf = v.env_func + (size_t)pk.env_w * pk.env_h;
     v.env_marg_cdf = v.env_cond_cdf + (size_t)(pk.env_w + 1) * pk.env_h;
+    v.emit_boxes = scene->emit_boxes.as<float4>();
+    v.num_emit_boxes = (uint32_t)(pk.emit_boxes.size() / 2);
     scene->bytes = bytes;
     scene->num_materials = desc->num_materials;
     *out_scene = guard.release();
@@ -899,7 +904,7 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     auto aligned = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
     const uint64_t f4 = slots64 * sizeof(float4), u4 = slots64 * sizeof(uint32_t);
     const uint64_t need = aligned(sizeof(SingleJobBlock)) + aligned(C_COUNT * sizeof(uint32_t)) + 14 * aligned(f4) +
-                          7 * aligned(u4) + aligned(u4) /* idle slots */ + 10 * aligned(u4) +
+                          7 * aligned(u4) + aligned(u4) /* idle slots */ + 11 * aligned(u4) +
                           3 * aligned(items64 * sizeof(float4));
     if (need > kNoAllocScratchBytes)
         return fail(ctx, VVPT_ERR_INVALID_ARG,
@@ -977,8 +982,8 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     for (uint32_t **p : u4s)
         *p = reinterpret_cast<uint32_t *>(take(u4));
     const JobTable jt = single_job_table(djob, reinterpret_cast<uint32_t *>(take(u4)));
-    uint32_t **qs[10] = {&q.ext[0], &q.ext[1], &q.shade_l, &q.shade_p, &q.shade_m,
-                         &q.conn,   &q.ext_key, &q.walk,  &q.regen[0], &q.regen[1]};
+    uint32_t **qs[11] = {&q.ext[0], &q.ext[1],  &q.shade_l, &q.shade_p,  &q.shade_m, &q.conn,
+                         &q.nee,    &q.ext_key, &q.walk,    &q.regen[0], &q.regen[1]};
     for (uint32_t **p : qs)
         *p = reinterpret_cast<uint32_t *>(take(u4));
     BatchResults br;

@@ -61,7 +61,8 @@ struct Engine; // engine.cu
 }  // namespace vvpt
 
 struct vvpt_scene {
-    vvpt::DevBuf nodes, wnodes, tris, verts, indices, instances, tlas_order, materials, lights, textures, texels, env_dist;
+    vvpt::DevBuf nodes, wnodes, tris, verts, indices, instances, tlas_order, materials, lights, textures, texels, env_dist,
+        emit_boxes;
     vvpt::SceneView view{};
     uint64_t bytes = 0;
     uint32_t num_materials = 0;

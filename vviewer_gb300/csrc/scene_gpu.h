@@ -157,6 +157,14 @@ struct SceneView {
     const float *env_marg_cdf; // env_h + 1
     uint32_t env_w, env_h;
     float env_func_int;        // integral of env_func over [0,1]^2
+    // World boxes (lo, hi pairs, padded) that hold every TLAS instance whose
+    // material can emit (emission above the emitter rays' 0.05 threshold):
+    // a BSDF-direction emitter ray whose line misses all of them adds nothing.
+    // At most kMaxEmitBoxes; more emissive instances are merged into that many.
+    const float4 *emit_boxes;
+    uint32_t num_emit_boxes;
 };
+
+constexpr uint32_t kMaxEmitBoxes = 32;
 
 }  // namespace vvpt

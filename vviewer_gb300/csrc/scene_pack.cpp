@@ -336,6 +336,45 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
         indices.insert(indices.end(), md.indices, md.indices + 3ull * md.num_triangles);
     }
 
+    // ---- which materials can emit: the emitter rays add radiance where
+    // emissive.w * emissive.rgb * texel exceeds 0.05 in some channel; bound it
+    // by the largest texel of the emissive texture (1 for 8-bit formats). The
+    // 0.04 cut leaves a margin for rounding; NaN counts as emitting.
+    std::vector<char> may_emit(desc->num_materials, 0);
+    {
+        std::vector<double> tex_max(desc->num_textures, -1.0);
+        auto texel_bound = [&](uint32_t t) -> double {
+            if (t >= desc->num_textures)
+                return INFINITY;
+            const vvpt_texture_desc &td = desc->textures[t];
+            if (td.format != VVPT_TEXTURE_RGBA32F)
+                return 1.0;
+            if (tex_max[t] < 0.0) {
+                const float *px = static_cast<const float *>(td.data);
+                double mx = 0.0;
+                for (uint64_t k = 0; k < (uint64_t)td.width * td.height && !std::isinf(mx); k++)
+                    for (int c = 0; c < 3; c++) {
+                        const double v = std::fabs((double)px[4 * k + c]);
+                        mx = std::isnan(v) ? INFINITY : std::max(mx, v);
+                    }
+                tex_max[t] = mx;
+            }
+            return tex_max[t];
+        };
+        for (uint32_t i = 0; i < desc->num_materials; i++) {
+            const vvpt_material &mt = desc->materials[i];
+            if ((uint32_t)mt.uv_tiling[2] == VVPT_MATERIAL_VOLUME)
+                continue;
+            double b = 0.0;
+            for (int c = 0; c < 3; c++) {
+                const double v = std::fabs((double)mt.emissive[3] * (double)mt.emissive[c]);
+                b = std::isnan(v) ? INFINITY : std::max(b, v);
+            }
+            may_emit[i] = !(b == 0.0 || b * texel_bound(mt.textures2[0]) <= 0.04);
+        }
+    }
+    std::vector<Box3> emit;
+
     // ---- instances + TLAS
     const uint32_t ni = desc->num_instances;
     std::vector<DevInstance> &dinst = out.instances;
@@ -401,7 +440,44 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
             out.cull_r = std::max(out.cull_r, (float)(na * (ninv * bt + pm)));
             tlas_boxes.push_back(w);
             tlas_ids.push_back(i);
+            if (may_emit[d.material])
+                emit.push_back(w);
         }
+    }
+    if (emit.size() > kMaxEmitBoxes) {
+        // merge into kMaxEmitBoxes boxes: runs of neighbours along the axis
+        // of widest centroid spread (unions stay conservative)
+        double clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (const Box3 &b : emit)
+            for (int a = 0; a < 3; a++) {
+                const double c = 0.5 * ((double)b.lo[a] + (double)b.hi[a]);
+                clo[a] = std::min(clo[a], c);
+                chi[a] = std::max(chi[a], c);
+            }
+        int ax = 0;
+        for (int a = 1; a < 3; a++)
+            if (chi[a] - clo[a] > chi[ax] - clo[ax])
+                ax = a;
+        std::stable_sort(emit.begin(), emit.end(), [ax](const Box3 &x, const Box3 &y) {
+            return (double)x.lo[ax] + x.hi[ax] < (double)y.lo[ax] + y.hi[ax];
+        });
+        std::vector<Box3> merged;
+        const size_t n = emit.size();
+        for (size_t g = 0; g < kMaxEmitBoxes; g++) {
+            const size_t k = g * n / kMaxEmitBoxes, end = (g + 1) * n / kMaxEmitBoxes;
+            Box3 u = emit[k];
+            for (size_t j = k + 1; j < end; j++)
+                for (int a = 0; a < 3; a++) {
+                    u.lo[a] = std::min(u.lo[a], emit[j].lo[a]);
+                    u.hi[a] = std::max(u.hi[a], emit[j].hi[a]);
+                }
+            merged.push_back(u);
+        }
+        emit.swap(merged);
+    }
+    for (const Box3 &b : emit) {
+        out.emit_boxes.push_back(make_float4(b.lo[0], b.lo[1], b.lo[2], 0.0f));
+        out.emit_boxes.push_back(make_float4(b.hi[0], b.hi[1], b.hi[2], 0.0f));
     }
     // one instance per TLAS leaf: entering an instance costs a BLAS traversal
     BVHBuildOptions tlas_opt;

@@ -38,6 +38,7 @@ struct PackedScene {
     float env_func_int = 0.0f;
     int tlas_depth = 0;
     int max_blas_depth = 0;
+    std::vector<float4> emit_boxes;   // SceneView::emit_boxes (lo, hi pairs)
 };
 
 // Builder for large BLAS (e.g. the GPU builder): fills `out` and returns true,

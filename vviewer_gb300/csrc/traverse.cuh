@@ -538,4 +538,43 @@ __device__ __forceinline__ Hit trace_closest(const SceneView &s, const float3 &o
     return trace_after(s, o, d, tmin, tmax, no_hit(), err);
 }
 
+// A BSDF-direction emitter ray adds radiance only at an emissive surface,
+// and its candidate walk keeps the direction and moves the origin along the
+// line, so it can contribute only if the half-line from `o` along `d` meets
+// one of the scene's emissive boxes. The slab interval of each axis is
+// widened by 1e-5 of its ends (far above float rounding) and the boxes are
+// padded, so a ray that reaches an emitter is never rejected.
+__device__ __forceinline__ bool may_reach_emitter(const SceneView &s, const float3 &o, const float3 &d)
+{
+    const float big = 3.402823466e38f; // NaN and infinities fail |x| <= big
+    if (!(fabsf(o.x) <= big && fabsf(o.y) <= big && fabsf(o.z) <= big && fabsf(d.x) <= big && fabsf(d.y) <= big &&
+          fabsf(d.z) <= big))
+        return true;
+    for (uint32_t k = 0; k < s.num_emit_boxes; k++) {
+        const float4 lo = __ldg(&s.emit_boxes[2 * k]), hi = __ldg(&s.emit_boxes[2 * k + 1]);
+        float t0 = 0.0f, t1 = INFINITY;
+        bool out = false;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float oa = a == 0 ? o.x : (a == 1 ? o.y : o.z);
+            const float da = a == 0 ? d.x : (a == 1 ? d.y : d.z);
+            const float la = a == 0 ? lo.x : (a == 1 ? lo.y : lo.z);
+            const float ha = a == 0 ? hi.x : (a == 1 ? hi.y : hi.z);
+            if (da == 0.0f) {
+                out |= oa < la || oa > ha;
+            } else {
+                const float ta = (la - oa) / da, tb = (ha - oa) / da;
+                float tn = fminf(ta, tb), tf = fmaxf(ta, tb);
+                tn -= 1e-5f * fabsf(tn);
+                tf += 1e-5f * fabsf(tf);
+                t0 = fmaxf(t0, tn);
+                t1 = fminf(t1, tf);
+            }
+        }
+        if (!out && t0 <= t1)
+            return true;
+    }
+    return false;
+}
+
 }  // namespace vvpt

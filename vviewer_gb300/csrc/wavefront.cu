@@ -119,6 +119,7 @@ __device__ __forceinline__ float material_alpha(const SceneView &s, const DevMat
     return m.albedo.w * tex2d(s, m.tex2[3], tuv.x, tuv.y).x;
 }
 
+
 // ---------------------------------------------------------------------------
 // Light sampling (shaders/pt/lightSampling.glsl:1-106), without the shadow
 // trace, which `connect` performs.
@@ -427,6 +428,7 @@ __global__ void k_begin(Queues q, int pp)
         q.counters[C_SHADE_M] = 0u;
         q.counters[C_WALK] = 0u;
         q.counters[C_CONN] = 0u;
+        q.counters[C_NEEQ] = 0u;
         q.counters[C_EXT0 + (1 - pp)] = 0u;
         q.counters[C_REGEN0 + (1 - pp)] = 0u;
     }
@@ -746,7 +748,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         uint32_t slot = 0;
-        bool want_conn = false, want_done = false, want_ext = false;
+        bool want_conn = false, want_nee = false, want_done = false, want_ext = false;
         if (i < n) {
         if (i < nl)
             slot = q.shade_l[i];
@@ -989,6 +991,8 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
             // MIS weight and the contribution are zero: skip the ray.
             has_nee = false;
         }
+        if (has_nee && !may_reach_emitter(s, origin, dir))
+            has_nee = false; // no emissive surface on its line: it adds zero
 
         const bool done = stop || last;
         uint32_t nf = F_ITEM | (inside ? F_INSIDE : 0u) | ((min(d + 1u, 255u)) << kDepthShift) | (sdepth << kSurfShift);
@@ -1020,13 +1024,17 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         }
         if (sampled)
             ps.nee_b[slot] = f4(nee_beta, nee_pdf);
-        want_conn = has_shadow || (has_nee && !fuse);
+        want_conn = has_shadow;
+        want_nee = has_nee && !fuse;
         want_done = done;
         want_ext = !done;
         }
         uint32_t pos = warp_append_all(want_conn, &q.counters[C_CONN]);
         if (want_conn)
             q.conn[pos] = slot;
+        pos = warp_append_all(want_nee, &q.counters[C_NEEQ]);
+        if (want_nee)
+            q.nee[pos] = slot;
         pos = warp_append_all(want_done, &q.counters[C_REGEN0 + (1 - pp)]);
         if (want_done)
             q.regen[1 - pp][pos] = slot;
@@ -1368,15 +1376,15 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
 // extension ray is never traced, so the emitter ray cannot ride on it).
 __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_emitter(JobTable jt, PathState ps, Queues q)
 {
-    const uint32_t n = q.counters[C_CONN];
+    const uint32_t n = q.counters[C_NEEQ];
     uint32_t err = 0;
     uint32_t nnee = 0;
     if (blockIdx.x * blockDim.x < n)
-        tlas_cache_fill(jt.jobs[ps.job[q.conn[blockIdx.x * blockDim.x]]].scene);
+        tlas_cache_fill(jt.jobs[ps.job[q.nee[blockIdx.x * blockDim.x]]].scene);
     else
         tlas_cache_none();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t slot = q.conn[i];
+        const uint32_t slot = q.nee[i];
         const uint32_t flags = ps.flags[slot];
         if (!(flags & F_NEE))
             continue;

@@ -75,7 +75,8 @@ enum CounterIndex {
     C_NEE = 13,
     C_PATHS = 14,
     C_WALK = 15,
-    C_COUNT = 16
+    C_NEEQ = 16,
+    C_COUNT = 17
 };
 
 struct Queues {
@@ -83,7 +84,8 @@ struct Queues {
     uint32_t *ext_key;  // per extension-queue entry: shade bin (0 Lambert, 1 PBR, 2 miss) | 4 = emitter walk
     uint32_t *shade_l, *shade_p, *shade_m;
     uint32_t *walk;     // paths whose pending emitter ray needs the full candidate walk
-    uint32_t *conn;
+    uint32_t *conn;     // paths with a shadow ray
+    uint32_t *nee;      // paths that end with an emitter ray (k_emitter)
     uint32_t *regen[2];
     uint32_t *counters; // CounterIndex
 };
