@@ -436,7 +436,10 @@ __global__ void k_begin(Queues q, int pp)
 
 // Finalizes finished samples, hands out work items, and generates camera
 // rays (raygen.rgen.glsl:24-99, 126-129).
-__global__ void __launch_bounds__(256) k_regen(JobTable jt, PathState ps, Queues q, int pp)
+#ifndef VVPT_REGEN_MIN_BLOCKS
+#define VVPT_REGEN_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(256, VVPT_REGEN_MIN_BLOCKS) k_regen(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_REGEN0 + pp];
     const uint32_t *queue = q.regen[pp];
