@@ -72,3 +72,22 @@ def make_near_rays(fs, n, seed):
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return np.concatenate([o, np.zeros((n, 1)), d, np.full((n, 1), 1e4)], 1).astype(np.float32)
+
+
+def many_lights_scene(width: int = 64, height: int = 64, samples: int = 16):
+    """The Cornell box with 40 small emissive quads: more emissive instances
+    than the 32 boxes the prefilter keeps, so the boxes are merged."""
+    from vviewer_gb300.scene import MaterialLambert, Transform
+
+    e, info = scenes.cornell_box(2, width, height, samples, 8, 4)
+    lamp = e.create_material(MaterialLambert, "lamp")
+    lamp.emissive = [3.0, 3.0, 3.0, 1.0]
+    quad = next(so.mesh for so in e.scene.objects_flat() if so.name == "light")
+    rng = np.random.default_rng(4)
+    for k in range(40):
+        # the ceiling quad scaled by 0.3 and moved inside the room, facing down
+        so = e.scene.add_scene_object(f"lamp{k}", Transform((rng.uniform(0.0, 0.65), rng.uniform(-0.05, 0.6),
+                                                             rng.uniform(0.0, 0.65)), (0.3, 0.3, 0.3)))
+        so.mesh = quad
+        so.material = lamp
+    return e, info

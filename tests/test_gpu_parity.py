@@ -121,6 +121,17 @@ def test_gltf_model_scene_matches_oracle(ctx, tmp_path):
     assert np.isclose(res.albedo, ref["albedo"], rtol=1e-5, atol=1e-6).all(-1).mean() >= 0.99
 
 
+def test_many_emitters_match_oracle(ctx):
+    """41 emissive instances: the emitter-ray prefilter merges their boxes
+    into 32; every emitter contribution must survive it."""
+    from raygen import many_lights_scene
+
+    e, info = many_lights_scene(96, 96, 32)
+    res, ref = render_pair(ctx, e, info)
+    rel, close, z4 = compare_renders(res.radiance, ref["radiance"], res.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+
+
 def test_thin_lens_and_non_square_match_oracle(ctx):
     e, info = scenes.cornell_box(4, 80, 48, 16, 8, 4)
     cam = e.scene.camera

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from raygen import HIT_SCENES, make_near_rays, make_rays
+from raygen import HIT_SCENES, make_near_rays, make_rays, many_lights_scene
 from vviewer_gb300.renderer import HIT_DTYPE
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -103,25 +103,6 @@ def test_hit_just_above_coplanar_faces(host_lib):
     assert hh["instance"][0] == 0
 
 
-def _many_lights_scene():
-    """The Cornell box with 40 small emissive quads: more emissive instances
-    than the 32 boxes the prefilter keeps, so the boxes are merged."""
-    from vviewer_gb300 import scenes
-    from vviewer_gb300.scene import MaterialLambert, Transform
-
-    e, _ = scenes.cornell_box(2)
-    lamp = e.create_material(MaterialLambert, "lamp")
-    lamp.emissive = [3.0, 3.0, 3.0, 1.0]
-    quad = next(so.mesh for so in e.scene.objects_flat() if so.name == "light")
-    rng = np.random.default_rng(4)
-    for k in range(40):
-        so = e.scene.add_scene_object(f"lamp{k}", Transform((rng.uniform(-0.4, 0.4), -rng.uniform(0.1, 0.9),
-                                                             rng.uniform(-0.4, 0.4)), (0.3, 0.3, 0.3)))
-        so.mesh = quad
-        so.material = lamp
-    return e
-
-
 def _emissive_instances(fs):
     out = np.zeros(len(fs.instances), dtype=bool)
     for k, inst in enumerate(fs.instances):
@@ -138,7 +119,7 @@ def test_emitter_prefilter_keeps_every_ray_that_reaches_an_emitter(host_lib, nam
     emissive instance: those are the rays whose emitter contribution can be
     non-zero. Rays start anywhere, on surfaces, and just off surfaces."""
     if name == "many_lights":
-        fs, lo, hi = _many_lights_scene().scene.build(), -0.2, 1.2
+        fs, lo, hi = many_lights_scene()[0].scene.build(), -0.2, 1.2
     else:
         build, (lo, hi) = HIT_SCENES[name]
         fs = build().scene.build()

@@ -3,7 +3,7 @@ them to vengine (AssimpLoadModel.cpp), vengine's node tree
 (VulkanModel3D.cpp:49-75) and placement (SceneUtils.cpp:76-130), and scene
 files that name glTF models and their EMBEDDED materials."""
 import json
-import warnings
+import struct
 import zlib
 
 import numpy as np
@@ -322,10 +322,8 @@ def _encode_filtered(img: np.ndarray, ft: int) -> bytes:
         prev = cur
 
     def chunk(tag, data):
-        import struct
         return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
 
-    import struct
     return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0))
             + chunk(b"IDAT", zlib.compress(bytes(raw))) + chunk(b"IEND", b""))
 
