@@ -1534,6 +1534,9 @@ struct StripPlan {
 // 512 TMEM columns of an SM), then the deepest ring that fits; the rows of
 // every 128-pixel column are cut into segments so that one wave of CTAs
 // covers the layer.
+#ifndef VVPT_STRIP_FUSED_ONE_CTA
+#define VVPT_STRIP_FUSED_ONE_CTA 0
+#endif
 bool plan_strip(const ConvArgs &a, StripPlan &pl)
 {
     if (a.cin % 16 || a.cin < 16 || a.cout > 256 || a.cout < 1 || (reinterpret_cast<uintptr_t>(a.in) & 15))
@@ -1557,7 +1560,7 @@ bool plan_strip(const ConvArgs &a, StripPlan &pl)
     while (ncols < 2 * N)
         ncols <<= 1;
     constexpr int kStatic = 2048; // mbarriers, TMEM address, flags (1 KB aligned)
-    for (int c = 4; c >= 1; c--) {
+    for (int c = (a.cc && VVPT_STRIP_FUSED_ONE_CTA) ? 1 : 4; c >= 1; c--) {
         if (c * ncols > 512)
             continue;
         const int dyn = std::min(optin - kStatic, sm_smem / c - reserved - kStatic);
@@ -1622,7 +1625,7 @@ bool launch_strip(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels 
 {
     StripPlan pl;
     CUtensorMap tmap;
-    if (!err || kind == kConvTiles || !plan_strip(a, pl) || (a.cc && pl.per_sm < 2) || !encode_input_map(a, tmap))
+    if (!err || kind == kConvTiles || !plan_strip(a, pl) || (a.cc && pl.per_sm < 2 && !VVPT_STRIP_FUSED_ONE_CTA) || !encode_input_map(a, tmap))
         return false;
     if (kind == kConvPersistent)
         pl.grid = std::min(pl.grid, 16);
