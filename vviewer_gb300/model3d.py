@@ -566,7 +566,7 @@ def add_model3d(scene: Scene, parent: SceneObject | None, model: Model3D,
     them. The root's transform can be overridden, and so can every mesh's
     material; meshes without one get "defaultMaterial"."""
     engine = scene.engine
-    default_mat = engine.material("defaultMaterial")
+    default_mat = engine._materials_by_name.get("defaultMaterial")
     override = engine.material(override_material) if override_material is not None else None
 
     def add(node: ModelNode, parent: SceneObject | None, is_root: bool):

@@ -338,7 +338,11 @@ def import_scene(path: str | Path, engine: Engine | None = None) -> Engine:
                 raise ValueError(f"object {o['name']}: unknown model {model}")
             sub = o["mesh"].get("submesh")
             candidates = models[model].meshes()
-            mesh = models[model].mesh(sub) if sub is not None else (candidates[0] if len(candidates) == 1 else None)
+            mesh = models[model].mesh(sub) if sub is not None else None
+            if mesh is None and len(candidates) == 1:
+                # a one-mesh model whose mesh name differs (assimp's naming of
+                # unnamed OBJ objects, for one): its only mesh
+                mesh = candidates[0]
             if mesh is None:
                 raise ValueError(f"object {o['name']}: model {model} has no mesh {sub!r}")
             so.mesh = mesh
