@@ -44,7 +44,6 @@ from __future__ import annotations
 
 import base64
 import json
-import math
 import struct
 import urllib.parse
 import warnings
