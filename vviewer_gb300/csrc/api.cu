@@ -119,7 +119,7 @@ PathState carve_path_state(char *base, size_t n)
     ps.sh_dir = (float4 *)take(f4);
     ps.sh_c = (float4 *)take(f4);
     ps.nee_b = (float4 *)take(f4);
-    take(f4); // spare
+    ps.nee_c = (float4 *)take(f4);
     ps.hit_inst = (uint32_t *)take(u4);
     ps.rng = (uint32_t *)take(u4);
     ps.flags = (uint32_t *)take(u4);
@@ -539,9 +539,9 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
         if (info->flags & VVPT_RENDER_PROFILE_KERNELS) {
             // one kernel at a time with events around each launch
             static const char *names[K_NUM] = {"k_begin", "k_regen",  "k_extend", "k_partition",
-                                               "k_walk",  "k_shade", "k_shadow", "k_emitter"};
+                                               "k_walk",  "k_shade", "k_shadow"};
             static const double bpu[K_NUM] = {0.0,        kBytesRegen, kBytesExtend, kBytesPartition,
-                                              kBytesWalk, kBytesShade, kBytesShadow, kBytesEmitter};
+                                              kBytesWalk, kBytesShade, kBytesShadow};
             vvpt_kernel_profile prof{};
             prof.count = K_NUM;
             for (int k = 0; k < K_NUM; k++) {
@@ -565,7 +565,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                                      : (k == K_EXTEND || k == K_PARTITION) ? c[C_EXT0 + pp]
                                      : k == K_WALK   ? c[C_WALK]
                                      : k == K_SHADE  ? (uint64_t)c[C_SHADE_L] + c[C_SHADE_P] + c[C_SHADE_M]
-                                     : (k == K_SHADOW || k == K_EMITTER) ? c[C_CONN]
+                                     : k == K_SHADOW ? (uint64_t)c[C_CONN] + c[C_NEEQ]
                                                       : 1;
                     cudaEventRecord(ka, vv_stream(ctx));
                     launch_kernel((KernelId)k, jt, ps, q, pp, shape, vv_stream(ctx));
@@ -972,7 +972,7 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     q.counters = reinterpret_cast<uint32_t *>(take(C_COUNT * sizeof(uint32_t)));
     PathState ps;
     float4 **f4s[14] = {&ps.o, &ps.d, &ps.beta, &ps.rad, &ps.alb, &ps.nrm, &ps.cum_rad,
-                        &ps.cum_alb, &ps.cum_nrm, &ps.hit, &ps.sh_dir, &ps.sh_c, &ps.nee_b, nullptr};
+                        &ps.cum_alb, &ps.cum_nrm, &ps.hit, &ps.sh_dir, &ps.sh_c, &ps.nee_b, &ps.nee_c};
     for (float4 **p : f4s) {
         float4 *m = reinterpret_cast<float4 *>(take(f4));
         if (p)

@@ -461,7 +461,10 @@ __global__ void __launch_bounds__(256, VVPT_REGEN_MIN_BLOCKS) k_regen(JobTable j
         }
         if (flags & F_DONE) {
             const float total = (float)jt.jobs[job].params.total_samples;
-            cr += f3(ps.rad[slot]) / total;
+            float3 r = f3(ps.rad[slot]);
+            if (flags & F_NEE) // the emitter ray's contribution, after the shadow ray's
+                r = r + f3(ps.nee_c[slot]);
+            cr += r / total;
             ca += f3(ps.alb[slot]) / total;
             cn += f3(ps.nrm[slot]) / total;
             sample++;
@@ -767,6 +770,8 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         PathRng rng = load_rng(p, ps, slot);
         float3 beta = f3(ps.beta[slot]);
         float3 rad = f3(ps.rad[slot]);
+        if (flags & F_NEE) // the previous event's emitter ray (a path that continued with zfar > kExtTmax)
+            rad = rad + f3(ps.nee_c[slot]);
         float3 origin = f3(ps.o[slot]);
         float3 dir = f3(ps.d[slot]);
         uint32_t vol = ps.vol[slot];
@@ -1343,66 +1348,60 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
     return power_heuristic(nb.w, pdf) * T * em * f3(nb);
 }
 
-// Shadow rays of the events shaded this iteration.
+// Shadow rays of the events shaded this iteration, then the BSDF-direction
+// emitter rays of the paths that end at this event (their own queue, after
+// the shadow entries, in the same launch: the few long emitter walks overlap
+// the shadow rays instead of forming a launch of their own). An emitter ray's
+// contribution goes to nee_c, so the two parts never write the same word;
+// regen (or shade, for a path that continues) adds it after the shadow ray's,
+// in the order of the reference's additions.
 __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable jt, PathState ps, Queues q)
 {
-    const uint32_t n = q.counters[C_CONN];
+    const uint32_t nc = q.counters[C_CONN];
+    const uint32_t n = nc + q.counters[C_NEEQ];
     uint32_t err = 0;
-    uint32_t nsh = 0;
-    if (blockIdx.x * blockDim.x < n)
-        tlas_cache_fill(jt.jobs[ps.job[q.conn[blockIdx.x * blockDim.x]]].scene);
+    uint32_t nsh = 0, nnee = 0;
+    const uint32_t b0 = blockIdx.x * blockDim.x;
+    if (b0 < n)
+        tlas_cache_fill(jt.jobs[ps.job[b0 < nc ? q.conn[b0] : q.nee[b0 - nc]]].scene);
     else
         tlas_cache_none();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t slot = q.conn[i];
-        const uint32_t flags = ps.flags[slot];
-        if (!(flags & F_SHADOW))
-            continue;
-        const JobView &J = jt.jobs[ps.job[slot]];
-        const SceneView &s = J.scene;
-        const RenderParams &p = J.params;
-        const float4 sd = ps.sh_dir[slot];
-        const float3 T = shadow_transmittance(s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
-                                              ps.vol[slot], err);
-        if (!is_black(T))
-            ps.rad[slot] = f4(f3(ps.rad[slot]) + f3(ps.sh_c[slot]) * T, 0.0f);
-        ps.flags[slot] = flags & ~F_SHADOW;
-        nsh++;
+    for (uint32_t i = b0 + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (i < nc) {
+            const uint32_t slot = q.conn[i];
+            const uint32_t flags = ps.flags[slot];
+            if (!(flags & F_SHADOW))
+                continue;
+            const JobView &J = jt.jobs[ps.job[slot]];
+            const SceneView &s = J.scene;
+            const RenderParams &p = J.params;
+            const float4 sd = ps.sh_dir[slot];
+            const float3 T = shadow_transmittance(s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
+                                                  ps.vol[slot], err);
+            if (!is_black(T))
+                ps.rad[slot] = f4(f3(ps.rad[slot]) + f3(ps.sh_c[slot]) * T, 0.0f);
+            ps.flags[slot] = flags & ~F_SHADOW;
+            nsh++;
+        } else {
+            const uint32_t slot = q.nee[i - nc];
+            const uint32_t flags = ps.flags[slot]; // F_INSIDE; the shadow part may clear F_SHADOW meanwhile
+            const JobView &J = jt.jobs[ps.job[slot]];
+            const SceneView &s = J.scene;
+            const RenderParams &p = J.params;
+            const float4 nb = ps.nee_b[slot];
+            float3 emT, T, em;
+            float lpdf;
+            emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf,
+                        err);
+            float3 c = f3(0.0f);
+            if (!is_black(em))
+                c = power_heuristic(nb.w, lpdf) * T * em * f3(nb);
+            ps.nee_c[slot] = f4(c, 0.0f);
+            nnee++;
+        }
     }
     if (nsh)
         atomicAdd(&q.counters[C_SHADOW], nsh);
-    if (err)
-        atomicOr(&q.counters[C_ERR], err);
-}
-
-// BSDF-direction emitter rays of paths that end at this event (their next
-// extension ray is never traced, so the emitter ray cannot ride on it).
-__global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_emitter(JobTable jt, PathState ps, Queues q)
-{
-    const uint32_t n = q.counters[C_NEEQ];
-    uint32_t err = 0;
-    uint32_t nnee = 0;
-    if (blockIdx.x * blockDim.x < n)
-        tlas_cache_fill(jt.jobs[ps.job[q.nee[blockIdx.x * blockDim.x]]].scene);
-    else
-        tlas_cache_none();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t slot = q.nee[i];
-        const uint32_t flags = ps.flags[slot];
-        if (!(flags & F_NEE))
-            continue;
-        const JobView &J = jt.jobs[ps.job[slot]];
-        const SceneView &s = J.scene;
-        const RenderParams &p = J.params;
-        const float4 nb = ps.nee_b[slot];
-        float3 emT, T, em;
-        float lpdf;
-        emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf, err);
-        if (!is_black(em))
-            ps.rad[slot] = f4(f3(ps.rad[slot]) + power_heuristic(nb.w, lpdf) * T * em * f3(nb), 0.0f);
-        ps.flags[slot] = flags & ~F_NEE;
-        nnee++;
-    }
     if (nnee)
         atomicAdd(&q.counters[C_NEE], nnee);
     if (err)
@@ -1496,9 +1495,6 @@ void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Qu
         break;
     case K_SHADOW:
         k_shadow<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
-        break;
-    case K_EMITTER:
-        k_emitter<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
         break;
     default:
         break;

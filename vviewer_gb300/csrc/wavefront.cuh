@@ -50,6 +50,7 @@ struct PathState {
     float4 *sh_dir;  // shadow direction (xyz), tmax (w)
     float4 *sh_c;    // unoccluded light contribution (xyz)
     float4 *nee_b;   // beta for the emitter-ray contribution (xyz), BSDF pdf (w)
+    float4 *nee_c;   // emitter-ray contribution of a path flagged F_NEE (xyz), added by regen or shade
     uint32_t *rng;
     uint32_t *flags;
     uint32_t *vol;
@@ -85,7 +86,7 @@ struct Queues {
     uint32_t *shade_l, *shade_p, *shade_m;
     uint32_t *walk;     // paths whose pending emitter ray needs the full candidate walk
     uint32_t *conn;     // paths with a shadow ray
-    uint32_t *nee;      // paths that end with an emitter ray (k_emitter)
+    uint32_t *nee;      // paths that end with an emitter ray (k_shadow, after the shadow rays)
     uint32_t *regen[2];
     uint32_t *counters; // CounterIndex
 };
@@ -155,9 +156,8 @@ enum KernelId {
     K_PARTITION = 3,
     K_WALK = 4,
     K_SHADE = 5,
-    K_SHADOW = 6,
-    K_EMITTER = 7,
-    K_NUM = 8
+    K_SHADOW = 6, // shadow rays, then the emitter rays of paths that end
+    K_NUM = 7
 };
 constexpr int kKernelsPerIteration = K_NUM;
 void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Queues &q, int pingpong,
@@ -176,6 +176,5 @@ constexpr double kBytesShade = 4 + (4 + 4 + 4 + 4) + 5 * sizeof(float4) /* beta 
                                5 * sizeof(float4) /* alb nrm sh_dir sh_c nee_b */ + sizeof(float4) /* nee_b read */ +
                                2 * 4;
 constexpr double kBytesShadow = 4 + 4 + 4 + 4 * sizeof(float4) /* o sh_dir rad sh_c */ + sizeof(float4) + 4;
-constexpr double kBytesEmitter = 4 + 4 + 4 + 4 * sizeof(float4) /* o d nee_b rad */ + sizeof(float4) + 4;
 
 }  // namespace vvpt
