@@ -33,7 +33,7 @@ def load():
         lib = C.CDLL(str(LIB))
         lib.oracle_render.restype = C.c_int
         lib.oracle_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_int,
-                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_trace_closest.restype = C.c_int
         lib.oracle_trace_closest.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
         lib.oracle_set_sampler_tables.restype = None
@@ -57,10 +57,15 @@ def _sampler_tables(lib):
 
 
 def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threads: int = 0, fp64: bool = False,
-           env_is: bool = False, sampler: str = "rtgems"):
+           env_is: bool = False, sampler: str = "rtgems", alt_order: bool = False):
     """Renders with the oracle. Returns dict of H x W x 4 float32 arrays
     (radiance, albedo, normal, radiance_m2); pixels not in `pixels` stay 0.
-    sampler: 'rtgems' or 'pmj' (VVPT_RENDER_SAMPLER_PMJ)."""
+    sampler: 'rtgems' or 'pmj' (VVPT_RENDER_SAMPLER_PMJ).
+    alt_order: also return 'radiance_alt', the same render with every
+    BSDF-direction emitter ray's any-hit candidates taken in
+    instance-box-entry order rather than nearest first (the two ends of the
+    orders a hardware traversal may report them in; the paths are the same,
+    only those rays' contributions differ)."""
     from vviewer_gb300 import _native as N
 
     lib = load()
@@ -73,7 +78,8 @@ def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threa
         raise ValueError("sampler must be 'rtgems' or 'pmj'")
     ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
     H, W = info.height, info.width
-    out = {k: np.zeros((H, W, 4), dtype=np.float32) for k in ("radiance", "albedo", "normal", "radiance_m2")}
+    keys = ("radiance", "albedo", "normal", "radiance_m2") + (("radiance_alt",) if alt_order else ())
+    out = {k: np.zeros((H, W, 4), dtype=np.float32) for k in keys}
     px = None
     n = 0
     if pixels is not None:
@@ -81,9 +87,10 @@ def render(flat_scene, scene_data, info, pixels: np.ndarray | None = None, threa
         n = px.shape[0]
     threads = threads or (os.cpu_count() or 1)
     st = lib.oracle_render(C.addressof(desc), C.addressof(scene_data), C.addressof(ri),
-                           px.ctypes.data if px is not None else None, n, threads, 1 if fp64 else 0,
+                           px.ctypes.data if px is not None else None, n, threads,
+                           (1 if fp64 else 0) | (2 if alt_order else 0),
                            out["radiance"].ctypes.data, out["albedo"].ctypes.data, out["normal"].ctypes.data,
-                           out["radiance_m2"].ctypes.data)
+                           out["radiance_m2"].ctypes.data, out["radiance_alt"].ctypes.data if alt_order else None)
     if st != 0:
         raise RuntimeError(f"oracle_render failed with {st}")
     return out

@@ -900,6 +900,7 @@ struct Params {
     uint32_t W, H, batchSize, batches, depth, totalSamples, totalLights;
     uint32_t envLight = 0; // the environment is one more light of the pick
     uint32_t sampler = 0;  // 0: RTGEMS, 1: PMJ (VVPT_RENDER_SAMPLER_PMJ)
+    bool altOrder = false; // also render the emitter rays' other candidate order
 };
 
 // RayPayloadPrimary, shaders/pt/structs_pt.glsl:4-30
@@ -917,6 +918,7 @@ struct Payload {
     // PMJ sampler (structs_pt.glsl:24-29)
     uint32_t pmj = 0;
     uint32_t pixelX = 0, pixelY = 0, sampleIndex = 0, samplesPerPixel = 0;
+    V3 altDelta{0.0f, 0.0f, 0.0f}; // second image minus first, this sample
 };
 
 // ---- PMJ sampler, shaders/include/rng/rng_pmj.glsl:20-107, over the tables
@@ -1272,8 +1274,70 @@ LSR sampleLight(const Ctx &c, Payload &pl, V3 originPosition, bool allowEnv)
     return lsr;
 }
 
-// next_event_estimation.glsl with rayNEE.rahit/.rchit/.rmiss
-void nextEventEstimation(const Ctx &c, Payload &pl, float sampleDirectionPDF)
+// Entry distance of a ray into an instance's world box (the mesh box in
+// object space, entered along the object-space ray; same parameter t).
+float instance_entry(const Scene &s, uint32_t id, V3 o, V3 d, float tmin)
+{
+    const Inst &in = s.inst[id];
+    const Mesh &m = s.meshes[in.mesh];
+    V3 oo = xpoint(in.w2o, o), od = xvector(in.w2o, d);
+    float t0 = tmin;
+    for (int a = 0; a < 3; a++) {
+        float oa = comp(oo, a), da = comp(od, a);
+        float ta = (m.lo[a] - oa) / da, tb = (m.hi[a] - oa) / da;
+        if (std::isnan(ta) || std::isnan(tb))
+            continue;
+        if (ta > tb)
+            std::swap(ta, tb);
+        t0 = std::max(t0, ta);
+    }
+    return t0;
+}
+
+// Every candidate of a ray on [tmin, tmax] in instance-box-entry order: the
+// instances by the distance at which the ray enters their boxes (ties by
+// slot), each instance's candidates nearest first. This is the order a
+// stack traversal that visits the nearer child box first reports any-hit
+// candidates in when the instance boxes are TLAS leaves: a ray that starts
+// inside an instance's box sees all of that instance's candidates before
+// those of an instance it enters later, whatever their distances.
+std::vector<Hit> candidates_instance_order(const Scene &s, V3 o, V3 d, float tmin, float tmax)
+{
+    std::vector<Hit> all;
+    Hit after;
+    for (int k = 0; k < 4096; k++) {
+        Hit h = trace_after(s, o, d, tmin, tmax, after);
+        if (h.inst == NOHIT)
+            break;
+        all.push_back(h);
+        after = h;
+    }
+    std::vector<float> te(all.size());
+    for (size_t i = 0; i < all.size(); i++)
+        te[i] = instance_entry(s, all[i].inst, o, d, tmin);
+    std::vector<size_t> idx(all.size());
+    for (size_t i = 0; i < idx.size(); i++)
+        idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
+        if (te[a] != te[b])
+            return te[a] < te[b];
+        return all[a].inst < all[b].inst;
+    });
+    std::vector<Hit> r;
+    r.reserve(all.size());
+    for (size_t i : idx)
+        r.push_back(all[i]);
+    return r;
+}
+
+// next_event_estimation.glsl with rayNEE.rahit/.rchit/.rmiss. The any-hit
+// shader sees candidates in the order the hardware reports them; the defined
+// order here is nearest first (instanceOrder false). With instanceOrder the
+// walk takes the candidates in instance-box-entry order instead
+// (candidates_instance_order), the other end of what a traversal may report;
+// it only feeds the oracle's diagnostic second image. Returns the radiance
+// the emitter ray adds.
+V3 emitterRay(const Ctx &c, const Payload &pl, float sampleDirectionPDF, bool instanceOrder)
 {
     const float tmin = 0.0001f;
     const float tmax = c.p.zfar;
@@ -1289,8 +1353,18 @@ void nextEventEstimation(const Ctx &c, Payload &pl, float sampleDirectionPDF)
         Hit after;
         bool accepted = false;
         Hit acc;
+        std::vector<Hit> ordered;
+        if (instanceOrder)
+            ordered = candidates_instance_order(c.s, origin, dir, tmin, tmax);
         for (int guard = 0;; guard++) {
-            Hit h = trace_after(c.s, origin, dir, tmin, tmax, after);
+            Hit h;
+            if (instanceOrder) {
+                if (guard >= (int)ordered.size())
+                    break;
+                h = ordered[guard];
+            } else {
+                h = trace_after(c.s, origin, dir, tmin, tmax, after);
+            }
             if (h.inst == NOHIT)
                 break;
             const Inst &in = c.s.inst[h.inst];
@@ -1387,10 +1461,23 @@ void nextEventEstimation(const Ctx &c, Payload &pl, float sampleDirectionPDF)
         if (stop)
             break;
     }
-    if (!isBlack(emissive)) {
-        float w = PowerHeuristic(sampleDirectionPDF, pdf);
-        pl.radiance = pl.radiance + w * throughput * emissive * pl.beta;
+    if (isBlack(emissive))
+        return v3s(0.0f);
+    float w = PowerHeuristic(sampleDirectionPDF, pdf);
+    return w * throughput * emissive * pl.beta;
+}
+
+void nextEventEstimation(const Ctx &c, Payload &pl, float sampleDirectionPDF)
+{
+    V3 add = emitterRay(c, pl, sampleDirectionPDF, false);
+    if (c.p.altOrder) {
+        // the second image differs from the first only by what this emitter
+        // ray adds under the other candidate order
+        V3 alt = emitterRay(c, pl, sampleDirectionPDF, true);
+        pl.altDelta = pl.altDelta + (alt - add);
     }
+    if (!isBlack(add))
+        pl.radiance = pl.radiance + add;
 }
 
 void russianRoulette(Payload &pl)
@@ -1622,7 +1709,9 @@ inline void mat4mul(const float *m, float x, float y, float z, float w, float ou
 
 // raygen.rgen.glsl:24-145 for one pixel and one batch; returns the batch sums
 template <class Acc>
-void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, Acc cum[3])
+// cum[0..2]: radiance, albedo, normal; cum[3]: the radiance of the second
+// candidate order (Params::altOrder)
+void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, Acc cum[4])
 {
     const Params &p = c.p;
     Payload pl{};
@@ -1634,9 +1723,10 @@ void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, A
     pl.pixelY = py;
     float lensRadius = p.lensRadius, focalDistance = p.focalDistance;
     bool insideVolume = p.camVolume != -1;
-    for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 4; k++)
         cum[k] = Acc{0, 0, 0};
     for (uint32_t s = 0; s < p.batchSize; s++) {
+        pl.altDelta = v3s(0.0f);
         if (pl.pmj) {
             // raygen.rgen.glsl:57-61 (dimension start y * width + y, as written there)
             pl.rngState = py * p.W + py;
@@ -1697,6 +1787,10 @@ void raygen_batch(const Ctx &c, uint32_t px, uint32_t py, uint32_t batchIndex, A
         cum[0] = cum[0] + Acc{rr.x, rr.y, rr.z};
         cum[1] = cum[1] + Acc{aa.x, aa.y, aa.z};
         cum[2] = cum[2] + Acc{nn.x, nn.y, nn.z};
+        if (p.altOrder) {
+            V3 ra = (radiance + pl.altDelta) / total;
+            cum[3] = cum[3] + Acc{ra.x, ra.y, ra.z};
+        }
     }
 }
 
@@ -1858,10 +1952,14 @@ void oracle_set_sampler_tables(const float *pmj, const float *blue_noise)
 // Renders the listed pixels (all pixels when pixels == NULL) over every batch.
 // Outputs are W*H*4 floats (RGBA, A = 1); pixels not listed are left untouched.
 // fp64 != 0 accumulates the per-batch sums and the image in double precision.
+// options: bit 0 accumulates the radiance in double precision; bit 1 also
+// renders radiance_alt, the image with every emitter ray's candidates taken in
+// instance-box-entry order instead of nearest first (emitterRay).
 int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const vvpt_render_info *ri,
-                  const uint32_t *pixels, uint32_t num_pixels, int threads, int fp64, float *radiance, float *albedo,
-                  float *normal, float *radiance_m2)
+                  const uint32_t *pixels, uint32_t num_pixels, int threads, int options, float *radiance,
+                  float *albedo, float *normal, float *radiance_m2, float *radiance_alt)
 {
+    const bool fp64 = (options & 1) != 0;
     if (!desc || !sd || !ri || ri->width == 0 || ri->height == 0 || ri->batch_size == 0)
         return 1;
     Scene s;
@@ -1872,6 +1970,7 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
     set_env_light(s, ri, p);
     if (p.sampler && (!g_pmj || !g_blue_noise))
         return 3;
+    p.altOrder = (options & 2) != 0 && radiance_alt != nullptr;
     const Ctx c{s, p};
     const uint32_t npix = pixels ? num_pixels : p.W * p.H;
     if (threads <= 0)
@@ -1887,15 +1986,16 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
                 if (pix >= p.W * p.H)
                     continue;
                 uint32_t px = pix % p.W, py = pix / p.W;
-                double img[3][3] = {{0}};
-                float imgf[3][3] = {{0}};
+                double img[4][3] = {{0}};
+                float imgf[4][3] = {{0}};
                 double m2[3] = {0, 0, 0};
+                const int nq = p.altOrder ? 4 : 3;
                 if (p.depth > 0) {
                     for (uint32_t b = 0; b < p.batches; b++) {
                         if (fp64) {
-                            D3 cum[3];
+                            D3 cum[4];
                             raygen_batch(c, px, py, b, cum);
-                            for (int q = 0; q < 3; q++) {
+                            for (int q = 0; q < nq; q++) {
                                 img[q][0] += cum[q].x;
                                 img[q][1] += cum[q].y;
                                 img[q][2] += cum[q].z;
@@ -1904,9 +2004,9 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
                             m2[1] += cum[0].y * cum[0].y;
                             m2[2] += cum[0].z * cum[0].z;
                         } else {
-                            F3 cum[3];
+                            F3 cum[4];
                             raygen_batch(c, px, py, b, cum);
-                            for (int q = 0; q < 3; q++) {
+                            for (int q = 0; q < nq; q++) {
                                 imgf[q][0] = imgf[q][0] + cum[q].x;
                                 imgf[q][1] = imgf[q][1] + cum[q].y;
                                 imgf[q][2] = imgf[q][2] + cum[q].z;
@@ -1917,8 +2017,8 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
                         }
                     }
                 }
-                float *outs[3] = {radiance, albedo, normal};
-                for (int q = 0; q < 3; q++) {
+                float *outs[4] = {radiance, albedo, normal, p.altOrder ? radiance_alt : nullptr};
+                for (int q = 0; q < 4; q++) {
                     if (!outs[q])
                         continue;
                     for (int ch = 0; ch < 3; ch++)

@@ -6,7 +6,8 @@ the twelve golden images of src/bin/unittests/RenderTests.cpp whose scenes
 can be rebuilt from assets present in the reference tree. The GPU machines do
 not have the reference tree, so the tests read this file instead.
 
-Run: python tests/golden/make_fixtures.py [reference_root]
+Run: python tests/golden/make_fixtures.py <reference_root>
+(reference_root: the top of a kwstanths/vviewer checkout)
 """
 import sys
 from pathlib import Path
@@ -23,7 +24,7 @@ GOLDENS = ["FurnacePBR", "FurnaceLambert", "PointLight", "DirectionalLight", "Me
 MODELS = ["cube", "plane", "uvsphere"]
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str) -> None:
     ref = Path(ref_root)
     out = {}
     for m in MODELS:
@@ -39,4 +40,6 @@ def main(ref_root: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <reference_root>")
+    main(sys.argv[1])

@@ -260,3 +260,65 @@ def compare_images(test_rgb: np.ndarray, ref_rgb: np.ndarray) -> float:
     """CompareImages (RenderTests.cpp:7-33): MSE over the three channels."""
     d = test_rgb[..., :3].astype(np.float64) - ref_rgb[..., :3].astype(np.float64)
     return float((d * d).mean())
+
+
+ORDERS = Path(__file__).resolve().parent / "golden" / "meshlight_orders.npz"
+# Scenes whose golden depends on the order in which the hardware reported the
+# any-hit candidates of BSDF-direction emitter rays (rayNEE.rahit.glsl:43-131):
+# the emissive plane of MeshLight cuts into the glossy sphere, so rays that
+# reach the plane can also hit the sphere behind it, and the reference keeps
+# whichever candidate its traversal reported first. Data: the oracle's
+# full-image renders in the two end orders (tests/golden/make_meshlight_orders.py).
+ORDER_DEPENDENT = {"MeshLight"}
+
+
+@lru_cache(maxsize=1)
+def _orders():
+    z = np.load(ORDERS)
+    return z["pixels"].astype(np.int64), z["nearest"], z["alt"]
+
+
+def order_dependent_pixels(name: str):
+    """(pixel indices, nearest-first values, instance-order values) of the
+    pixels whose radiance depends on the emitter rays' candidate order, or
+    None for scenes where no pixel does."""
+    return _orders() if name in ORDER_DEPENDENT else None
+
+
+def golden_check_with_orders(name: str, radiance_rgb: np.ndarray, alt_rgb: np.ndarray | None = None):
+    """Compares a render (H x W x 3, nearest-first candidate order) with the
+    golden. Returns (mse_outside, bracketed, mse_bracket):
+      mse_outside: the reference's CompareImages MSE summed over the pixels
+        whose value does not depend on the candidate order (normalised by the
+        full image, so it is the full-image MSE when no pixel depends on it);
+      bracketed: fraction of the order-dependent pixel channels whose golden
+        value lies between this render and the instance-order render, within
+        one RGBE quantisation step of the golden;
+      mse_bracket: how far the golden lies outside that bracket, as a
+        full-image MSE.
+    alt_rgb (H x W x 3) overrides the stored instance-order values."""
+    from vviewer_gb300.assets import rgbe_encode
+
+    h, w = radiance_rgb.shape[:2]
+    gold_rgbe = golden_rgbe(name).reshape(-1, 4)
+    gold = rgbe_decode(gold_rgbe).astype(np.float64)
+    q = rgbe_decode(rgbe_encode(radiance_rgb.reshape(-1, 3).astype(np.float32))).astype(np.float64)
+    total = h * w * 3
+    dep = order_dependent_pixels(name)
+    mask = np.zeros(h * w, dtype=bool)
+    if dep is None:
+        return float(((q - gold) ** 2).sum() / total), 1.0, 0.0
+    pix, _, alt = dep
+    if alt_rgb is not None:
+        alt = alt_rgb.reshape(-1, 3)[pix]
+    mask[pix] = True
+    mse_outside = float(((q - gold) ** 2)[~mask].sum() / total)
+    qa = rgbe_decode(rgbe_encode(np.asarray(alt, dtype=np.float32))).astype(np.float64)
+    lo = np.minimum(q[pix], qa)
+    hi = np.maximum(q[pix], qa)
+    e = gold_rgbe[pix, 3].astype(np.int32)
+    step = np.where(e != 0, np.ldexp(1.0, e - 136), 0.0)[:, None]
+    g = gold[pix]
+    bracketed = float(((g >= lo - step) & (g <= hi + step)).mean())
+    mse_bracket = float(((g - np.clip(g, lo, hi)) ** 2).sum() / total)
+    return mse_outside, bracketed, mse_bracket
