@@ -316,7 +316,10 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx,
  * a fixed device-memory pool and forbid allocations they did not make,
  * processes under a hard memory cap, or frame loops that must not take the
  * implicit device synchronisation of the allocator. Same result as
- * vvpt_render (bit for bit). All scratch (parameters, counters, ray queues,
+ * vvpt_render (bit for bit), from the same render parameters (sizes checked
+ * the same way, VVPT_RENDER_ENV_IS honoured); the PMJ sampler, whose tables
+ * would need an allocation, is refused with VVPT_ERR_UNSUPPORTED. All scratch
+ * (parameters, counters, ray queues,
  * path state for up to 65,536 paths in flight, per-batch sums) comes from one
  * 64 MiB array the library defines at file scope, which every GPU that loads
  * the library holds until the process exits. Limit: the request must fit it:
@@ -326,8 +329,11 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx,
  * VVPT_ERR_INVALID_ARG before any GPU work. Outputs must be device buffers
  * (outputs->on_device = 1). The scene must already be resident
  * (vvpt_scene_upload allocates; this call does not).
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. All calls in the process share the
+ * The first call on a device looks up the array's device address and keeps
+ * it for the life of the process; make that first call before any stream
+ * capture, and do not call this entry point again after cudaDeviceReset (or
+ * any other teardown of the device's primary context) in the same process:
+ * the kept address would be stale. All calls in the process share the
  * array: calls that overlap on the GPU (two contexts on one device, or two
  * threads) race and corrupt each other's results, so serialise them. */
 VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx,

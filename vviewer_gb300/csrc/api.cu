@@ -895,11 +895,20 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
         return fail(ctx, VVPT_ERR_INVALID_ARG, "vvpt_render_noalloc writes device buffers only (outputs.on_device = 1)");
     if (info->flags & VVPT_RENDER_SAMPLER_PMJ)
         return fail(ctx, VVPT_ERR_UNSUPPORTED, "vvpt_render_noalloc renders with the RTGEMS sampler only");
-    if (info->width == 0 || info->height == 0 || info->batch_size == 0)
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "width, height and batch_size must be positive");
-    const uint64_t npix64 = (uint64_t)info->width * info->height;
-    const uint32_t batches = info->samples / info->batch_size;
-    const uint64_t items64 = npix64 * batches;
+    // The same parameters as vvpt_render, from the same function: it checks
+    // the sizes (width * height <= 2^28, width * height * batches < 2^32) and
+    // the camera volume, and sets every field, environment importance
+    // sampling included. With the RTGEMS sampler it allocates nothing.
+    RenderParams hp;
+    vvpt_status pst = make_render_params(ctx, scene, sd, info, hp);
+    if (pst != VVPT_OK)
+        return pst;
+    hp.want_m2 = out->radiance_m2 ? 1u : 0u;
+    // every product below is of checked sizes: items < 2^32, so the largest
+    // term, 3 * 16 * items, stays below 2^38
+    const uint64_t npix64 = (uint64_t)hp.width * hp.height;
+    const uint32_t batches = hp.batches;
+    const uint64_t items64 = hp.total_items;
     const uint64_t slots64 = std::max<uint64_t>(32, std::min<uint64_t>(items64, kNoAllocMaxSlots));
     auto aligned = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
     const uint64_t f4 = slots64 * sizeof(float4), u4 = slots64 * sizeof(uint32_t);
@@ -919,33 +928,6 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
     if (st != VVPT_OK)
         return st;
     cudaStream_t stream = vv_stream(ctx);
-
-    RenderParams hp{};
-    for (int c = 0; c < 4; c++) {
-        hp.view_inv[c] = make_float4(sd->view_inverse[c * 4 + 0], sd->view_inverse[c * 4 + 1],
-                                     sd->view_inverse[c * 4 + 2], sd->view_inverse[c * 4 + 3]);
-        hp.proj_inv[c] = make_float4(sd->projection_inverse[c * 4 + 0], sd->projection_inverse[c * 4 + 1],
-                                     sd->projection_inverse[c * 4 + 2], sd->projection_inverse[c * 4 + 3]);
-    }
-    hp.background = make_float3(sd->background[0], sd->background[1], sd->background[2]);
-    hp.env_type = sd->background[3];
-    hp.lens_radius = sd->exposure[2];
-    hp.focal_distance = sd->exposure[3];
-    hp.env_intensity = sd->exposure[1];
-    hp.zfar = sd->volumes[2];
-    hp.zfar_trunc = (float)(uint32_t)std::max(0.0f, sd->volumes[2]);
-    hp.cam_volume = (int32_t)sd->volumes[0];
-    if (hp.cam_volume != -1 && (hp.cam_volume < 0 || (uint32_t)hp.cam_volume >= scene->num_materials))
-        return fail(ctx, VVPT_ERR_INVALID_ARG, "camera volume material index out of range");
-    hp.width = info->width;
-    hp.height = info->height;
-    hp.batch_size = info->batch_size;
-    hp.batches = batches;
-    hp.depth = std::min(info->depth, 255u);
-    hp.total_samples = info->batch_size * batches;
-    hp.num_lights = scene->view.num_lights;
-    hp.total_items = (uint32_t)items64;
-    hp.want_m2 = out->radiance_m2 ? 1u : 0u;
 
     float4 *d_out[4] = {reinterpret_cast<float4 *>(out->radiance), reinterpret_cast<float4 *>(out->albedo),
                         reinterpret_cast<float4 *>(out->normal), reinterpret_cast<float4 *>(out->radiance_m2)};
