@@ -333,5 +333,9 @@ def write_hdr(path: str | Path, image: np.ndarray) -> None:
 
 
 def srgb_encode(linear: np.ndarray) -> np.ndarray:
-    x = np.clip(linear, 0.0, 1.0)
-    return np.where(x <= 0.0031308, x * 12.92, 1.055 * np.power(x, 1.0 / 2.4) - 0.055)
+    """linearToSRGB(clamp(x, 0, 1)) in float32 arithmetic, as
+    ImageUtils.cpp:12-21 evaluates it (float constants, powf)."""
+    x = np.clip(np.asarray(linear, dtype=np.float32), np.float32(0.0), np.float32(1.0))
+    lin = x * np.float32(12.92)
+    pw = np.float32(1.055) * np.power(x, np.float32(1.0) / np.float32(2.4)) - np.float32(0.055)
+    return np.where(x <= np.float32(0.0031308), lin, pw).astype(np.float32)

@@ -84,3 +84,32 @@ class Denoiser:
         h, w, _ = radiance.shape
         self.ctx.check(self.ctx.lib.vvpt_denoiser_apply(self.handle, radiance.data_ptr(), albedo.data_ptr(),
                                                         normal.data_ptr(), out.data_ptr(), w, h))
+
+    def save(self, path) -> None:
+        """Writes the network's parameters (float32) to an .npz file."""
+        np.savez_compressed(path, params=self.params())
+
+    def load(self, path) -> None:
+        """Reads parameters written by save()."""
+        with np.load(path) as z:
+            self.set_params(z["params"])
+
+
+class DenoiserStep:
+    """The denoising step of the output stage (the OIDN call of
+    VulkanRendererPathTracing.cpp:985-1018) over host images: radiance,
+    albedo and normal as the renderer returns them (H x W x 4 float32; the
+    normal buffer stored as n * 0.5 + 0.5, the form the network is trained
+    on). Returns the denoised radiance, alpha 1."""
+
+    def __init__(self, denoiser: Denoiser):
+        self.denoiser = denoiser
+
+    def denoise(self, radiance: np.ndarray, albedo: np.ndarray, normal: np.ndarray) -> np.ndarray:
+        import torch
+
+        bufs = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda() for x in (radiance, albedo, normal)]
+        out = torch.zeros_like(bufs[0])
+        self.denoiser.apply(*bufs, out)
+        torch.cuda.synchronize()
+        return out.cpu().numpy()

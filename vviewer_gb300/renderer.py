@@ -292,27 +292,35 @@ def write_png(path: str | Path, rgba8: np.ndarray) -> None:
 
 
 def write_to_disk(data: np.ndarray, filename: str, file_type: str) -> None:
-    """ImageUtils.cpp:51-76: RGBE HDR of the first three channels, or sRGB 8-bit PNG."""
+    """ImageUtils.cpp:51-76. "png": every channel, alpha included, becomes
+    uint8(255 * linearToSRGB(clamp(v, 0, 1))) (truncation, float32), written
+    as an 8-bit RGBA PNG; "hdr": RGBE of the first three channels (the
+    Radiance format has no alpha)."""
     if file_type == "png":
-        rgba = np.clip(data, 0.0, 1.0)
-        rgb8 = (255.0 * srgb_encode(rgba[..., :3])).astype(np.uint8)
-        a8 = (255.0 * srgb_encode(rgba[..., 3:4])).astype(np.uint8)
-        write_png(filename + ".png", np.concatenate([rgb8, a8], axis=-1))
-    else:
+        rgba = np.asarray(data, dtype=np.float32)
+        write_png(filename + ".png", (np.float32(255.0) * srgb_encode(rgba)).astype(np.uint8))
+    elif file_type == "hdr":
         write_hdr(filename + ".hdr", data)
+    else:
+        raise ValueError("writeToDisk(): Unsupported file type")
 
 
 def apply_exposure(data: np.ndarray, exposure: float) -> np.ndarray:
-    out = data.copy()
-    out[..., :3] = out[..., :3] * np.float32(2.0 ** exposure)
+    """ImageUtils.cpp:34-49: v * 2^exposure on the first three channels."""
+    out = np.array(data, dtype=np.float32, copy=True)
+    out[..., :3] = out[..., :3] * np.float32(np.power(np.float32(2.0), np.float32(exposure)))
     return out
 
 
 class RendererPathTracing:
     """engine.renderer().rendererPathTracing() of the reference."""
 
-    def __init__(self, engine: Engine, device: int = 0, context: Context | None = None):
+    def __init__(self, engine: Engine, device: int = 0, context: Context | None = None, denoiser=None):
         self.engine = engine
+        # denoise=True runs this (the OIDN step of storeToDisk): any object
+        # with denoise(radiance, albedo, normal) -> radiance over H x W x 4
+        # float32 arrays, e.g. DenoiserStep over a trained Denoiser
+        self.denoiser = denoiser
         self._ctx = context
         self._device = device
         self._info = RenderInfo()
@@ -366,13 +374,22 @@ class RendererPathTracing:
             self._in_progress = False
 
     def store_to_disk(self, res: RenderResult) -> None:
+        """VulkanRendererPathTracing.cpp:958-1027: with writeAllFiles the
+        albedo and normal AOVs as HDR; without denoising the radiance, exposed
+        for PNG only; with denoising also the noisy radiance as
+        `<name>_radiance.hdr`, then the denoised image, exposed for PNG."""
         info = self._info
         if info.write_all_files:
             write_to_disk(res.albedo, info.filename + "_albedo", "hdr")
             write_to_disk(res.normal, info.filename + "_normal", "hdr")
         radiance = res.radiance
         if info.denoise:
-            raise NotImplementedError("denoise=True needs the learned denoiser, which this build does not ship yet")
+            if self.denoiser is None:
+                raise ValueError("denoise=True needs a denoiser: set RendererPathTracing.denoiser "
+                                 "(e.g. DenoiserStep over a trained Denoiser)")
+            if info.write_all_files:
+                write_to_disk(radiance, info.filename + "_radiance", "hdr")
+            radiance = np.asarray(self.denoiser.denoise(res.radiance, res.albedo, res.normal), dtype=np.float32)
         if info.file_type == "png" and info.exposure != 0.0:
             radiance = apply_exposure(radiance, info.exposure)
         write_to_disk(radiance, info.filename, info.file_type)
