@@ -1975,6 +1975,62 @@ int oracle_render(const vvpt_scene_desc *desc, const vvpt_scene_data *sd, const 
     const uint32_t npix = pixels ? num_pixels : p.W * p.H;
     if (threads <= 0)
         threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (fp64 && !p.altOrder && p.depth > 0 && p.batches >= 128 && npix < 4u * (uint32_t)threads) {
+        // Few pixels and many batches (converged reference images): each
+        // pixel's batches are split into chunks of 64 rendered in parallel,
+        // and the chunks' double-precision sums are added in chunk order.
+        const uint32_t chunk = 64, nchunks = (p.batches + chunk - 1) / chunk;
+        const uint64_t units = (uint64_t)npix * nchunks;
+        std::vector<double> part(units * 12, 0.0);
+        std::atomic<uint64_t> nextu{0};
+        auto workc = [&]() {
+            for (;;) {
+                const uint64_t u = nextu.fetch_add(1);
+                if (u >= units)
+                    break;
+                const uint32_t k = (uint32_t)(u / nchunks), ch = (uint32_t)(u % nchunks);
+                const uint32_t pix = pixels ? pixels[k] : k;
+                if (pix >= p.W * p.H)
+                    continue;
+                double *acc = &part[u * 12];
+                for (uint32_t b = ch * chunk; b < std::min(p.batches, (ch + 1) * chunk); b++) {
+                    D3 cum[4];
+                    raygen_batch(c, pix % p.W, pix / p.W, b, cum);
+                    for (int q = 0; q < 3; q++) {
+                        acc[3 * q + 0] += cum[q].x;
+                        acc[3 * q + 1] += cum[q].y;
+                        acc[3 * q + 2] += cum[q].z;
+                    }
+                    acc[9] += cum[0].x * cum[0].x;
+                    acc[10] += cum[0].y * cum[0].y;
+                    acc[11] += cum[0].z * cum[0].z;
+                }
+            }
+        };
+        std::vector<std::thread> cpool;
+        for (int t = 0; t < threads; t++)
+            cpool.emplace_back(workc);
+        for (auto &t : cpool)
+            t.join();
+        float *outs[4] = {radiance, albedo, normal, radiance_m2};
+        for (uint32_t k = 0; k < npix; k++) {
+            const uint32_t pix = pixels ? pixels[k] : k;
+            if (pix >= p.W * p.H)
+                continue;
+            double sum[12] = {0};
+            for (uint32_t ch = 0; ch < nchunks; ch++)
+                for (int i = 0; i < 12; i++)
+                    sum[i] += part[((uint64_t)k * nchunks + ch) * 12 + i];
+            for (int q = 0; q < 4; q++) {
+                if (!outs[q])
+                    continue;
+                for (int chn = 0; chn < 3; chn++)
+                    outs[q][4 * (size_t)pix + chn] = (float)sum[3 * q + chn];
+                outs[q][4 * (size_t)pix + 3] = 1.0f;
+            }
+        }
+        return 0;
+    }
     std::atomic<uint32_t> next{0};
     auto work = [&]() {
         for (;;) {

@@ -333,3 +333,92 @@ def test_png_row_filters(ft):
     img = np.random.default_rng(ft).integers(0, 256, (9, 11, 4), dtype=np.uint8)
     dec, channels = decode_png(_encode_filtered(img, ft))
     assert channels == 4 and (dec == img).all()
+
+
+def _grey_png(path, img):
+    """8-bit greyscale PNG (colour type 0)."""
+    h, w = img.shape
+    raw = b"".join(b"\x00" + img[y].astype(np.uint8).tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    path.write_bytes(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 0, 0, 0, 0)) +
+                     chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+def _obj_with_mtl(tmp_path):
+    """Two objects; 'Box' has faces before any usemtl, then under 'red', then
+    under 'textured'; 'Panel' uses 'bumpy' and an undefined material."""
+    rgba = np.zeros((4, 4, 4), dtype=np.uint8)
+    rgba[..., 0] = 200
+    rgba[..., 3] = np.arange(16, dtype=np.uint8).reshape(4, 4) * 16
+    write_png(tmp_path / "albedo.png", rgba)
+    write_png(tmp_path / "normal.png", np.full((2, 2, 3), 128, dtype=np.uint8))
+    _grey_png(tmp_path / "height.png", np.full((2, 2), 77, dtype=np.uint8))
+    (tmp_path / "mats.mtl").write_text(
+        "# two-material library\n"
+        "newmtl red\nKd 0.8 0.1 0.1\nKs 0.2 0.2 0.2\nNs 25\n"
+        "newmtl textured\nKd 0 0 0\nKs 0 0 0\nNs 100\nmap_Kd albedo.png\n"
+        "newmtl bumpy\nKd 0.5 0.5 0.5\nKs 0.5 0.25 0\nNs 50\nmap_Bump -bm 1.0 normal.png\n"
+        "newmtl flat\nKd 0 0 0\nKs 0.3 0.2 0.1\nNs 10\nbump height.png\n")
+    (tmp_path / "model.obj").write_text(
+        "mtllib mats.mtl\n"
+        "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\nvn 0 0 1\n"
+        "o Box\nf 1/1/1 2/2/1 3/3/1\nusemtl red\nf 1/1/1 3/3/1 4/4/1\nusemtl textured\nf 1/1/1 2/2/1 3/3/1 4/4/1\n"
+        "o Panel\nusemtl bumpy\nf 1/1/1 2/2/1 3/3/1\nusemtl missing\nf 1/1/1 3/3/1 4/4/1\nusemtl flat\nf 2/2/1 3/3/1 4/4/1\n")
+    return tmp_path / "model.obj"
+
+
+def test_obj_mtl_materials_follow_the_reference(tmp_path):
+    """assimpLoadMaterialsOBJ (AssimpLoadModel.cpp:252-363) over assimp's OBJ
+    import: materials "<stem>:<name>" with the importer's default first,
+    PBR values derived from Kd / Ks / Ns, textures from map_Kd and map_Bump,
+    and one mesh per run of faces under one material."""
+    e = Engine()
+    model = import_model(e, _obj_with_mtl(tmp_path), name="m")
+    names = [m.name for m in model.materials]
+    assert names == ["model:DefaultMaterial", "model:red", "model:textured", "model:bumpy", "model:flat"]
+    mats = {m.name.split(":")[1]: m for m in model.materials}
+    f = np.float32
+    d = mats["DefaultMaterial"]
+    assert d.albedo == [0.6, 0.6, 0.6, 1.0] and d.metallic == 0.0 and d.roughness == 1.0
+    r = mats["red"]
+    assert np.allclose(r.albedo, [0.8, 0.1, 0.1, 1.0])
+    assert r.metallic == float(f(1) - f(0.8) / (f(0.8) + f(0.2))) and r.roughness == float(f(1) - f(25) / f(100))
+    assert r.albedo_texture == TEX_WHITE_COLOR
+    t = mats["textured"]
+    # a black Kd with a diffuse texture becomes white; four channels: alpha
+    # texture and a transparent material
+    assert t.albedo == [1.0, 1.0, 1.0, 1.0] and t.albedo_texture != TEX_WHITE_COLOR
+    assert t.roughness == 0.0 and t.metallic == 0.0
+    built = t.pack()
+    assert built.metallic_roughness_ao[3] == 1.0  # transparent
+    alpha = e.textures[built.textures2[3]][1]
+    assert np.array_equal(alpha[..., 0], (np.arange(16).reshape(4, 4) * 16).astype(np.uint8))
+    b = mats["bumpy"]
+    assert b.normal_texture != mats["red"].normal_texture  # map_Bump with options before the file
+    fl = mats["flat"]
+    # black Kd, non-black Ks: albedo takes Ks; a one-channel map_Bump is not a normal map
+    assert np.allclose(fl.albedo[:3], [0.3, 0.2, 0.1]) and fl.normal_texture == mats["red"].normal_texture
+    assert fl.metallic == 1.0
+    # meshes per run of faces under one material, nodes per object
+    assert [n.name for n in model.root.children] == ["Box", "Panel"]
+    box, panel = model.root.children
+    assert [m.name for m in box.meshes] == ["Box", "Box-1", "Box-2"]
+    assert [m.name.split(":")[1] for m in box.materials] == ["DefaultMaterial", "red", "textured"]
+    assert [m.indices.shape[0] for m in box.meshes] == [1, 1, 2]
+    assert [m.name.split(":")[1] for m in panel.materials] == ["bumpy", "DefaultMaterial", "flat"]
+    # placed as the reference places a model: its meshes with their materials
+    add_model3d(e.scene, None, model)
+    fs = e.scene.build()
+    used = sorted({int(i.material_index) for i in fs.instances})
+    assert len(used) == 5
+
+
+def test_obj_without_materials_keeps_one_mesh(tmp_path):
+    p = tmp_path / "tri.obj"
+    p.write_text("o Tri\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    model = import_model(Engine(), p, import_materials=False)
+    assert list(model.meshes_by_name) == ["Tri"] and model.materials == []
+    assert model.root.children[0].materials == [None]

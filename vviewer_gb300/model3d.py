@@ -53,7 +53,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _native as N
-from .assets import calc_tangent_space, load_obj
+from .assets import calc_tangent_space
 from .scene import VERTEX_DTYPE, Engine, Material, MaterialPBRStandard, Mesh, Scene, SceneObject, Transform
 
 f32 = np.float32
@@ -526,13 +526,180 @@ def _load_gltf(engine: Engine, path: Path, name: str, import_materials: bool) ->
     return Model3D(name, _flatten(root), by_name, materials)
 
 
-def _load_obj_model(engine: Engine, path: Path, name: str) -> Model3D:
-    """An OBJ model: assimp's root node (named after the file) over one node
-    holding the mesh. The OBJ's own materials are not read: the objects get
-    the override material or the engine's default material."""
-    mesh = engine.add_mesh(load_obj(path))
-    child = ModelNode(mesh.name, Transform(), [mesh], [None])
-    return Model3D(name, ModelNode(path.name, Transform(), [], [], [child]), {mesh.name: mesh}, [])
+# ---------------------------------------------------------------- OBJ with .mtl materials
+
+def _obj_groups(text: str):
+    """Parses an OBJ file into (V, VT, VN, mtllib files, groups). A group is a
+    run of faces of one object ('o') under one material ('usemtl'): the
+    importer (assimp 5.2.5's OBJ loader) starts a new mesh at each change of
+    either. Each group: (object name, material name or None, faces as corner
+    lists of 1-based (v, vt, vn) indices)."""
+    v, vt, vn = [], [], []
+    libs, groups = [], []
+    obj, mtl = "defaultobject", None
+    for line in text.splitlines():
+        parts = line.split()
+        if not parts or parts[0].startswith("#"):
+            continue
+        tag = parts[0]
+        if tag == "v":
+            v.append([float(x) for x in parts[1:4]])
+        elif tag == "vt":
+            vt.append([float(x) for x in parts[1:3]])
+        elif tag == "vn":
+            vn.append([float(x) for x in parts[1:4]])
+        elif tag == "o" and len(parts) > 1:
+            obj = parts[1]
+        elif tag == "usemtl" and len(parts) > 1:
+            mtl = " ".join(parts[1:])
+        elif tag == "mtllib" and len(parts) > 1:
+            libs.append(" ".join(parts[1:]))
+        elif tag == "f":
+            corners = []
+            for c in parts[1:]:
+                idx = c.split("/")
+                corners.append((int(idx[0]), int(idx[1]) if len(idx) > 1 and idx[1] else 0,
+                                int(idx[2]) if len(idx) > 2 and idx[2] else 0))
+            if not groups or groups[-1][0] != obj or groups[-1][1] != mtl:
+                groups.append((obj, mtl, []))
+            groups[-1][2].append(corners)
+    return (np.array(v, dtype=f32).reshape(-1, 3), np.array(vt, dtype=f32).reshape(-1, 2),
+            np.array(vn, dtype=f32).reshape(-1, 3), libs, groups)
+
+
+def _mtl_materials(text: str) -> list[dict]:
+    """.mtl entries as assimp's OBJ material importer reads them: Kd (default
+    0.6 grey), Ks (default black), Ns (default 0), map_Kd, and map_Bump /
+    bump as the height texture (texture options before the file name are
+    skipped: the file is the last token)."""
+    out = []
+    cur = None
+    for line in text.splitlines():
+        parts = line.split()
+        if not parts or parts[0].startswith("#"):
+            continue
+        tag = parts[0]
+        if tag == "newmtl":
+            cur = {"name": " ".join(parts[1:]), "Kd": [0.6, 0.6, 0.6], "Ks": [0.0, 0.0, 0.0], "Ns": 0.0}
+            out.append(cur)
+        elif cur is None:
+            continue
+        elif tag in ("Kd", "Ks") and len(parts) > 1:
+            vals = [float(x) for x in parts[1:4]]
+            cur[tag] = vals if len(vals) == 3 else [vals[0]] * 3
+        elif tag == "Ns" and len(parts) > 1:
+            cur["Ns"] = float(parts[1])
+        elif tag == "map_Kd" and len(parts) > 1:
+            cur["map_Kd"] = parts[-1]
+        elif tag in ("map_Bump", "map_bump", "bump") and len(parts) > 1:
+            cur["map_Bump"] = parts[-1]
+    return out
+
+
+def _obj_material(engine: Engine, folder: Path, stem: str, m: dict, cache: dict) -> Material:
+    """assimpLoadMaterialsOBJ (AssimpLoadModel.cpp:252-363) for one .mtl entry:
+    a PBR material "<file stem>:<name>" with albedo Kd; a map_Kd image gives
+    the albedo texture (sRGB; a black Kd becomes white) and, with four
+    channels, an alpha texture from its alpha channel and a transparent
+    material; metallic = 1 - max(Kd) / (max(Kd) + max(Ks)); roughness =
+    1 - Ns / 100; a black Kd with a non-black Ks takes Ks as albedo; a
+    map_Bump image that is not one-channel is the normal map (linear)."""
+    mat = engine.create_material(MaterialPBRStandard, f"{stem}:{m['name']}")
+    albedo = [float(c) for c in m["Kd"]] + [1.0]
+
+    def image(file: str):
+        if file not in cache:
+            fp = folder / file
+            try:
+                data = fp.read_bytes()
+            except OSError as e:
+                warnings.warn(f"{fp}: {e}; the slot stays untextured")
+                data = None
+            cache[file] = _decode_image(data, str(fp)) if data is not None else None
+        return cache[file]
+
+    if "map_Kd" in m:
+        dec = image(m["map_Kd"])
+        if dec is not None:
+            rgba, channels = dec
+            mat.albedo_texture = engine.add_texture(N.TEXTURE_RGBA8_SRGB, rgba)
+            if max(albedo[:3]) == 0.0 and min(albedo[:3]) == 0.0:
+                albedo[:3] = [1.0, 1.0, 1.0]
+            if channels == 4:
+                mat.alpha_texture = engine.add_texture(N.TEXTURE_RGBA8_LINEAR, _channel_texture(rgba, 3))
+                if albedo[3] == 0.0:
+                    albedo[3] = 1.0
+                mat.set_transparent(True)
+    ks = [float(c) for c in m["Ks"]]
+    diffuse_amount = f32(max(albedo[:3]))
+    specular_amount = f32(max(ks))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        mat.metallic = float(f32(1.0) - diffuse_amount / (diffuse_amount + specular_amount))
+    mat.roughness = float(f32(1.0) - f32(m["Ns"]) / f32(100.0))
+    if max(albedo[:3]) == 0.0 and min(albedo[:3]) == 0.0 and specular_amount != 0.0:
+        albedo[:3] = ks
+    mat.albedo = albedo
+    mat.ao = 1.0
+    if "map_Bump" in m:
+        dec = image(m["map_Bump"])
+        if dec is not None and dec[1] != 1:
+            mat.normal_texture = engine.add_texture(N.TEXTURE_RGBA8_LINEAR, dec[0])
+    return mat
+
+
+def _load_obj_model(engine: Engine, path: Path, name: str, import_materials: bool = True) -> Model3D:
+    """An OBJ model as assimp hands it to vengine: a root node named after the
+    file over one node per object, whose meshes are the object's runs of
+    faces under one material. The first mesh of an object takes the object's
+    name, later ones "<object>-<k>" (k = 1, 2, ...). With import_materials the
+    materials come from the .mtl files the OBJ names (mtllib), in the
+    importer's order: its default material "DefaultMaterial" (grey 0.6) first,
+    then the files' entries; faces before any usemtl, or naming a material no
+    file defines, use the default one."""
+    from .assets import mesh_from_obj_arrays
+
+    V, VT, VN, libs, groups = _obj_groups(path.read_text())
+    stem = path.stem
+    by_name: dict = {}
+    mats: dict = {}
+    materials: list = []
+    if import_materials:
+        entries = [{"name": "DefaultMaterial", "Kd": [0.6, 0.6, 0.6], "Ks": [0.0, 0.0, 0.0], "Ns": 0.0}]
+        for lib in libs:
+            fp = path.parent / lib
+            try:
+                entries += _mtl_materials(fp.read_text())
+            except OSError as e:
+                warnings.warn(f"{fp}: {e}; its materials are not loaded")
+        cache: dict = {}
+        for m in entries:
+            if m["name"] not in mats:
+                mats[m["name"]] = _obj_material(engine, path.parent, stem, m, cache)
+                materials.append(mats[m["name"]])
+    nodes: dict = {}
+    counts: dict = {}
+    for obj, mtl, faces in groups:
+        tris = [(f[0], f[k], f[k + 1]) for f in faces for k in range(1, len(f) - 1)]
+        corners = np.zeros((len(tris), 3, 3), dtype=np.int64)
+        for t, tri in enumerate(tris):
+            for c in range(3):
+                vi, ti, ni = tri[c]
+                corners[t, c] = (_obj_index(vi, len(V)) + 1, (_obj_index(ti, len(VT)) + 1) if ti else 0,
+                                 (_obj_index(ni, len(VN)) + 1) if ni else 0)
+        k = counts.get(obj, 0)
+        counts[obj] = k + 1
+        mesh_name = obj if k == 0 else f"{obj}-{k}"
+        mesh = engine.add_mesh(mesh_from_obj_arrays(mesh_name, V, VT, VN, corners.reshape(-1, 3)))
+        by_name[mesh_name] = mesh
+        if obj not in nodes:
+            nodes[obj] = ModelNode(obj, Transform(), [], [])
+        nodes[obj].meshes.append(mesh)
+        nodes[obj].materials.append(mats.get(mtl, mats.get("DefaultMaterial")) if import_materials else None)
+    return Model3D(name, ModelNode(path.name, Transform(), [], [], list(nodes.values())), by_name, materials)
+
+
+def _obj_index(i: int, n: int) -> int:
+    return i - 1 if i > 0 else n + i
 
 
 def import_model(engine: Engine, path: str | Path, name: str | None = None,
@@ -549,7 +716,7 @@ def import_model(engine: Engine, path: str | Path, name: str | None = None,
     if ext in (".gltf", ".glb"):
         model = _load_gltf(engine, path, name, import_materials)
     elif ext == ".obj":
-        model = _load_obj_model(engine, path, name)
+        model = _load_obj_model(engine, path, name, import_materials)
     else:
         raise ValueError(f"{path}: model format {ext or '(none)'} is not supported (glTF, GLB, OBJ)")
     models[name] = model
