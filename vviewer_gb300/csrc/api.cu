@@ -576,7 +576,7 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                     prof.kernels[k].launches += 1;
                     prof.kernels[k].units += units;
                     prof.kernels[k].total_ms += ms;
-                    stats.kernel_launches += 1;
+                    stats.kernel_launches += launches_of(k);
                 }
                 VV_CUDA(cudaMemcpy(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost),
                         "read counters");
@@ -994,7 +994,7 @@ VVPT_API vvpt_status vvpt_render_noalloc(vvpt_ctx *ctx, vvpt_scene *scene, const
                 launch_kernel((KernelId)kk, jt, ps, q, (int)(it & 1), shape, stream);
             it++;
         }
-        stats.kernel_launches += 8 * K_NUM;
+        stats.kernel_launches += 8 * kKernelsPerIteration;
         VV_CUDA(cudaGetLastError(), "launch iteration");
         VV_CUDA(cudaMemcpyAsync(ctx->counters_pinned, q.counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 stream),

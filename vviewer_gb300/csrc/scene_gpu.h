@@ -29,12 +29,19 @@ static_assert(sizeof(BVHNode) == 64, "BVHNode must be 64 bytes");
 
 // Bottom-level acceleration structures use the binary nodes above
 // (VVPT_BLAS_WIDE = 0, the default) or compressed 8-wide nodes
-// (VVPT_BLAS_WIDE = 1, a build option). Both give the same closest hits; on
-// GB300 the binary layout traverses faster (the wide one visits 2.7x fewer
-// BLAS nodes per ray but spends more instructions per visit, and the
-// traversal kernels are issue-bound under divergence).
+// (VVPT_BLAS_WIDE = 1, a build option). Both give the same closest hits. With
+// the wide nodes the traversal kernels trace one ray per lane, or with
+// VVPT_GROUP_TRAVERSAL = 1 one ray per group of eight lanes (a child slot or
+// a triangle per lane). On GB300 the binary layout with one ray per lane is
+// the fastest: the traversal kernels are issue-bound under divergence, the
+// wide nodes cost more instructions per visit, and eight lanes per ray leave
+// too few rays in flight to cover the memory latency of each node fetch.
+// The TLAS uses binary nodes in every form.
 #ifndef VVPT_BLAS_WIDE
 #define VVPT_BLAS_WIDE 0
+#endif
+#ifndef VVPT_GROUP_TRAVERSAL
+#define VVPT_GROUP_TRAVERSAL 0
 #endif
 
 // Compressed 8-wide node (80 bytes, five 128-bit loads). Child box planes are

@@ -171,14 +171,41 @@ __device__ __forceinline__ float cull_slack(const SceneView &s, const float3 &o,
     return dm > 0.0f ? 1e-5f * (s.cull_o * om + s.cull_r) / dm : 0.0f;
 }
 
+// Loads of BVH nodes and triangles. On the device they carry an L2
+// evict-last policy (VVPT_SCENE_L2_KEEP, default on): the scene's nodes and
+// triangles are re-read by every traversal kernel, while the path state and
+// queues stream through L2 once per kernel, so the scene's lines are the
+// ones to keep.
+#ifndef VVPT_SCENE_L2_KEEP
+#define VVPT_SCENE_L2_KEEP 1
+#endif
+#if defined(__CUDA_ARCH__) && VVPT_SCENE_L2_KEEP
+__device__ __forceinline__ uint64_t scene_l2_policy()
+{
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float4 ldg_scene(const float4 *p)
+{
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p), "l"(scene_l2_policy()));
+    return v;
+}
+#else
+__device__ __forceinline__ float4 ldg_scene(const float4 *p) { return __ldg(p); }
+#endif
+
 __device__ __forceinline__ BVHNode load_node(const BVHNode *nodes, int idx)
 {
     const float4 *p = reinterpret_cast<const float4 *>(nodes + idx);
     BVHNode n;
-    n.lxy = __ldg(p + 0);
-    n.rxy = __ldg(p + 1);
-    n.lrz = __ldg(p + 2);
-    float4 c = __ldg(p + 3);
+    n.lxy = ldg_scene(p + 0);
+    n.rxy = ldg_scene(p + 1);
+    n.lrz = ldg_scene(p + 2);
+    float4 c = ldg_scene(p + 3);
     n.c = make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z), __float_as_int(c.w));
     return n;
 }
@@ -417,7 +444,7 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
 #endif
         if (leaf_count > 0) {
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
-            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            const float4 p0 = ldg_scene(tp), p1 = ldg_scene(tp + 1), p2 = ldg_scene(tp + 2);
             const uint32_t prim = __float_as_uint(p0.w);
             float t, u, v;
             if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
@@ -521,6 +548,255 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
     }
     return best;
 }
+
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL && defined(__CUDACC__)
+// ---------------------------------------------------------------------------
+// Cooperative traversal: eight consecutive lanes of a warp (a lane group)
+// trace one ray together. Every lane holds the same traversal state (ray,
+// best hit, stack) and takes the same branches; the two steps that carry the
+// work are spread over the lanes: a wide BLAS node visit tests one child slot
+// per lane, and a triangle step tests up to eight of the pending triangles at
+// once, the nearest (t, primitive) winning through a group reduction. A warp
+// holds four groups, so a warp instruction serves up to four rays' node or
+// triangle work with eight lanes each, where the one-ray-per-lane loop above
+// ran at about six active lanes per instruction under divergence. The result
+// is the same closest hit: candidate order does not matter to the
+// (t, instance, primitive) minimum, and the node tests keep their margins.
+struct LaneGroup {
+    uint32_t mask; // the group's eight lanes
+    int gl;        // this lane's index in the group (0..7)
+};
+
+__device__ __forceinline__ LaneGroup lane_group()
+{
+    LaneGroup g;
+    const int lane = (int)(threadIdx.x & 31u);
+    g.gl = lane & 7;
+    g.mask = 0xFFu << (lane & 24);
+    return g;
+}
+
+__device__ __forceinline__ float fmin3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// wide_visit with lane gl testing child slot gl ^ oct: the ballot bit of lane
+// gl is then the node-group bit of that slot (bit = slot ^ oct). Same plane
+// reconstruction and margins as wide_visit.
+__device__ __forceinline__ void wide_visit_group(const float4 (&w)[5], const float3 &o, const float3 &invd,
+                                                 uint32_t oct, float tmin, float tmax, const LaneGroup &g,
+                                                 uint32_t &node_bits, uint32_t &imask, uint32_t &child_base,
+                                                 uint32_t &tri_base, uint32_t &tri_bits)
+{
+    const uint32_t eim = __float_as_uint(w[0].w);
+    const float ax = __fmul_rn(__uint_as_float((eim & 0xffu) << 23), invd.x);
+    const float ay = __fmul_rn(__uint_as_float(((eim >> 8) & 0xffu) << 23), invd.y);
+    const float az = __fmul_rn(__uint_as_float(((eim >> 16) & 0xffu) << 23), invd.z);
+    const float bx = __fmul_rn(__fsub_rn(w[0].x, o.x), invd.x);
+    const float by = __fmul_rn(__fsub_rn(w[0].y, o.y), invd.y);
+    const float bz = __fmul_rn(__fsub_rn(w[0].z, o.z), invd.z);
+    const float kUlps = 8.0f * 5.9604645e-08f; // 8 x 2^-24
+    const float mx = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(ax), fabsf(bx)));
+    const float my = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(ay), fabsf(by)));
+    const float mz = __fmul_rn(kUlps, __fmaf_rn(255.0f, fabsf(az), fabsf(bz)));
+    imask = eim >> 24;
+    child_base = __float_as_uint(w[1].x);
+    tri_base = __float_as_uint(w[1].y);
+    const uint32_t slot = (uint32_t)g.gl ^ oct;
+    const int h = (int)(slot >> 2), k = (int)(slot & 3u);
+    const bool nx = (oct & 1u) != 0, ny = (oct & 2u) != 0, nz = (oct & 4u) != 0;
+    // this slot's near / far plane words per axis: lo (w2.xy, w2.zw, w3.xy), hi (w3.zw, w4.xy, w4.zw)
+    const uint32_t lox = __float_as_uint(h ? w[2].y : w[2].x), hix = __float_as_uint(h ? w[3].w : w[3].z);
+    const uint32_t loy = __float_as_uint(h ? w[2].w : w[2].z), hiy = __float_as_uint(h ? w[4].y : w[4].x);
+    const uint32_t loz = __float_as_uint(h ? w[3].y : w[3].x), hiz = __float_as_uint(h ? w[4].w : w[4].z);
+    const float tnx = __fmaf_rn(byte_as_float(nx ? hix : lox, k), ax, __fsub_rn(bx, mx));
+    const float tfx = __fmaf_rn(byte_as_float(nx ? lox : hix, k), ax, __fadd_rn(bx, mx));
+    const float tny = __fmaf_rn(byte_as_float(ny ? hiy : loy, k), ay, __fsub_rn(by, my));
+    const float tfy = __fmaf_rn(byte_as_float(ny ? loy : hiy, k), ay, __fadd_rn(by, my));
+    const float tnz = __fmaf_rn(byte_as_float(nz ? hiz : loz, k), az, __fsub_rn(bz, mz));
+    const float tfz = __fmaf_rn(byte_as_float(nz ? loz : hiz, k), az, __fadd_rn(bz, mz));
+    const float tn = fmaxf(fmax3f(tnx, tny, tnz), tmin);
+    const float tf = fminf(fmin3f(tfx, tfy, tfz), tmax);
+    const bool hit = tn <= tf;
+    const bool internal = ((imask >> slot) & 1u) != 0;
+    const uint32_t m = (__float_as_uint(h ? w[1].w : w[1].z) >> (8 * k)) & 0xffu;
+    const uint32_t lane0 = threadIdx.x & 24u;
+    node_bits = (__ballot_sync(g.mask, hit && internal) >> lane0) & 0xffu;
+    const uint32_t mine = (hit && !internal && m) ? ((1u << (m >> 5)) - 1u) << (m & 31u) : 0u;
+    tri_bits = __reduce_or_sync(g.mask, mine);
+}
+
+// trace_after for a lane group (see above). All eight lanes call it with the
+// same arguments and get the same result.
+__device__ __forceinline__ Hit trace_after_group(const SceneView &s, const float3 &o, const float3 &d, float tmin,
+                                                 float tmax, const Hit &after, uint32_t &err, const LaneGroup &g)
+{
+    Hit best;
+    best.t = tmax;
+    best.u = best.v = 0.0f;
+    best.inst = kNoHit;
+    best.prim = kNoHit;
+    const float slack = cull_slack(s, o, d);
+    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t), slack);
+    const float3 winvd = safe_inv(d);
+    float3 co = o, cinvd = winvd;
+    WatertightRay wr = wt_setup(o, d);
+    uint32_t inst_id = kNoHit;
+    uint32_t node_base = s.tlas_root, tri_base = 0;
+    bool in_blas = false;
+    int node = 0; // TLAS node to visit, -1 none
+    uint32_t w_base = 0, w_bits = 0, w_imask = 0, t_base = 0, t_bits = 0, oct = 0;
+    int2 stack[kTraversalStack];
+    int sp = 0;
+    const int cached = vvpt_tlas_cache_src == s.nodes + s.tlas_root ? vvpt_tlas_cache_count : 0;
+    auto push = [&](int value, int tag, int count) {
+        if (sp < kTraversalStack)
+            stack[sp++] = make_int2(value, (tag << 28) | count);
+        else
+            err |= kErrStackOverflow;
+    };
+    for (;;) {
+        if (t_bits) {
+            // up to eight pending triangles, one per lane
+            const int cnt = __popc(t_bits);
+            float ct = INFINITY, cu = 0.0f, cv = 0.0f;
+            uint32_t cp = kNoHit;
+            if (g.gl < cnt) {
+                const int b = (int)__fns(t_bits, 0, g.gl + 1);
+                const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + t_base + (uint32_t)b);
+                const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                const uint32_t prim = __float_as_uint(p0.w);
+                float t, u, v;
+                if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
+                    is_after(t, inst_id, prim, after)) {
+                    ct = t;
+                    cu = u;
+                    cv = v;
+                    cp = prim;
+                }
+            }
+            if (cnt <= 8) {
+                t_bits = 0;
+            } else {
+                const uint32_t b8 = __fns(t_bits, 0, 8); // the eighth set bit
+                t_bits &= ~((2u << b8) - 1u);
+            }
+            // group minimum of (t, primitive)
+            float mt = ct;
+            uint32_t mp = cp;
+#pragma unroll
+            for (int sh = 1; sh < 8; sh <<= 1) {
+                const float ot = __shfl_xor_sync(g.mask, mt, sh);
+                const uint32_t op = __shfl_xor_sync(g.mask, mp, sh);
+                if (ot < mt || (ot == mt && op < mp)) {
+                    mt = ot;
+                    mp = op;
+                }
+            }
+            if (mp != kNoHit) {
+                const uint32_t owner = __ffs(__ballot_sync(g.mask, cp == mp && ct == mt)) - 1;
+                best.u = __shfl_sync(g.mask, cu, (int)owner);
+                best.v = __shfl_sync(g.mask, cv, (int)owner);
+                best.t = mt;
+                best.inst = inst_id;
+                best.prim = mp;
+            }
+            continue;
+        }
+        if (w_bits) {
+            const int b = __ffs((int)w_bits) - 1;
+            w_bits &= w_bits - 1u;
+            const uint32_t slot = (uint32_t)b ^ oct;
+            const uint32_t child = w_base + (uint32_t)__popc(w_imask & ((1u << slot) - 1u));
+            if (w_bits)
+                push((int)w_base, kTagWide, (int)((w_bits << 8) | w_imask));
+            float4 wn[5];
+            load_wide(s.wnodes, node_base + child, wn);
+            wide_visit_group(wn, co, cinvd, oct, box_tmin, cull_far(best.t, slack), g, w_bits, w_imask, w_base,
+                             t_base, t_bits);
+            continue;
+        }
+        if (node >= 0) {
+            // TLAS (binary nodes): every lane tests both children
+            const BVHNode n = node < cached ? load_node_cached(node) : load_node(s.nodes, (int)node_base + node);
+            float tl, tr;
+            const float far_t = cull_far(best.t, slack);
+            box2(n, co, cinvd, box_tmin, far_t, tl, tr);
+            const bool hl = tl <= far_t && n.c.x >= 0;
+            const bool hr = tr <= far_t && n.c.y >= 0;
+            const bool swap = hl && hr && tr < tl;
+            int next = -1;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const bool right = (k == 0) == swap;
+                const bool h = right ? hr : hl;
+                if (!h)
+                    continue;
+                const int idx = right ? n.c.y : n.c.x;
+                const int cnt = right ? n.c.w : n.c.z;
+                if (cnt == 0) {
+                    if (next < 0)
+                        next = idx;
+                    else
+                        push(idx, kTagNode, 0);
+                } else {
+                    push(idx, kTagInst, cnt);
+                }
+            }
+            node = next;
+            continue;
+        }
+        if (sp == 0)
+            break;
+        const int2 e = stack[--sp];
+        const int tag = (int)((unsigned)e.y >> 28);
+        const int cnt = e.y & 0x0FFFFFFF;
+        if (tag == kTagNode) {
+            node = e.x;
+        } else if (tag == kTagWide) {
+            w_base = (uint32_t)e.x;
+            w_bits = ((uint32_t)cnt >> 8) & 0xffu;
+            w_imask = (uint32_t)cnt & 0xffu;
+        } else if (tag == kTagInst) {
+            if (cnt > 1)
+                push(e.x + 1, kTagInst, cnt - 1);
+            inst_id = __ldg(s.tlas_order + e.x);
+            const DevInstance &inst = s.instances[inst_id];
+            const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
+            co = wt_xform_point(rows, o);
+            const float3 cd = wt_xform_vector(rows, d);
+            cinvd = safe_inv(cd);
+            wr = wt_setup(co, cd);
+            node_base = inst.node_offset;
+            tri_base = inst.tri_offset;
+            in_blas = true;
+            push(0, kTagReturn, 0);
+            oct = (__float_as_uint(cd.x) >> 31) | ((__float_as_uint(cd.y) >> 31) << 1) |
+                  ((__float_as_uint(cd.z) >> 31) << 2);
+            w_base = 0;
+            w_imask = 1u;
+            w_bits = 1u << oct;
+        } else {
+            co = o;
+            cinvd = winvd;
+            node_base = s.tlas_root;
+            in_blas = false;
+            inst_id = kNoHit;
+        }
+    }
+    (void)in_blas;
+    return best;
+}
+#endif
 
 __device__ __forceinline__ Hit no_hit()
 {

@@ -33,6 +33,27 @@ constexpr float kExtTmax = 10000.0f;
 constexpr float kConnTmin = 0.0001f;    // lightSampling.glsl:112, next_event_estimation.glsl:3
 constexpr int kCandidateCap = 1024;     // per-segment candidate bound for any-hit loops
 
+// Who traces a ray in the candidate walks below: one lane on its own
+// (trace_after), or a group of eight lanes that all run the walk with the
+// same data (trace_after_group, the traversal kernels' form).
+struct LaneTracer {
+    __device__ __forceinline__ Hit operator()(const SceneView &s, const float3 &o, const float3 &d, float tmin,
+                                              float tmax, const Hit &after, uint32_t &err) const
+    {
+        return trace_after(s, o, d, tmin, tmax, after, err);
+    }
+};
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+struct GroupTracer {
+    LaneGroup g;
+    __device__ __forceinline__ Hit operator()(const SceneView &s, const float3 &o, const float3 &d, float tmin,
+                                              float tmax, const Hit &after, uint32_t &err) const
+    {
+        return trace_after_group(s, o, d, tmin, tmax, after, err, g);
+    }
+};
+#endif
+
 // Warp-aggregated queue append. Must be called by all 32 lanes of the warp
 // at a convergence point (the kernels below keep their loop bounds
 // warp-uniform); lanes with want == false get no slot.
@@ -587,19 +608,47 @@ __global__ void __launch_bounds__(256, VVPT_REGEN_MIN_BLOCKS) k_regen(JobTable j
 #ifndef VVPT_SHADE_MIN_BLOCKS
 #define VVPT_SHADE_MIN_BLOCKS 2
 #endif
+// the Lambert and miss shading kernels
+#ifndef VVPT_SHADE_LM_MIN_BLOCKS
+#define VVPT_SHADE_LM_MIN_BLOCKS 2
+#endif
+// Rays per traversal-kernel lane: one (the one-ray-per-lane loop) or, with
+// the wide BLAS, one per group of eight lanes (trace_after_group). first_ray
+// is the queue index of a block's first ray, ray_stride the grid stride.
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+constexpr uint32_t kLanesPerRay = 8;
+#else
+constexpr uint32_t kLanesPerRay = 1;
+#endif
+__device__ __forceinline__ uint32_t first_ray() { return blockIdx.x * (blockDim.x / kLanesPerRay); }
+__device__ __forceinline__ uint32_t my_ray() { return (blockIdx.x * blockDim.x + threadIdx.x) / kLanesPerRay; }
+__device__ __forceinline__ uint32_t ray_stride() { return gridDim.x * blockDim.x / kLanesPerRay; }
+// Before a group's lane 0 writes what every lane of the group has read.
+__device__ __forceinline__ void group_sync()
+{
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+    __syncwarp(0xFFu << (threadIdx.x & 24u));
+#endif
+}
+
 __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
     uint32_t err = 0;
-    if (blockIdx.x * blockDim.x < n)
-        tlas_cache_fill(jt.jobs[ps.job[queue[blockIdx.x * blockDim.x]]].scene);
+    if (first_ray() < n)
+        tlas_cache_fill(jt.jobs[ps.job[queue[first_ray()]]].scene);
     else
         tlas_cache_none();
-    // Lanes run independently: a lane takes its next ray as soon as its
-    // current one is done, so a warp is never held by its slowest ray. The
-    // shade bin is written per queue entry and compacted by k_partition.
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+    // One ray per group of eight lanes; the group's lanes share the
+    // traversal (trace_after_group) and lane 0 writes the result.
+    const LaneGroup g = lane_group();
+#endif
+    // A lane (group) takes its next ray as soon as its current one is done,
+    // so a warp is never held by its slowest ray. The shade bin is written
+    // per queue entry and compacted by k_partition.
+    for (uint32_t i = my_ray(); i < n; i += ray_stride()) {
         const uint32_t slot = queue[i];
         const SceneView &s = jt.jobs[ps.job[slot]].scene;
         const float3 o = f3(ps.o[slot]);
@@ -607,16 +656,22 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
         const uint32_t flags = ps.flags[slot];
         // with an emitter ray riding on this ray, start at its tmin
         const bool fused = (flags & F_NEE_FUSED) != 0;
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+        Hit h = trace_after_group(s, o, d, fused ? kConnTmin : kExtTmin, kExtTmax, no_hit(), err, g);
+#else
         Hit h = trace_closest(s, o, d, fused ? kConnTmin : kExtTmin, kExtTmax, err);
+#endif
         uint32_t key = 0;
         if (fused && h.inst != kNoHit && h.t < kExtTmin) {
             // the emitter ray's first candidate lies below the extension
             // ray's tmin: the emitter ray takes the full candidate walk
             key = 4;
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+            h = trace_after_group(s, o, d, kExtTmin, kExtTmax, no_hit(), err, g);
+#else
             h = trace_closest(s, o, d, kExtTmin, kExtTmax, err);
+#endif
         }
-        ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-        ps.hit_inst[slot] = h.inst;
         if (h.inst == kNoHit) {
             key |= 2;
         } else {
@@ -626,7 +681,14 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
             if (fused && h.t <= kExtTmax && m.mrao.w >= 0.99f)
                 key |= 4;
         }
-        q.ext_key[i] = key;
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+        if (g.gl == 0)
+#endif
+        {
+            ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+            ps.hit_inst[slot] = h.inst;
+            q.ext_key[i] = key;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
         atomicAdd(&q.counters[C_SEGMENTS], n);
@@ -664,9 +726,10 @@ __global__ void __launch_bounds__(256) k_partition(PathState ps, Queues q, int p
     }
 }
 
-__device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir,
-                                         bool inside, uint32_t vol, float3 &out_em_T, float3 &out_T, float3 &out_em,
-                                         float &out_pdf, uint32_t &err);
+template <class Tracer>
+__device__ __noinline__ void emitter_ray(const Tracer &trace, const SceneView &s, const RenderParams &p, float3 o,
+                                         const float3 &dir, bool inside, uint32_t vol, float3 &out_em_T,
+                                         float3 &out_T, float3 &out_em, float &out_pdf, uint32_t &err);
 
 // The pending emitter rays whose first candidate is transparent (or below the
 // extension ray's tmin): the full candidate walk, before shade adds this
@@ -675,11 +738,18 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_walk(JobTable jt
 {
     const uint32_t n = q.counters[C_WALK];
     uint32_t err = 0;
-    if (blockIdx.x * blockDim.x < n)
-        tlas_cache_fill(jt.jobs[ps.job[q.walk[blockIdx.x * blockDim.x]]].scene);
+    if (first_ray() < n)
+        tlas_cache_fill(jt.jobs[ps.job[q.walk[first_ray()]]].scene);
     else
         tlas_cache_none();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+    const GroupTracer trace{lane_group()};
+    const bool writer = trace.g.gl == 0;
+#else
+    const LaneTracer trace{};
+    const bool writer = true;
+#endif
+    for (uint32_t i = my_ray(); i < n; i += ray_stride()) {
         const uint32_t slot = q.walk[i];
         const JobView &J = jt.jobs[ps.job[slot]];
         const SceneView &s = J.scene;
@@ -688,10 +758,14 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_walk(JobTable jt
         const float4 nb = ps.nee_b[slot];
         float3 emT, T, em;
         float lpdf;
-        emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf, err);
-        if (!is_black(em))
-            ps.rad[slot] = f4(f3(ps.rad[slot]) + power_heuristic(nb.w, lpdf) * T * em * f3(nb), 0.0f);
-        ps.flags[slot] = flags & ~(F_NEE_FUSED | F_NEE_FULL);
+        emitter_ray(trace, s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em,
+                    lpdf, err);
+        group_sync();
+        if (writer) {
+            if (!is_black(em))
+                ps.rad[slot] = f4(f3(ps.rad[slot]) + power_heuristic(nb.w, lpdf) * T * em * f3(nb), 0.0f);
+            ps.flags[slot] = flags & ~(F_NEE_FUSED | F_NEE_FULL);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && n)
         atomicAdd(&q.counters[C_NEE], n);
@@ -737,31 +811,39 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 // One shading event per queued path: the body of rayPrimary*.rchit.glsl:45-175
 // (hits) or rayPrimary.rmiss.glsl:40-106 (misses), followed by Russian
 // roulette (russian_roulette.glsl:1-11).
-__global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable jt, PathState ps, Queues q, int pp)
+// One kernel per material-sorted queue (k_partition): KIND 0 shades the
+// Lambert hits, 1 the metallic/roughness hits, 2 the misses. Each is compiled
+// for its own case only (the other surface models are dead code there), so
+// the Lambert and miss kernels fit more resident blocks than the
+// metallic/roughness one.
+template <int KIND>
+__global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MIN_BLOCKS : VVPT_SHADE_MIN_BLOCKS)
+    k_shade(JobTable jt, PathState ps, Queues q, int pp)
 {
-    const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P], nm = q.counters[C_SHADE_M];
-    const uint32_t n = nl + np + nm;
+    // KIND 3: all three queues in one launch (VVPT_SHADE_SPLIT = 0)
+    const uint32_t nl = q.counters[C_SHADE_L], np = q.counters[C_SHADE_P];
+    const uint32_t n = KIND == 3 ? nl + np + q.counters[C_SHADE_M]
+                                 : q.counters[KIND == 0 ? C_SHADE_L : (KIND == 1 ? C_SHADE_P : C_SHADE_M)];
+    const uint32_t *queue = KIND == 0 ? q.shade_l : (KIND == 1 ? q.shade_p : q.shade_m);
+    auto entry = [&](uint32_t i) {
+        if (KIND != 3)
+            return queue[i];
+        return i < nl ? q.shade_l[i] : (i < nl + np ? q.shade_p[i - nl] : q.shade_m[i - nl - np]);
+    };
     uint32_t err = 0, walks = 0;
     {
         const uint32_t f = blockIdx.x * blockDim.x;
-        if (f < n) {
-            const uint32_t slot = f < nl ? q.shade_l[f] : (f < nl + np ? q.shade_p[f - nl] : q.shade_m[f - nl - np]);
-            tlas_cache_fill(jt.jobs[ps.job[slot]].scene);
-        } else {
+        if (f < n)
+            tlas_cache_fill(jt.jobs[ps.job[entry(f)]].scene);
+        else
             tlas_cache_none();
-        }
     }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         uint32_t slot = 0;
         bool want_conn = false, want_nee = false, want_done = false, want_ext = false;
         if (i < n) {
-        if (i < nl)
-            slot = q.shade_l[i];
-        else if (i < nl + np)
-            slot = q.shade_p[i - nl];
-        else
-            slot = q.shade_m[i - nl - np];
+        slot = entry(i);
         const JobView &J = jt.jobs[ps.job[slot]];
         const SceneView &s = J.scene;
         const RenderParams &p = J.params;
@@ -780,7 +862,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
         bool inside = (flags & F_INSIDE) != 0;
         const float4 hv = ps.hit[slot];
         const uint32_t inst_id = ps.hit_inst[slot];
-        const bool is_hit = inst_id != kNoHit;
+        const bool is_hit = KIND == 3 ? inst_id != kNoHit : KIND != 2; // hits (0, 1) or misses (2)
 
         // the previous event's emitter ray, added before this event's own
         // contributions (next_event_estimation.glsl:28-32 runs inside the
@@ -879,7 +961,7 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
             SurfaceHit h = make_surface_hit(s, inst_id, prim, hv.y, hv.z, dir);
             const DevMaterial &m = s.materials[h.material];
             const float2 tuv = make_float2(h.uv.x * m.uv_tiling.x, h.uv.y * m.uv_tiling.y);
-            const bool lambert = (uint32_t)m.uv_tiling.z == 2u;
+            const bool lambert = KIND == 3 ? (uint32_t)m.uv_tiling.z == 2u : KIND == 0;
             bool passthrough = false;
             if (m.mrao.w > 0.0f) {
                 float alpha = material_alpha(s, m, tuv);
@@ -1059,8 +1141,9 @@ __global__ void __launch_bounds__(256, VVPT_SHADE_MIN_BLOCKS) k_shade(JobTable j
 // Shadow ray with transparent surfaces and media (lightSampling.glsl:108-144,
 // raySecondary.rahit.glsl:31-72, raySecondary.rchit.glsl:32-78,
 // raySecondary.rmiss.glsl:17-44). Candidates are processed nearest first.
-__device__ float3 shadow_transmittance(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir,
-                                       float tmax_light, bool inside, uint32_t vol, uint32_t &err)
+template <class Tracer>
+__device__ float3 shadow_transmittance(const Tracer &trace, const SceneView &s, const RenderParams &p, float3 o,
+                                       const float3 &dir, float tmax_light, bool inside, uint32_t vol, uint32_t &err)
 {
     const float tmin = kConnTmin;
     float3 T = f3(1.0f);
@@ -1074,7 +1157,7 @@ __device__ float3 shadow_transmittance(const SceneView &s, const RenderParams &p
         Hit acc;
         int guard = 0;
         for (;;) {
-            Hit h = trace_after(s, o, dir, tmin, distT, after, err);
+            Hit h = trace(s, o, dir, tmin, distT, after, err);
             if (h.inst == kNoHit)
                 break;
             if (++guard > kCandidateCap) {
@@ -1202,8 +1285,10 @@ __device__ __forceinline__ void emitter_eval(const SceneView &s, const RenderPar
 // BSDF-direction emitter ray (next_event_estimation.glsl:1-33,
 // rayNEE.rahit.glsl:32-132, rayNEE.rchit.glsl:33-82, rayNEE.rmiss.glsl:12-19).
 // Returns the emitter radiance times throughput and its light pdf.
-__device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams &p, float3 o, const float3 &dir, bool inside,
-                            uint32_t vol, float3 &out_em_T, float3 &out_T, float3 &out_em, float &out_pdf, uint32_t &err)
+template <class Tracer>
+__device__ __noinline__ void emitter_ray(const Tracer &trace, const SceneView &s, const RenderParams &p, float3 o,
+                                         const float3 &dir, bool inside, uint32_t vol, float3 &out_em_T,
+                                         float3 &out_T, float3 &out_em, float &out_pdf, uint32_t &err)
 {
     const float tmin = kConnTmin;
     const float tmax = p.zfar;
@@ -1218,7 +1303,7 @@ __device__ __noinline__ void emitter_ray(const SceneView &s, const RenderParams 
         Hit acc;
         int guard = 0;
         for (;;) {
-            Hit h = trace_after(s, o, dir, tmin, tmax, after, err);
+            Hit h = trace(s, o, dir, tmin, tmax, after, err);
             if (h.inst == kNoHit)
                 break;
             if (++guard > kCandidateCap) {
@@ -1340,7 +1425,7 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
     }
     if (full) {
         float3 emT;
-        emitter_ray(s, p, o, dir, inside, vol, emT, T, em, pdf, err);
+        emitter_ray(LaneTracer{}, s, p, o, dir, inside, vol, emT, T, em, pdf, err);
         walks++;
     }
     if (is_black(em))
@@ -1361,12 +1446,19 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
     const uint32_t n = nc + q.counters[C_NEEQ];
     uint32_t err = 0;
     uint32_t nsh = 0, nnee = 0;
-    const uint32_t b0 = blockIdx.x * blockDim.x;
+    const uint32_t b0 = first_ray();
     if (b0 < n)
         tlas_cache_fill(jt.jobs[ps.job[b0 < nc ? q.conn[b0] : q.nee[b0 - nc]]].scene);
     else
         tlas_cache_none();
-    for (uint32_t i = b0 + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+    const GroupTracer trace{lane_group()};
+    const bool writer = trace.g.gl == 0;
+#else
+    const LaneTracer trace{};
+    const bool writer = true;
+#endif
+    for (uint32_t i = my_ray(); i < n; i += ray_stride()) {
         if (i < nc) {
             const uint32_t slot = q.conn[i];
             const uint32_t flags = ps.flags[slot];
@@ -1376,12 +1468,15 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
             const SceneView &s = J.scene;
             const RenderParams &p = J.params;
             const float4 sd = ps.sh_dir[slot];
-            const float3 T = shadow_transmittance(s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
+            const float3 T = shadow_transmittance(trace, s, p, f3(ps.o[slot]), f3(sd), sd.w, (flags & F_INSIDE) != 0,
                                                   ps.vol[slot], err);
-            if (!is_black(T))
-                ps.rad[slot] = f4(f3(ps.rad[slot]) + f3(ps.sh_c[slot]) * T, 0.0f);
-            ps.flags[slot] = flags & ~F_SHADOW;
-            nsh++;
+            group_sync();
+            if (writer) {
+                if (!is_black(T))
+                    ps.rad[slot] = f4(f3(ps.rad[slot]) + f3(ps.sh_c[slot]) * T, 0.0f);
+                ps.flags[slot] = flags & ~F_SHADOW;
+                nsh++;
+            }
         } else {
             const uint32_t slot = q.nee[i - nc];
             const uint32_t flags = ps.flags[slot]; // F_INSIDE; the shadow part may clear F_SHADOW meanwhile
@@ -1391,13 +1486,15 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
             const float4 nb = ps.nee_b[slot];
             float3 emT, T, em;
             float lpdf;
-            emitter_ray(s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T, em, lpdf,
-                        err);
+            emitter_ray(trace, s, p, f3(ps.o[slot]), f3(ps.d[slot]), (flags & F_INSIDE) != 0, ps.vol[slot], emT, T,
+                        em, lpdf, err);
             float3 c = f3(0.0f);
             if (!is_black(em))
                 c = power_heuristic(nb.w, lpdf) * T * em * f3(nb);
-            ps.nee_c[slot] = f4(c, 0.0f);
-            nnee++;
+            if (writer) {
+                ps.nee_c[slot] = f4(c, 0.0f);
+                nnee++;
+            }
         }
     }
     if (nsh)
@@ -1438,9 +1535,18 @@ __global__ void k_trace_closest(SceneView s, const float4 *rays, uint32_t n, flo
 {
     uint32_t err = 0;
     tlas_cache_fill(s);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+    const LaneGroup g = lane_group();
+#endif
+    for (uint32_t i = my_ray(); i < n; i += ray_stride()) {
         float4 a = rays[2 * i], b = rays[2 * i + 1];
+#if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
+        Hit h = trace_after_group(s, f3(a), f3(b), a.w, b.w, no_hit(), err, g);
+        if (g.gl != 0)
+            continue;
+#else
         Hit h = trace_closest(s, f3(a), f3(b), a.w, b.w, err);
+#endif
         tuv[i] = make_float4(h.t, h.u, h.v, 0.0f);
         ids[2 * i] = h.inst;
         ids[2 * i + 1] = h.prim;
@@ -1491,7 +1597,13 @@ void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Qu
         k_walk<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
         break;
     case K_SHADE:
-        k_shade<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
+#if VVPT_SHADE_SPLIT
+        k_shade<0><<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
+        k_shade<1><<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
+        k_shade<2><<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
+#else
+        k_shade<3><<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
+#endif
         break;
     case K_SHADOW:
         k_shadow<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);
@@ -1512,7 +1624,7 @@ void launch_reduce(const RenderParams &hp, const BatchResults &br, float4 *radia
 void launch_trace_closest(const SceneView &s, const float4 *rays, uint32_t n, float4 *tuv, uint32_t *ids, uint32_t *err,
                           cudaStream_t stream)
 {
-    int grid = (int)std::min<uint32_t>((n + 255) / 256, 65535u);
+    int grid = (int)std::min<uint64_t>(((uint64_t)n * kLanesPerRay + 255) / 256, 65535u);
     if (grid < 1)
         grid = 1;
     k_trace_closest<<<grid, 256, kTlasCacheBytes, stream>>>(s, rays, n, tuv, ids, err);

@@ -159,7 +159,14 @@ enum KernelId {
     K_SHADOW = 6, // shadow rays, then the emitter rays of paths that end
     K_NUM = 7
 };
-constexpr int kKernelsPerIteration = K_NUM;
+// K_SHADE launches one kernel per material-sorted queue (VVPT_SHADE_SPLIT,
+// default on) or one over all three
+#ifndef VVPT_SHADE_SPLIT
+#define VVPT_SHADE_SPLIT 1
+#endif
+constexpr int kShadeLaunches = VVPT_SHADE_SPLIT ? 3 : 1;
+constexpr int launches_of(int k) { return k == K_SHADE ? kShadeLaunches : 1; }
+constexpr int kKernelsPerIteration = K_NUM + kShadeLaunches - 1;
 void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Queues &q, int pingpong,
                    const LaunchShape &shape, cudaStream_t stream);
 
