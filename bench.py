@@ -359,7 +359,7 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
-N_SCENES = 8
+N_SCENES = 64
 
 
 def _job_scenes(ctx, n_scenes: int):
@@ -372,8 +372,8 @@ def _job_scenes(ctx, n_scenes: int):
 
 
 def run_batched(args) -> None:
-    """64 jobs from the seeded job mix (scenes of 10k-2M triangles, 256^2 to
-    1920x1080, 16/64/256 spp) rendered together through the job engine: one
+    """64 jobs from the seeded job mix, each with its own scene (10k-2M
+    triangles, 256^2 to 1920x1080, 16/64/256 spp) rendered together through the job engine: one
     step submits all 64 and waits for the last. value = total paths / wall
     time with device outputs; e2e = the same with host outputs; the same jobs
     one after another through vvpt_render give sequential_paths_per_s."""
@@ -382,7 +382,7 @@ def run_batched(args) -> None:
     from vviewer_gb300 import Context, scenes
     ctx = Context(0)
     engines, gpus, tris = _job_scenes(ctx, N_SCENES)
-    mix = scenes.job_mix(1, 64, N_SCENES)
+    mix = scenes.job_mix(1, 64, N_SCENES, distinct=True)
     sds = [engines[k].scene.scene_data(i.width, i.height) for k, i in mix]
     paths = sum(i.width * i.height * (i.samples // i.batch_size) * i.batch_size for _, i in mix)
     dev = [{k: torch.zeros((i.height, i.width, 4), dtype=torch.float32, device="cuda")
@@ -457,10 +457,12 @@ def run_batched(args) -> None:
 
 def run_serving(args) -> None:
     """512 requests with Poisson arrivals (mean gap 50 ms, seeded) against the
-    resident scene pool of the batched workload; preview sizes (256^2 / 512^2,
-    8 / 16 / 32 spp). A submitter thread issues each request at its arrival
-    time; latency = submit to outputs on the host. value = aggregate paths/s
-    from the first arrival to the last completion."""
+    resident pool of the batched workload's 64 scenes, sizes and spp drawn as
+    in the batched workload, admitted against a 150 GB device-memory budget
+    (--preview: 256^2 / 512^2 at 8 / 16 / 32 spp instead). A submitter
+    thread issues each request at its arrival time; latency = submit to the
+    finished image in host memory. value = aggregate paths/s from the first
+    arrival to the last completion."""
     import threading
 
     import torch
@@ -469,7 +471,7 @@ def run_serving(args) -> None:
     ctx = Context(0)
     ctx.set_budget(150 * (1 << 30))
     engines, gpus, tris = _job_scenes(ctx, N_SCENES)
-    reqs = scenes.serving_requests(1, args.requests, N_SCENES)
+    reqs = scenes.serving_requests(1, args.requests, N_SCENES, preview=args.preview)
     sds = [engines[k].scene.scene_data(i.width, i.height) for _, k, i in reqs]
     paths = sum(i.width * i.height * (i.samples // i.batch_size) * i.batch_size for _, _, i in reqs)
     tuning = None
@@ -509,8 +511,10 @@ def run_serving(args) -> None:
             "warmup": args.warmup, "ms_per_step": span_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes, Poisson arrivals)",
             "config": {"workload": "serving_512_requests", "requests": len(reqs), "mean_gap_ms": 50.0,
-                       "scenes": N_SCENES, "scene_triangles": tris, "resolutions": "256^2 / 512^2",
-                       "spp": "8 / 16 / 32", "depth": 8, "batch_size": 4, "paths": paths, "seed": 1,
+                       "scenes": N_SCENES, "scene_triangles": tris,
+                       "resolutions": "256^2 / 512^2" if args.preview else "256^2 / 512^2 / 1024^2 / 1920x1080",
+                       "spp": "8 / 16 / 32" if args.preview else "16 / 64 / 256", "depth": 8, "batch_size": 4,
+                       "paths": paths, "seed": 1, "latency": "submit to the finished image on the host",
                        "budget_bytes": 150 * (1 << 30), "outputs": "host", "tuning": tuning},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                            "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
@@ -603,22 +607,28 @@ def run_denoise(args) -> None:
 
 
 def _rel_rmse(img, ref) -> float:
-    """Relative RMSE: sqrt(mean((img - ref)^2 / (ref^2 + 0.01))) over the
-    pixels and the 3 radiance channels (the relative MSE of the denoising
-    literature; a plain L2 ratio would be decided by the few sun highlights)."""
+    """Relative RMSE of an image against a reference: the root of
+    sum((img - ref)^2) / sum(ref^2) over the pixels and the three radiance
+    channels."""
     d = img[..., :3].double() - ref[..., :3].double()
-    return float((d.pow(2) / (ref[..., :3].double().pow(2) + 0.01)).mean().sqrt())
+    return float((d.pow(2).sum() / ref[..., :3].double().pow(2).sum()).sqrt())
 
 
 def run_converged(args) -> None:
-    """Converged images per hour at relative RMSE <= 1e-2 against a
-    4096-spp render, on the instanced sky scene (C5: 512 instances, 32 mesh
-    lights, thin lens, importance-sampled sky) at 960 x 544. Plain tracer: the
-    error is measured at 64 and 256 spp and fitted as e^2 = a / spp + b (b: the
-    4096-spp reference's own noise), giving the spp and time it needs.
-    Tracer + denoiser: the smallest spp whose denoised image meets the target,
-    time = render + denoise. The denoiser is trained first on tracer pairs of
-    other seeds (4/8/16/32-spp inputs, 1024-spp targets)."""
+    """Converged images per hour at relative RMSE <= 1e-2 against an
+    FP64-accumulated 4096-spp render of the same view, on the C5 scene (512
+    instances of seeded displaced meshes, 32 mesh lights, thin lens, a
+    4096 x 2048 sky with a 5e4 sun, environment importance sampled) at
+    960 x 544 (multiples of 16 for the denoiser).
+
+    Plain single-job tracer: vvpt_render at 64 / 256 / 1024 spp; the error is
+    fitted as e^2 = a / spp + b and the spp for the target read off the fit.
+    Batched, served and denoised: M requests of the view submitted together
+    to the job engine at a low spp, each denoised as it completes; images per
+    hour = M / wall time, latency = submit to denoised image (p50 / p99).
+    The denoiser is first trained on crops of other seeds of the same scene
+    generator: 512^2 inputs at 4 / 8 / 16 spp stored as FP16 (radiance,
+    albedo, normal) and 4096-spp FP64-accumulated targets."""
     import torch
 
     from vviewer_gb300 import Context, scenes
@@ -626,100 +636,148 @@ def run_converged(args) -> None:
     ctx = Context(0)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
-    W, H = 960, 544  # multiples of 16 for the denoiser
+    W, H = 960, 544
     target = 1e-2
+    ref_spp = 4096
+    keys = ("radiance", "albedo", "normal")
 
-    def render(g, sd, info, spp, w, h):
+    def bufs(w, h, m2=False):
+        return {k: torch.zeros((h, w, 4), device="cuda") for k in keys + (("radiance_m2",) if m2 else ())}
+
+    def render(g, sd, info, spp, w, h, fp64=False, m2=False):
         info.samples = spp
-        bufs = {k: torch.zeros((h, w, 4), device="cuda") for k in ("radiance", "albedo", "normal")}
+        b = bufs(w, h, m2)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        g.render(sd, info, outputs={k: v.data_ptr() for k, v in bufs.items()}, env_is=True)
+        g.render(sd, info, outputs={k: v.data_ptr() for k, v in b.items()}, env_is=True, reduce_fp64=fp64,
+                 want_m2=m2)
         torch.cuda.synchronize()
-        return bufs, time.perf_counter() - t
+        return b, time.perf_counter() - t
 
-    # training pairs from other seeds: noisy inputs at several spp, one target
-    dn = Denoiser(ctx, seed=1)
-    crops = {k: [] for k in ("radiance", "albedo", "normal", "target")}
-    t_train = time.perf_counter()
-    for seed in range(2, 10):
+    # ---- training set: crops of other seeds
+    t_set = time.perf_counter()
+    crops = {k: [] for k in keys + ("target",)}
+    in_spps = (4, 8, 16)
+    for seed in range(2, 2 + args.train_crops):
         e, info = scenes.instanced_sky_scene(seed, 512, 512, 4, 8, 4, sky_w=2048, sky_h=1024)
         g = ctx.upload(e.scene.build())
         sd = e.scene.scene_data(512, 512)
-        ref, _ = render(g, sd, info, 1024, 512, 512)
-        for spp in (4, 8, 16, 32):
+        ref, _ = render(g, sd, info, ref_spp, 512, 512, fp64=True)
+        for spp in in_spps:
             noisy, _ = render(g, sd, info, spp, 512, 512)
-            for k in ("radiance", "albedo", "normal"):
-                crops[k].append(noisy[k])
-            crops["target"].append(ref["radiance"])
+            for k in keys:
+                crops[k].append(noisy[k].half())
+            crops["target"].append(ref["radiance"].half())
         g.release()
-    batch = {k: torch.stack(v).contiguous() for k, v in crops.items()}
+    tset = {k: torch.stack(v).contiguous() for k, v in crops.items()}
+    t_set = time.perf_counter() - t_set
+    dn = Denoiser(ctx, seed=1)
     losses = []
     gen = torch.Generator().manual_seed(1)
+    t_train = time.perf_counter()
     for step in range(args.train_steps):
-        idx = torch.randint(0, batch["radiance"].shape[0], (4,), generator=gen).cuda()
+        idx = torch.randint(0, tset["radiance"].shape[0], (4,), generator=gen).cuda()
         ys = int(torch.randint(0, 512 - 256 + 1, (1,), generator=gen)) // 16 * 16
         xs = int(torch.randint(0, 512 - 256 + 1, (1,), generator=gen)) // 16 * 16
-        sub = [batch[k][idx, ys:ys + 256, xs:xs + 256].contiguous() for k in ("radiance", "albedo", "normal", "target")]
+        sub = [tset[k][idx, ys:ys + 256, xs:xs + 256].float().contiguous() for k in keys + ("target",)]
         lr = 2e-3 if step < args.train_steps * 3 // 4 else 5e-4
         losses.append(dn.train_step(*sub, lr=lr))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t_train
 
+    # ---- the judged view
     e, info = scenes.instanced_sky_scene(1, W, H, 16, 8, 4, sky_w=4096, sky_h=2048)
     g = ctx.upload(e.scene.build())
     sd = e.scene.scene_data(W, H)
-    ref, t_ref = render(g, sd, info, 4096, W, H)
+    ref, t_ref = render(g, sd, info, ref_spp, W, H, fp64=True, m2=True)
+    nb = ref_spp // info.batch_size
+    x = ref["radiance"][..., :3].double()
+    var = (nb * ref["radiance_m2"][..., :3].double() - x * x).clamp(min=0) / (nb - 1)
+    ref_noise = float((var.sum() / x.pow(2).sum()).sqrt())  # the reference's own relative RMSE
+
+    # plain single-job tracer
     plain = {}
-    for spp in (64, 256):
+    for spp in (64, 256, 1024):
         img, t = render(g, sd, info, spp, W, H)
         plain[spp] = (_rel_rmse(img["radiance"], ref["radiance"]), t)
-    paths_per_s = W * H * 256 / plain[256][1]
-    e64, e256 = plain[64][0] ** 2, plain[256][0] ** 2
-    a = max((e64 - e256) / (1 / 64 - 1 / 256), 1e-12)
-    b = max(e256 - a / 256, 0.0)
-    spp_plain = a / (target ** 2 - b) if target ** 2 > b else float("inf")
+    paths_per_s = W * H * 1024 / plain[1024][1]
+    e64, e1024 = plain[64][0] ** 2, plain[1024][0] ** 2
+    a = max((e64 - e1024) / (1 / 64 - 1 / 1024), 1e-30)
+    b = max(e1024 - a / 1024, 0.0)
+
+    def plain_spp_for(err):
+        return a / (err ** 2 - b) if err ** 2 > b else float("inf")
+
+    spp_plain = plain_spp_for(target)
     t_plain = W * H * spp_plain / paths_per_s
+
+    # denoised error by input spp (the engine's images are vvpt_render's, bit for bit)
     den = torch.zeros((H, W, 4), device="cuda")
-    rows, best = [], None
-    for spp in (4, 8, 16, 32, 64, 128, 256):
+    sweep = []
+    for spp in (4, 8, 16, 32, 64):
         img, t_r = render(g, sd, info, spp, W, H)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         dn.apply(img["radiance"], img["albedo"], img["normal"], den)
         torch.cuda.synchronize()
         t_d = time.perf_counter() - t0
         err = _rel_rmse(den, ref["radiance"])
-        # the plain tracer's spp and time for the same error (fit e^2 = a / spp + b)
-        spp_eq = a / (err ** 2 - b) if err ** 2 > b else float("inf")
-        t_eq = W * H * spp_eq / paths_per_s
-        row = {"spp": spp, "rel_rmse_noisy": _rel_rmse(img["radiance"], ref["radiance"]),
-               "rel_rmse_denoised": err, "render_s": t_r, "denoise_s": t_d,
-               "plain_spp_same_error": spp_eq, "plain_s_same_error": t_eq, "gain": t_eq / (t_r + t_d)}
-        rows.append(row)
-        if best is None or row["gain"] > best["gain"]:
-            best = row
+        sweep.append({"spp": spp, "rel_rmse_noisy": _rel_rmse(img["radiance"], ref["radiance"]),
+                      "rel_rmse_denoised": err, "render_s": t_r, "denoise_s": t_d,
+                      "plain_spp_same_error": plain_spp_for(err)})
+    met = [r for r in sweep if r["rel_rmse_denoised"] <= target]
+    pick = met[0] if met else min(sweep, key=lambda r: r["rel_rmse_denoised"])
+    err_pick = pick["rel_rmse_denoised"]
+
+    # batched + served + denoised: M requests together through the job engine
+    M = args.requests_converged
+    outs = [bufs(W, H) for _ in range(M)]
+    dens = [torch.zeros((H, W, 4), device="cuda") for _ in range(M)]
+    info.samples = pick["spp"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    jobs, t_sub = [], []
+    for o in outs:
+        t_sub.append(time.perf_counter())
+        jobs.append(g.submit(sd, info, outputs={k: v.data_ptr() for k, v in o.items()}, env_is=True))
+    lat = []
+    for j, o, dd, ts in zip(jobs, outs, dens, t_sub):
+        j.wait()
+        dn.apply(o["radiance"], o["albedo"], o["normal"], dd)
+        torch.cuda.synchronize()
+        lat.append(1e3 * (time.perf_counter() - ts))
+        j.release()
+    wall = time.perf_counter() - t0
+    served_err = _rel_rmse(dens[-1], ref["radiance"])
+    served_iph = 3600.0 * M / wall
+    # the plain tracer at the error the served images reach (the target when met)
+    err_eq = max(served_err, target)
+    t_plain_eq = W * H * plain_spp_for(err_eq) / paths_per_s
+    plain_iph = 3600.0 / t_plain_eq
     g.release()
-    reachable = target ** 2 > b
-    line = {"metric": "converged images/hour at equal error vs the plain tracer", "unit": "images/h", "n_gpus": 1,
-            "steps": 1, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 tracer, bf16 denoiser", "data": "synthetic (seeded procedural scene)",
-            "value": 3600.0 / (best["render_s"] + best["denoise_s"]),
+    line = {"metric": "converged images/hour at relative RMSE <= 1e-2 vs the plain single-job tracer",
+            "unit": "images/h", "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 tracer, bf16 denoiser",
+            "data": "synthetic (seeded procedural scene)", "value": served_iph,
             "config": {"workload": "converged_instanced_sky_960x544", "target_rel_rmse": target,
-                       "metric": "sqrt(mean((x - ref)^2 / (ref^2 + 0.01)))",
-                       "reference": "4096 spp (GPU tracer, environment importance sampled)",
-                       "train": f"{args.train_steps} steps of 4 x 256^2 crops, 8 seeds x 4/8/16/32 spp inputs, "
-                                "1024-spp targets"},
-            "denoised": {"spp": best["spp"], "rel_rmse": best["rel_rmse_denoised"],
-                         "seconds": best["render_s"] + best["denoise_s"]},
-            "plain_same_error": {"spp": best["plain_spp_same_error"], "seconds": best["plain_s_same_error"],
-                                 "images_per_hour": 3600.0 / best["plain_s_same_error"]},
-            "gain_vs_plain": best["gain"],
-            "plain_fit": {"rel_rmse": {str(k): v[0] for k, v in plain.items()}, "a": a, "b": b,
-                          "paths_per_s": paths_per_s,
-                          "spp_for_target": spp_plain if reachable else None,
-                          "target_reachable": reachable},
-            "denoised_sweep": rows, "train_s": t_train, "final_train_loss": float(np.mean(losses[-20:])),
-            "reference_s": t_ref}
+                       "metric": "sqrt(sum((x - ref)^2) / sum(ref^2)) over RGB",
+                       "reference": f"{ref_spp} spp, FP64-accumulated batch sums (VVPT_RENDER_REDUCE_FP64), "
+                                    "environment importance sampled",
+                       "requests": M, "request_spp": pick["spp"],
+                       "train": f"{args.train_steps} steps of 4 x 256^2 crops from {args.train_crops} seeds x "
+                                f"{len(in_spps)} input spp (4/8/16, FP16), {ref_spp}-spp FP64 targets"},
+            "target_met": served_err <= target, "served_rel_rmse": served_err,
+            "reference_rel_noise": ref_noise,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(np.max(lat))},
+            "plain": {"images_per_hour": plain_iph, "spp": plain_spp_for(err_eq), "seconds_per_image": t_plain_eq,
+                      "at_rel_rmse": err_eq, "spp_for_target": spp_plain if spp_plain != float("inf") else None,
+                      "seconds_for_target": t_plain if t_plain != float("inf") else None,
+                      "fit": {"a": a, "b": b, "rel_rmse": {str(k): v[0] for k, v in plain.items()},
+                              "paths_per_s": paths_per_s}},
+            "gain_vs_plain": served_iph / plain_iph,
+            "denoised_sweep": sweep, "train_set_s": t_set, "train_s": t_train,
+            "final_train_loss": float(np.mean(losses[-20:])), "reference_s": t_ref}
     dn.close()
     ctx.close()
     print(json.dumps(line), flush=True)
@@ -736,7 +794,10 @@ def main():
                     default="cornell_medium")
     ap.add_argument("--sequential", action="store_true", help="batched64: also time the jobs one by one")
     ap.add_argument("--requests", type=int, default=512, help="serving512: number of requests")
+    ap.add_argument("--preview", action="store_true", help="serving512: preview sizes and spp")
     ap.add_argument("--train-steps", type=int, default=1500, help="converged: denoiser training steps")
+    ap.add_argument("--train-crops", type=int, default=16, help="converged: training scenes (512^2 crops)")
+    ap.add_argument("--requests-converged", type=int, default=16, help="converged: requests served together")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (no vvpt_autotune pass)")
     ap.add_argument("--width", type=int, default=0)

@@ -227,7 +227,13 @@ enum {
      * the sample index plus a blue-noise offset; per-sample dimension start
      * pixel.y * width + pixel.y and sample index batch * batch_size + s as
      * in raygen.rgen.glsl:57-61. Tables: vvpt_sampler_tables. */
-    VVPT_RENDER_SAMPLER_PMJ = 8u
+    VVPT_RENDER_SAMPLER_PMJ = 8u,
+    /* No counterpart in the reference (whose images accumulate in float,
+     * raygen.rgen.glsl:134-144): the per-batch sums are added in double
+     * precision, in batch order, and rounded to float once. For reference
+     * images of many batches (an FP64-accumulated high-spp render); the
+     * default float sum in batch order is the reference's sequence. */
+    VVPT_RENDER_REDUCE_FP64 = 16u
 };
 
 /* Sizes of the low-discrepancy sampler's tables

@@ -363,6 +363,26 @@ def test_converged_render_matches_fp64_oracle(ctx):
     assert abs(a.mean() - b.mean()) <= 1e-3 * b.mean(), (a.mean(), b.mean())
 
 
+def test_fp64_batch_reduction(ctx):
+    """VVPT_RENDER_REDUCE_FP64: the same per-batch sums added in double
+    precision. Against the float reduction the images differ by float
+    rounding only; against the oracle's FP64 render (double sums throughout)
+    they agree like the other renders."""
+    e, info = scenes.cornell_box(2, 64, 48, 1024, 8, 4)
+    fs = e.scene.build()
+    sd = e.scene.scene_data(info.width, info.height)
+    g = ctx.upload(fs)
+    f32 = g.render(sd, info, want_m2=True)
+    f64 = g.render(sd, info, want_m2=True, reduce_fp64=True)
+    g.release()
+    a, b = f64.radiance[..., :3].astype(np.float64), f32.radiance[..., :3].astype(np.float64)
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-7) and not np.array_equal(a, b)
+    assert np.array_equal(f64.albedo[..., 3], f32.albedo[..., 3])
+    ref = oracle.render(fs, sd, info, fp64=True)
+    rel, close, z4 = compare_renders(f64.radiance, ref["radiance"], f64.radiance_m2, info.samples // info.batch_size)
+    assert rel < 1e-4 and close >= 0.95 and z4 < 0.005, (rel, close, z4)
+
+
 def test_instanced_sky_scene_matches_oracle(ctx):
     """512 rigid instances of 8 displaced meshes (20.7M instanced
     triangles), 32 mesh lights, thin lens, procedural sky with the

@@ -32,6 +32,7 @@ TEXTURE_RGBA32F = 2
 RENDER_WANT_BATCH_M2 = 1
 RENDER_ENV_IS = 4
 RENDER_SAMPLER_PMJ = 8
+RENDER_REDUCE_FP64 = 16
 PMJ_SEQUENCES = 16
 PMJ_SAMPLES = 16384
 BLUE_NOISE_TEXTURES = 48

@@ -62,6 +62,7 @@ vvpt_status make_render_params(vvpt_ctx *ctx, const vvpt_scene *scene, const vvp
         return fail(ctx, VVPT_ERR_INVALID_ARG, "width * height * batches exceeds 2^32");
     hp.total_items = (uint32_t)total_items64;
     hp.want_m2 = (info->flags & VVPT_RENDER_WANT_BATCH_M2) ? 1u : 0u;
+    hp.reduce_fp64 = (info->flags & VVPT_RENDER_REDUCE_FP64) ? 1u : 0u;
     const int mode = (int)hp.env_type;
     hp.env_light = ((info->flags & VVPT_RENDER_ENV_IS) && scene->view.env_func_int > 0.0f && (mode == 1 || mode == 2))
                        ? 1u

@@ -1512,13 +1512,29 @@ __global__ void k_reduce(RenderParams p, BatchResults br, float4 *rad, float4 *a
     const uint32_t npix = p.width * p.height;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
         float3 r = f3(0.0f), a = f3(0.0f), nn = f3(0.0f), q2 = f3(0.0f);
-        for (uint32_t b = 0; b < p.batches; b++) {
-            const size_t it = (size_t)b * npix + pix;
-            float3 rb = f3(br.rad[it]);
-            r = r + rb;
-            a = a + f3(br.alb[it]);
-            nn = nn + f3(br.nrm[it]);
-            q2 = q2 + rb * rb;
+        if (p.reduce_fp64) {
+            double s[12] = {0.0};
+            for (uint32_t b = 0; b < p.batches; b++) {
+                const size_t it = (size_t)b * npix + pix;
+                const float4 rb = br.rad[it], ab = br.alb[it], nb = br.nrm[it];
+                s[0] += rb.x, s[1] += rb.y, s[2] += rb.z;
+                s[3] += ab.x, s[4] += ab.y, s[5] += ab.z;
+                s[6] += nb.x, s[7] += nb.y, s[8] += nb.z;
+                s[9] += (double)rb.x * rb.x, s[10] += (double)rb.y * rb.y, s[11] += (double)rb.z * rb.z;
+            }
+            r = f3((float)s[0], (float)s[1], (float)s[2]);
+            a = f3((float)s[3], (float)s[4], (float)s[5]);
+            nn = f3((float)s[6], (float)s[7], (float)s[8]);
+            q2 = f3((float)s[9], (float)s[10], (float)s[11]);
+        } else {
+            for (uint32_t b = 0; b < p.batches; b++) {
+                const size_t it = (size_t)b * npix + pix;
+                float3 rb = f3(br.rad[it]);
+                r = r + rb;
+                a = a + f3(br.alb[it]);
+                nn = nn + f3(br.nrm[it]);
+                q2 = q2 + rb * rb;
+            }
         }
         if (rad)
             rad[pix] = f4(r, 1.0f);

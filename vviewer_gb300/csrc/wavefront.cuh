@@ -26,6 +26,7 @@ struct RenderParams {
     uint32_t num_lights;  // pathTracingData.lights.r
     uint32_t total_items; // width * height * batches
     uint32_t want_m2;
+    uint32_t reduce_fp64; // 1: batch sums added in double (VVPT_RENDER_REDUCE_FP64)
     uint32_t env_light;   // 1: the environment is sampled as one more light (VVPT_RENDER_ENV_IS)
     uint32_t sampler;     // 0: RTGEMS stream, 1: PMJ (VVPT_RENDER_SAMPLER_PMJ)
     const float *pmj;        // [16][16384][2] (sampler 1)

@@ -155,15 +155,17 @@ class GpuScene:
     def render(self, scene_data: N.SceneData, info: RenderInfo, want_m2: bool = False,
                outputs: dict | None = None, profile: bool = False,
                host_outputs: dict | None = None, env_is: bool = False,
-               sampler: str = "rtgems") -> RenderResult | None:
+               sampler: str = "rtgems", reduce_fp64: bool = False) -> RenderResult | None:
         """Renders into new host arrays, into caller-provided host arrays
         (`host_outputs`), or into device pointers when `outputs` maps
         radiance/albedo/normal/radiance_m2 to device addresses. env_is: the
         environment is importance sampled as a light (VVPT_RENDER_ENV_IS).
         sampler: 'rtgems' (the reference's default xorshift stream) or 'pmj'
-        (its low-discrepancy sampler, VVPT_RENDER_SAMPLER_PMJ)."""
+        (its low-discrepancy sampler, VVPT_RENDER_SAMPLER_PMJ). reduce_fp64:
+        the batch sums are added in double precision (VVPT_RENDER_REDUCE_FP64)."""
         flags = ((N.RENDER_WANT_BATCH_M2 if want_m2 else 0) | (N.RENDER_PROFILE_KERNELS if profile else 0) |
-                 (N.RENDER_ENV_IS if env_is else 0) | _sampler_flag(sampler))
+                 (N.RENDER_ENV_IS if env_is else 0) | _sampler_flag(sampler) |
+                 (N.RENDER_REDUCE_FP64 if reduce_fp64 else 0))
         ri = N.RenderInfo(info.samples, info.depth, info.batch_size, info.width, info.height, flags)
         if host_outputs is not None:
             o = N.Outputs(host_outputs.get("radiance"), host_outputs.get("albedo"), host_outputs.get("normal"),

@@ -319,15 +319,17 @@ RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
 SPPS = [16, 64, 256]
 
 
-def job_mix(seed: int, n_jobs: int, n_scenes: int) -> list[tuple[int, RenderInfo]]:
-    """(scene index, render info) per job: scene drawn from a pool of n_scenes,
-    resolution from {256^2, 512^2, 1024^2, 1920x1080}, spp from {16, 64, 256}."""
+def job_mix(seed: int, n_jobs: int, n_scenes: int, distinct: bool = False) -> list[tuple[int, RenderInfo]]:
+    """(scene index, render info) per job: scene drawn from a pool of n_scenes
+    (or, with distinct, job j renders scene j), resolution from {256^2, 512^2,
+    1024^2, 1920x1080}, spp from {16, 64, 256}."""
     rng = np.random.Generator(np.random.PCG64(seed))
     jobs = []
     for j in range(n_jobs):
         w, h = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
         spp = SPPS[int(rng.integers(0, len(SPPS)))]
-        jobs.append((int(rng.integers(0, n_scenes)),
+        k = int(rng.integers(0, n_scenes))
+        jobs.append((j if distinct else k,
                      RenderInfo(samples=spp, depth=8, batch_size=4, width=w, height=h, filename=f"job{j}",
                                 write_files=False)))
     return jobs
@@ -471,19 +473,21 @@ SERVING_RESOLUTIONS = [(256, 256), (512, 512)]
 SERVING_SPPS = [8, 16, 32]
 
 
-def serving_requests(seed: int, n_requests: int, n_scenes: int, mean_gap_ms: float = 50.0):
+def serving_requests(seed: int, n_requests: int, n_scenes: int, mean_gap_ms: float = 50.0, preview: bool = False):
     """(arrival ms, scene index, render info) per request: Poisson arrivals
     (exponential gaps, mean `mean_gap_ms`), scenes from the pool of the
-    batched workload, resolution from {256^2, 512^2} and spp from {8, 16, 32}
-    (preview renders: about 3.1M paths per request, an offered load of about
-    61M paths/s at 50 ms gaps, below one GPU's throughput)."""
+    batched workload, resolution and spp drawn as in the batched workload
+    ({256^2, 512^2, 1024^2, 1920x1080}, {16, 64, 256}: about 94M paths per
+    request, an offered load far above one GPU, so requests queue for
+    admission), or with `preview` from {256^2, 512^2} and {8, 16, 32}."""
     rng = np.random.Generator(np.random.PCG64(seed))
     gaps = rng.exponential(mean_gap_ms, n_requests)
     t = np.cumsum(gaps) - gaps[0]
+    res, spps = (SERVING_RESOLUTIONS, SERVING_SPPS) if preview else (RESOLUTIONS, SPPS)
     out = []
     for j in range(n_requests):
-        w, h = SERVING_RESOLUTIONS[int(rng.integers(0, len(SERVING_RESOLUTIONS)))]
-        spp = SERVING_SPPS[int(rng.integers(0, len(SERVING_SPPS)))]
+        w, h = res[int(rng.integers(0, len(res)))]
+        spp = spps[int(rng.integers(0, len(spps)))]
         out.append((float(t[j]), int(rng.integers(0, n_scenes)),
                     RenderInfo(samples=spp, depth=8, batch_size=4, width=w, height=h, filename=f"req{j}",
                                write_files=False)))
