@@ -544,6 +544,32 @@ def denoiser_flops(h: int, w: int, n: int = 1) -> float:
     return total
 
 
+def denoiser_layer_bounds(h: int, w: int, hbm_gbs: float, tflops: float) -> list[dict]:
+    """Per convolution layer of one forward pass: FLOPs, compulsory bytes
+    (BF16 input and output activations once, BF16 weights once) and the
+    roofline time max(bytes / HBM, FLOP / tensor peak). The 32-channel
+    full-resolution layers sit below the ridge (about 144 FLOP/B against
+    peak/HBM of about 285), so HBM bounds them."""
+    from oracle import denoiser_oracle as D
+    lv_of = []
+    for l in range(D.LEVELS):
+        lv_of += [l, l]
+    for l in range(D.LEVELS - 2, -1, -1):
+        lv_of += [l, l]
+    lv_of.append(0)
+    out = []
+    for k, ((cin, cout, _), l) in enumerate(zip(D.layers(), lv_of)):
+        px = (h >> l) * (w >> l)
+        fl = 2.0 * 9 * cin * cout * px
+        by = 2.0 * px * (cin + cout) + 2.0 * 9 * cin * cout
+        t_hbm = by / (hbm_gbs * 1e9) * 1e3
+        t_tc = fl / (tflops * 1e12) * 1e3
+        out.append({"layer": k, "level": l, "cin": cin, "cout": cout, "flops": fl, "bytes": by,
+                    "flop_per_byte": fl / by, "bound": "hbm" if t_hbm > t_tc else "tensor",
+                    "bound_ms": max(t_hbm, t_tc)})
+    return out
+
+
 def run_denoise(args) -> None:
     """Denoiser inference at 3840 x 2160 (one frame; --width/--height for
     another size, multiples of 16) and one training step on 8 crops of 256^2,
@@ -590,7 +616,10 @@ def run_denoise(args) -> None:
     train_ms = (time.perf_counter() - t0) / 5 * 1e3
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = flops / (infer_ms / 1e3) / 1e12
+    layers = denoiser_layer_bounds(H, W, hbm, peak)
+    bound_ms = sum(l["bound_ms"] for l in layers)
     line = {"metric": "denoised frames/s", "value": 1e3 / infer_ms, "unit": "frames/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": infer_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic inputs",
@@ -600,6 +629,8 @@ def run_denoise(args) -> None:
                              "than L2"},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None, "flops_per_frame": flops},
+            "layer_roofline": {"bound_ms": bound_ms, "frac_of_bound": bound_ms / infer_ms,
+                               "hbm_gbs": hbm, "tensor_tflops": peak, "layers": layers},
             "train_step_ms": train_ms, "train_tflops": 3 * denoiser_flops(256, 256, 8) / (train_ms / 1e3) / 1e12}
     dn.close()
     ctx.close()

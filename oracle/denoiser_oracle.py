@@ -120,6 +120,37 @@ def features(rad, alb, nrm, R):
     return R(x)
 
 
+def forward_image(flat_params, rad, alb, nrm, exact=False):
+    """The denoised image vvpt_denoiser_apply returns: the network's forward
+    pass with the GPU's rounding points (BF16 features, weights and hidden
+    activations; the output layer's sums kept in full precision), then
+    expm1(max(y, 0)) per radiance channel and alpha 1. [n, h, w, 4] float64."""
+    R = _R(exact)
+    P = unpack_params(np.asarray(flat_params, dtype=np.float64))
+    L = layers()
+    Wq = [(R(W), b.astype(np.float32).astype(np.float64)) for W, b in P]
+
+    def fwd(li, x):
+        W, b = Wq[li]
+        z = conv3x3(x, W) + b
+        return R(np.maximum(z, 0.0)) if L[li][2] else z
+
+    xs, es, ds = [None] * LEVELS, [None] * LEVELS, {}
+    xs[0] = features(rad, alb, nrm, R)
+    for lv in range(LEVELS):
+        if lv > 0:
+            xs[lv] = R(pool(es[lv - 1]))
+        es[lv] = fwd(2 * lv + 1, fwd(2 * lv, xs[lv]))
+    for lv in range(LEVELS - 2, -1, -1):
+        coarse = es[LEVELS - 1] if lv == LEVELS - 2 else ds[lv + 1]
+        li = 10 + 2 * (LEVELS - 2 - lv)
+        ds[lv] = fwd(li + 1, fwd(li, np.concatenate([up(coarse), es[lv]], axis=-1)))
+    y = fwd(len(L) - 1, ds[0])
+    out = np.ones(y.shape[:3] + (4,))
+    out[..., :3] = np.expm1(np.maximum(y[..., :3], 0.0))
+    return out
+
+
 def loss_and_grads(flat_params, rad, alb, nrm, target, exact=False):
     """Loss and flat gradient with the GPU's rounding points (exact=False)."""
     R = _R(exact)

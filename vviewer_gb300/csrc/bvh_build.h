@@ -21,11 +21,22 @@ struct Box3 {
     float hi[3];
 };
 
+// BLAS build parameters (build-time overridable for tuning experiments)
+#ifndef VVPT_BVH_BINS
+#define VVPT_BVH_BINS 32
+#endif
+#ifndef VVPT_BVH_MAX_LEAF
+#define VVPT_BVH_MAX_LEAF 4
+#endif
+#ifndef VVPT_BVH_COST_TRAVERSAL
+#define VVPT_BVH_COST_TRAVERSAL 1.0
+#endif
+
 struct BVHBuildOptions {
-    int bins = 32;          // SAH bins per axis
-    int max_leaf = 4;       // preferred leaf size
+    int bins = VVPT_BVH_BINS;         // SAH bins per axis
+    int max_leaf = VVPT_BVH_MAX_LEAF; // preferred leaf size
     int max_depth = 56;     // force leaves below this depth (traversal stack bound)
-    double cost_traversal = 1.0;
+    double cost_traversal = VVPT_BVH_COST_TRAVERSAL;
     double cost_intersect = 1.0;
     int threads = 0;        // 0 = hardware concurrency (large builds only)
 };

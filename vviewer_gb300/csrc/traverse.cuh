@@ -18,6 +18,12 @@
 
 namespace vvpt {
 
+// Traversal step counter hook (node visits, triangle tests, instance
+// entries) for host builds that measure BVH quality; empty otherwise.
+#ifndef VVPT_TRAVERSAL_STAT
+#define VVPT_TRAVERSAL_STAT(kind)
+#endif
+
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 // device status word bits
 constexpr uint32_t kErrStackOverflow = 1u;
@@ -171,13 +177,13 @@ __device__ __forceinline__ float cull_slack(const SceneView &s, const float3 &o,
     return dm > 0.0f ? 1e-5f * (s.cull_o * om + s.cull_r) / dm : 0.0f;
 }
 
-// Loads of BVH nodes and triangles. On the device they carry an L2
-// evict-last policy (VVPT_SCENE_L2_KEEP, default on): the scene's nodes and
-// triangles are re-read by every traversal kernel, while the path state and
-// queues stream through L2 once per kernel, so the scene's lines are the
-// ones to keep.
+// Loads of BVH nodes and triangles. With VVPT_SCENE_L2_KEEP = 1 (a build
+// option) they carry an L2 evict-last policy, so that the scene's lines,
+// re-read by every traversal kernel, outlive the path state and queues that
+// stream through L2. Measured on the 1080p medium scene: no gain (137.3
+// against 140.3 M paths/s without it, within run-to-run spread), so off.
 #ifndef VVPT_SCENE_L2_KEEP
-#define VVPT_SCENE_L2_KEEP 1
+#define VVPT_SCENE_L2_KEEP 0
 #endif
 #if defined(__CUDA_ARCH__) && VVPT_SCENE_L2_KEEP
 __device__ __forceinline__ uint64_t scene_l2_policy()
@@ -443,6 +449,7 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
         }
 #endif
         if (leaf_count > 0) {
+            VVPT_TRAVERSAL_STAT(1);
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
             const float4 p0 = ldg_scene(tp), p1 = ldg_scene(tp + 1), p2 = ldg_scene(tp + 2);
             const uint32_t prim = __float_as_uint(p0.w);
@@ -460,6 +467,7 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             continue;
         }
         if (node >= 0) {
+            VVPT_TRAVERSAL_STAT(in_blas ? 0 : 3);
             const BVHNode n = (!in_blas && node < cached) ? load_node_cached(node)
                                                           : load_node(s.nodes, (int)node_base + node);
             float tl, tr;
@@ -514,6 +522,7 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             leaf_first = e.x;
             leaf_count = cnt;
         } else if (tag == kTagInst) {
+            VVPT_TRAVERSAL_STAT(2);
             if (cnt > 1)
                 push(e.x + 1, kTagInst, cnt - 1);
             inst_id = __ldg(s.tlas_order + e.x);

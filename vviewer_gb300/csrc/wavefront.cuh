@@ -160,10 +160,14 @@ enum KernelId {
     K_SHADOW = 6, // shadow rays, then the emitter rays of paths that end
     K_NUM = 7
 };
-// K_SHADE launches one kernel per material-sorted queue (VVPT_SHADE_SPLIT,
-// default on) or one over all three
+// K_SHADE launches one kernel over the three material-sorted queues, or with
+// VVPT_SHADE_SPLIT = 1 (a build option) one kernel per queue, each compiled
+// for its own surface model. Measured on the 1080p medium scene: the same
+// shading time either way (the split kernels need the same 128 registers,
+// set by the medium, light-sampling and emitter-ray code they share; capped
+// at 3 blocks per SM they spill and run slower), so one launch.
 #ifndef VVPT_SHADE_SPLIT
-#define VVPT_SHADE_SPLIT 1
+#define VVPT_SHADE_SPLIT 0
 #endif
 constexpr int kShadeLaunches = VVPT_SHADE_SPLIT ? 3 : 1;
 constexpr int launches_of(int k) { return k == K_SHADE ? kShadeLaunches : 1; }
