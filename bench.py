@@ -753,9 +753,10 @@ def run_converged(args) -> None:
         torch.cuda.synchronize()
         t_d = time.perf_counter() - t0
         err = _rel_rmse(den, ref["radiance"])
+        spp_eq = plain_spp_for(err)
         sweep.append({"spp": spp, "rel_rmse_noisy": _rel_rmse(img["radiance"], ref["radiance"]),
                       "rel_rmse_denoised": err, "render_s": t_r, "denoise_s": t_d,
-                      "plain_spp_same_error": plain_spp_for(err)})
+                      "plain_spp_same_error": spp_eq if spp_eq != float("inf") else None})
     met = [r for r in sweep if r["rel_rmse_denoised"] <= target]
     pick = met[0] if met else min(sweep, key=lambda r: r["rel_rmse_denoised"])
     err_pick = pick["rel_rmse_denoised"]
@@ -784,7 +785,7 @@ def run_converged(args) -> None:
     # the plain tracer at the error the served images reach (the target when met)
     err_eq = max(served_err, target)
     t_plain_eq = W * H * plain_spp_for(err_eq) / paths_per_s
-    plain_iph = 3600.0 / t_plain_eq
+    plain_iph = 3600.0 / t_plain_eq  # 0 when the fit says the plain tracer cannot reach that error
     g.release()
     line = {"metric": "converged images/hour at relative RMSE <= 1e-2 vs the plain single-job tracer",
             "unit": "images/h", "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True,
@@ -801,12 +802,14 @@ def run_converged(args) -> None:
             "reference_rel_noise": ref_noise,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(np.max(lat))},
-            "plain": {"images_per_hour": plain_iph, "spp": plain_spp_for(err_eq), "seconds_per_image": t_plain_eq,
+            "plain": {"images_per_hour": plain_iph,
+                      "spp": plain_spp_for(err_eq) if plain_iph > 0 else None,
+                      "seconds_per_image": t_plain_eq if plain_iph > 0 else None,
                       "at_rel_rmse": err_eq, "spp_for_target": spp_plain if spp_plain != float("inf") else None,
                       "seconds_for_target": t_plain if t_plain != float("inf") else None,
                       "fit": {"a": a, "b": b, "rel_rmse": {str(k): v[0] for k, v in plain.items()},
                               "paths_per_s": paths_per_s}},
-            "gain_vs_plain": served_iph / plain_iph,
+            "gain_vs_plain": served_iph / plain_iph if plain_iph > 0 else None,
             "denoised_sweep": sweep, "train_set_s": t_set, "train_s": t_train,
             "final_train_loss": float(np.mean(losses[-20:])), "reference_s": t_ref}
     dn.close()
