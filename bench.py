@@ -275,7 +275,11 @@ def run_ours(args) -> None:
 
     env_is = bool(desc.get("env_is", False))
     tuning = None
-    if not args.no_autotune:
+    if args.tuning:
+        slots, blocks = (int(x) for x in args.tuning.split(","))
+        ctx.set_tuning(slots=slots, blocks_per_sm=blocks)
+        tuning = {"slots": slots, "blocks_per_sm": blocks, "threads_per_block": 0, "iterations_per_graph": 0}
+    elif not args.no_autotune:
         tuning = gpu.autotune(sd, info, budget_ms=4000.0, env_is=env_is)
     for _ in range(args.warmup):
         gpu.render(sd, info, outputs=dev_ptrs, env_is=env_is)
@@ -834,6 +838,7 @@ def main():
     ap.add_argument("--requests-converged", type=int, default=16, help="converged: requests served together")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (no vvpt_autotune pass)")
+    ap.add_argument("--tuning", default="", help="SLOTS,BLOCKS_PER_SM: a fixed tuning instead of the autotune pass")
     ap.add_argument("--width", type=int, default=0)
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)

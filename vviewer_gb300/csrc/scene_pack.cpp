@@ -480,8 +480,11 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
         out.emit_boxes.push_back(make_float4(b.hi[0], b.hi[1], b.hi[2], 0.0f));
     }
     // one instance per TLAS leaf: entering an instance costs a BLAS traversal
+#ifndef VVPT_TLAS_MAX_LEAF
+#define VVPT_TLAS_MAX_LEAF 1
+#endif
     BVHBuildOptions tlas_opt;
-    tlas_opt.max_leaf = 1;
+    tlas_opt.max_leaf = VVPT_TLAS_MAX_LEAF;
     BVHBuildResult tlas = build_bvh2(tlas_boxes, tlas_opt);
     out.tlas_root = (uint32_t)nodes.size();
     nodes.insert(nodes.end(), tlas.nodes.begin(), tlas.nodes.end());
