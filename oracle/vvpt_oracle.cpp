@@ -155,6 +155,7 @@ inline uint32_t initRNG(uint32_t px, uint32_t py, uint32_t resx, uint32_t frame)
 struct Tri {
     V3 p0, p1, p2;
     uint32_t prim;
+    uint32_t inst = 0xFFFFFFFFu; // baked small-instance triangles: their instance
 };
 struct Node {
     float lo[3], hi[3];
@@ -404,12 +405,13 @@ void trace_mesh(const Scene &s, uint32_t inst_id, V3 o, V3 d, float tmin, float 
             for (int k = n.first; k < n.first + n.count; k++) {
                 const Tri &tr = m.tris[k];
                 float t, u, v;
-                if (wtest(wr, tr, tmin, best.t, t, u, v) && hit_better(t, inst_id, tr.prim, best) &&
-                    hit_after(t, inst_id, tr.prim, after)) {
+                const uint32_t hinst = tr.inst != 0xFFFFFFFFu ? tr.inst : inst_id;
+                if (wtest(wr, tr, tmin, best.t, t, u, v) && hit_better(t, hinst, tr.prim, best) &&
+                    hit_after(t, hinst, tr.prim, after)) {
                     best.t = t;
                     best.u = u;
                     best.v = v;
-                    best.inst = inst_id;
+                    best.inst = hinst;
                     best.prim = tr.prim;
                 }
             }
@@ -1847,6 +1849,26 @@ bool build_scene(const vvpt_scene_desc *desc, Scene &s)
     }
     s.inst.resize(desc->num_instances);
     std::vector<std::array<float, 6>> tboxes;
+    // Small instances: at most kFlatMaxTriangles triangles, two or more of
+    // them. They leave the TLAS; their triangles, baked into world space, form
+    // one mesh under an identity instance, each triangle naming its instance
+    // (the library's layout, which changes the rounding of their hits: the
+    // test runs in world space on baked vertices).
+    const uint32_t kFlatMaxTriangles = 64;
+    std::vector<uint8_t> flat(desc->num_instances, 0);
+    uint32_t nflat = 0;
+    for (uint32_t i = 0; i < desc->num_instances; i++) {
+        const vvpt_instance &src = desc->instances[i];
+        Rows tmp;
+        if ((src.flags & VVPT_INSTANCE_IN_TLAS) && src.mesh_index < desc->num_meshes &&
+            s.meshes[src.mesh_index].ntri > 0 && s.meshes[src.mesh_index].ntri <= kFlatMaxTriangles &&
+            invert_rows(src.model, tmp)) {
+            flat[i] = 1;
+            nflat++;
+        }
+    }
+    if (nflat < 2)
+        std::fill(flat.begin(), flat.end(), 0);
     for (uint32_t i = 0; i < desc->num_instances; i++) {
         const vvpt_instance &src = desc->instances[i];
         Inst &in = s.inst[i];
@@ -1857,7 +1879,7 @@ bool build_scene(const vvpt_scene_desc *desc, Scene &s)
         if (!invert_rows(src.model, in.w2o) && (src.flags & VVPT_INSTANCE_IN_TLAS))
             return false;
         in.mesh = src.mesh_index < desc->num_meshes ? (int)src.mesh_index : -1;
-        in.in_tlas = (src.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh >= 0 && s.meshes[in.mesh].ntri > 0;
+        in.in_tlas = (src.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh >= 0 && s.meshes[in.mesh].ntri > 0 && !flat[i];
         if (in.in_tlas) {
             const Mesh &m = s.meshes[in.mesh];
             std::array<float, 6> b;
@@ -1887,6 +1909,91 @@ bool build_scene(const vvpt_scene_desc *desc, Scene &s)
             tboxes.push_back(b);
             s.tlas_ids.push_back(i);
         }
+    }
+    if (nflat >= 2) {
+        // world = ((r0 * x + r1 * y) + r2 * z) + r3 per model row, in double,
+        // rounded to float
+        Mesh fm;
+        std::vector<std::array<float, 6>> fboxes;
+        std::vector<Tri> ftris;
+        double mag = 0.0;
+        for (uint32_t i = 0; i < desc->num_instances; i++) {
+            if (!flat[i])
+                continue;
+            const Inst &in = s.inst[i];
+            const Mesh &m = s.meshes[in.mesh];
+            for (uint32_t t = 0; t < m.ntri; t++) {
+                V3 q[3];
+                std::array<float, 6> b;
+                for (int a = 0; a < 3; a++) {
+                    b[a] = FLT_MAX;
+                    b[3 + a] = -FLT_MAX;
+                }
+                for (int k = 0; k < 3; k++) {
+                    const float *p = m.v[m.idx[3 * t + k]].position;
+                    float w[3];
+                    for (int a = 0; a < 3; a++) {
+                        double v = (double)in.o2w.m[a][0] * p[0];
+                        v = v + (double)in.o2w.m[a][1] * p[1];
+                        v = v + (double)in.o2w.m[a][2] * p[2];
+                        v = v + (double)in.o2w.m[a][3];
+                        w[a] = (float)v;
+                        b[a] = std::min(b[a], w[a]);
+                        b[3 + a] = std::max(b[3 + a], w[a]);
+                        mag = std::max(mag, (double)std::fabs(w[a]));
+                    }
+                    q[k] = v3(w[0], w[1], w[2]);
+                }
+                Tri tr;
+                tr.p0 = q[0];
+                tr.p1 = q[1];
+                tr.p2 = q[2];
+                tr.prim = t;
+                tr.inst = i;
+                ftris.push_back(tr);
+                fboxes.push_back(b);
+            }
+        }
+        fm.ntri = (uint32_t)ftris.size();
+        for (int a = 0; a < 3; a++) {
+            fm.lo[a] = FLT_MAX;
+            fm.hi[a] = -FLT_MAX;
+        }
+        for (const auto &b : fboxes)
+            for (int a = 0; a < 3; a++) {
+                fm.lo[a] = std::min(fm.lo[a], b[a]);
+                fm.hi[a] = std::max(fm.hi[a], b[3 + a]);
+            }
+        build_bvh(fboxes, fm.bvh);
+        fm.tris.resize(ftris.size());
+        for (size_t k = 0; k < ftris.size(); k++)
+            fm.tris[k] = ftris[fm.bvh.order[k]];
+        const int fmi = (int)s.meshes.size();
+        std::array<float, 6> wb;
+        for (int a = 0; a < 3; a++) {
+            const float pad = 1e-5f * (std::fabs(fm.lo[a]) + std::fabs(fm.hi[a]) + 1e-3f);
+            wb[a] = fm.lo[a] - pad;
+            wb[3 + a] = fm.hi[a] + pad;
+        }
+        s.meshes.push_back(std::move(fm));
+        Inst syn;
+        const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++)
+                syn.o2w.m[r][c] = ident[c * 4 + r];
+        invert_rows(ident, syn.w2o);
+        for (uint32_t i = 0; i < desc->num_instances; i++)
+            if (flat[i]) {
+                syn.src = &desc->instances[i]; // never reported: hits name the baked triangle's instance
+                break;
+            }
+        syn.mesh = fmi;
+        syn.in_tlas = true;
+        s.cull_o = std::max(s.cull_o, 1.0f);
+        s.cull_r = std::max(s.cull_r, (float)mag);
+        s.tlas_ids.push_back((uint32_t)s.inst.size());
+        s.inst.push_back(syn);
+        tboxes.push_back(wb);
     }
     if (!tboxes.empty())
         build_bvh(tboxes, s.tlas);

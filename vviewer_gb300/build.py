@@ -21,9 +21,13 @@ BUILD_DIR = PKG / "_build"
 LIB = OUT_DIR / "libvvpt.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off on the host compilers: the scene packing (inverse
+# transforms, baked small-instance triangles) rounds the same on x86 and Arm
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(CSRC)]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-I", str(ROOT / "include"), "-I", str(CSRC)]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", str(ROOT / "include"),
+             "-I", str(CSRC)]
 
 
 def _nvcc() -> str:

@@ -65,10 +65,13 @@ struct alignas(16) WideNode {
 static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
 
 // Triangle in leaf order for intersection: v0.w carries the original
-// primitive index (gl_PrimitiveID) as raw bits.
+// primitive index (gl_PrimitiveID) as raw bits; v1.w is 0, or for the
+// baked world-space triangles of small instances (kFlattenMaxTriangles) the
+// instance slot + 1 as raw bits, the instance a hit on it reports.
 struct alignas(16) TriVerts {
     float4 v0, v1, v2;
 };
+constexpr uint32_t kFlattenMaxTriangles = 64;
 
 // Shading vertex: position + u, normal + v, tangent (+pad). Bitangents are not
 // kept: fixFrame (shaders/include/frame.glsl:7-36) overwrites the bitangent in

@@ -381,6 +381,27 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
     dinst.assign(ni, DevInstance{});
     std::vector<Box3> tlas_boxes;
     std::vector<uint32_t> tlas_ids;
+    // Small instances (at most kFlattenMaxTriangles triangles each, two or
+    // more of them) leave the TLAS: their triangles, baked into world space,
+    // form one extra BLAS under an identity instance, and each baked
+    // triangle carries its instance slot, which the traversal reports as the
+    // hit's instance. Rays then enter one BLAS instead of several small ones
+    // whose boxes span the scene (a room's walls, a medium's boundary).
+    std::vector<uint8_t> flat(ni, 0);
+    uint32_t nflat = 0;
+    for (uint32_t i = 0; i < ni; i++) {
+        const vvpt_instance &in = desc->instances[i];
+        if ((in.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh_index < nm && minfo[in.mesh_index].num_triangles > 0 &&
+            minfo[in.mesh_index].num_triangles <= kFlattenMaxTriangles) {
+            float4 inv[3];
+            if (affine_inverse_rows(in.model, inv)) {
+                flat[i] = 1;
+                nflat++;
+            }
+        }
+    }
+    if (nflat < 2)
+        std::fill(flat.begin(), flat.end(), 0);
     for (uint32_t i = 0; i < ni; i++) {
         const vvpt_instance &in = desc->instances[i];
         DevInstance &d = dinst[i];
@@ -403,6 +424,7 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
         }
         if ((in.flags & VVPT_INSTANCE_IN_TLAS) && in.mesh_index < nm && minfo[in.mesh_index].num_triangles > 0) {
             const Box3 &r = builds[in.mesh_index].root;
+            const bool in_flat = flat[i] != 0;
             Box3 w;
             for (int a = 0; a < 3; a++) {
                 w.lo[a] = INFINITY;
@@ -436,13 +458,105 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
             double pm = 0.0;
             for (int a = 0; a < 3; a++)
                 pm = std::max({pm, (double)std::fabs(r.lo[a]), (double)std::fabs(r.hi[a])});
-            out.cull_o = std::max(out.cull_o, (float)(na * ninv));
-            out.cull_r = std::max(out.cull_r, (float)(na * (ninv * bt + pm)));
-            tlas_boxes.push_back(w);
-            tlas_ids.push_back(i);
+            if (!in_flat) {
+                out.cull_o = std::max(out.cull_o, (float)(na * ninv));
+                out.cull_r = std::max(out.cull_r, (float)(na * (ninv * bt + pm)));
+                tlas_boxes.push_back(w);
+                tlas_ids.push_back(i);
+            }
             if (may_emit[d.material])
                 emit.push_back(w);
         }
+    }
+    if (nflat >= 2) {
+        // baked triangles: world = ((r.x * x + r.y * y) + r.z * z) + r.w per
+        // row of the instance's model matrix, in double, rounded to float
+        std::vector<TriVerts> ft;
+        std::vector<Box3> fb;
+        double fm = 0.0;
+        for (uint32_t i = 0; i < ni; i++) {
+            if (!flat[i])
+                continue;
+            const vvpt_instance &in = desc->instances[i];
+            const vvpt_mesh_desc &md = desc->meshes[in.mesh_index];
+            const float4 *R = dinst[i].o2w;
+            const float rr[3][4] = {{R[0].x, R[0].y, R[0].z, R[0].w},
+                                    {R[1].x, R[1].y, R[1].z, R[1].w},
+                                    {R[2].x, R[2].y, R[2].z, R[2].w}};
+            for (uint32_t t = 0; t < md.num_triangles; t++) {
+                float q[3][3];
+                Box3 b;
+                for (int a = 0; a < 3; a++) {
+                    b.lo[a] = INFINITY;
+                    b.hi[a] = -INFINITY;
+                }
+                for (int c = 0; c < 3; c++) {
+                    const float *p = md.vertices[md.indices[3 * t + c]].position;
+                    for (int a = 0; a < 3; a++) {
+                        double v = (double)rr[a][0] * p[0];
+                        v = v + (double)rr[a][1] * p[1];
+                        v = v + (double)rr[a][2] * p[2];
+                        v = v + (double)rr[a][3];
+                        q[c][a] = (float)v;
+                        b.lo[a] = std::min(b.lo[a], q[c][a]);
+                        b.hi[a] = std::max(b.hi[a], q[c][a]);
+                        fm = std::max(fm, (double)std::fabs(q[c][a]));
+                    }
+                }
+                TriVerts tv;
+                float pid, iid;
+                const uint32_t slot = i + 1;
+                std::memcpy(&pid, &t, 4);
+                std::memcpy(&iid, &slot, 4);
+                tv.v0 = make_float4(q[0][0], q[0][1], q[0][2], pid);
+                tv.v1 = make_float4(q[1][0], q[1][1], q[1][2], iid);
+                tv.v2 = make_float4(q[2][0], q[2][1], q[2][2], 0.0f);
+                ft.push_back(tv);
+                fb.push_back(b);
+            }
+        }
+        BVHBuildResult fbvh = build_bvh2(fb, BVHBuildOptions());
+        DevInstance syn;
+        std::memset(&syn, 0, sizeof(syn));
+        const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        affine_rows(ident, syn.o2w);
+        affine_rows(ident, syn.w2o);
+        syn.tri_offset = (uint32_t)tris.size();
+        syn.num_triangles = (uint32_t)ft.size();
+        syn.front_volume = syn.back_volume = -1;
+#if VVPT_BLAS_WIDE
+        WideBuildResult fw = collapse_to_wide(fbvh, fb);
+        syn.node_offset = (uint32_t)wnodes.size();
+        wnodes.insert(wnodes.end(), fw.nodes.begin(), fw.nodes.end());
+        const std::vector<uint32_t> &forder = fw.order;
+#else
+        syn.node_offset = (uint32_t)nodes.size();
+        nodes.insert(nodes.end(), fbvh.nodes.begin(), fbvh.nodes.end());
+        const std::vector<uint32_t> &forder = fbvh.order;
+#endif
+        for (uint32_t k = 0; k < (uint32_t)ft.size(); k++)
+            tris.push_back(ft[forder[k]]);
+        Box3 w;
+        for (int a = 0; a < 3; a++) {
+            w.lo[a] = INFINITY;
+            w.hi[a] = -INFINITY;
+        }
+        for (const Box3 &b : fb)
+            for (int a = 0; a < 3; a++) {
+                w.lo[a] = std::min(w.lo[a], b.lo[a]);
+                w.hi[a] = std::max(w.hi[a], b.hi[a]);
+            }
+        for (int a = 0; a < 3; a++) {
+            const float pad = 1e-5f * (std::fabs(w.lo[a]) + std::fabs(w.hi[a]) + 1e-3f);
+            w.lo[a] -= pad;
+            w.hi[a] += pad;
+        }
+        out.cull_o = std::max(out.cull_o, 1.0f);
+        out.cull_r = std::max(out.cull_r, (float)fm);
+        out.max_blas_depth = std::max(out.max_blas_depth, fbvh.depth);
+        dinst.push_back(syn);
+        tlas_boxes.push_back(w);
+        tlas_ids.push_back(ni);
     }
     if (emit.size() > kMaxEmitBoxes) {
         // merge into kMaxEmitBoxes boxes: runs of neighbours along the axis
@@ -495,7 +609,7 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
     {
         // the traversal stack holds at most two entries per TLAS level, the
         // instance return marker and one entry per BLAS level
-        int md = 0;
+        int md = out.max_blas_depth;
         for (auto &b : builds)
             md = std::max(md, b.bvh.depth);
         out.tlas_depth = tlas.depth;

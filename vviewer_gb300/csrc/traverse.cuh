@@ -423,13 +423,15 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + t_base + (uint32_t)b);
             const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
             const uint32_t prim = __float_as_uint(p0.w);
+            const uint32_t tag = __float_as_uint(p1.w);
+            const uint32_t hinst = tag ? tag - 1u : inst_id; // baked triangles name their instance
             float t, u, v;
-            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
-                is_after(t, inst_id, prim, after)) {
+            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, hinst, prim, best) &&
+                is_after(t, hinst, prim, after)) {
                 best.t = t;
                 best.u = u;
                 best.v = v;
-                best.inst = inst_id;
+                best.inst = hinst;
                 best.prim = prim;
             }
             continue;
@@ -453,13 +455,15 @@ __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, 
             const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
             const float4 p0 = ldg_scene(tp), p1 = ldg_scene(tp + 1), p2 = ldg_scene(tp + 2);
             const uint32_t prim = __float_as_uint(p0.w);
+            const uint32_t tag = __float_as_uint(p1.w);
+            const uint32_t hinst = tag ? tag - 1u : inst_id; // baked triangles name their instance
             float t, u, v;
-            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
-                is_after(t, inst_id, prim, after)) {
+            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, hinst, prim, best) &&
+                is_after(t, hinst, prim, after)) {
                 best.t = t;
                 best.u = u;
                 best.v = v;
-                best.inst = inst_id;
+                best.inst = hinst;
                 best.prim = prim;
             }
             leaf_first++;
@@ -678,19 +682,22 @@ __device__ __forceinline__ Hit trace_after_group(const SceneView &s, const float
             // up to eight pending triangles, one per lane
             const int cnt = __popc(t_bits);
             float ct = INFINITY, cu = 0.0f, cv = 0.0f;
-            uint32_t cp = kNoHit;
+            uint32_t cp = kNoHit, ci = kNoHit;
             if (g.gl < cnt) {
                 const int b = (int)__fns(t_bits, 0, g.gl + 1);
                 const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + t_base + (uint32_t)b);
                 const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
                 const uint32_t prim = __float_as_uint(p0.w);
+                const uint32_t tag = __float_as_uint(p1.w);
+                const uint32_t hinst = tag ? tag - 1u : inst_id;
                 float t, u, v;
-                if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, inst_id, prim, best) &&
-                    is_after(t, inst_id, prim, after)) {
+                if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, hinst, prim, best) &&
+                    is_after(t, hinst, prim, after)) {
                     ct = t;
                     cu = u;
                     cv = v;
                     cp = prim;
+                    ci = hinst;
                 }
             }
             if (cnt <= 8) {
@@ -699,24 +706,26 @@ __device__ __forceinline__ Hit trace_after_group(const SceneView &s, const float
                 const uint32_t b8 = __fns(t_bits, 0, 8); // the eighth set bit
                 t_bits &= ~((2u << b8) - 1u);
             }
-            // group minimum of (t, primitive)
+            // group minimum of (t, instance, primitive)
             float mt = ct;
-            uint32_t mp = cp;
+            uint32_t mi = ci, mp = cp;
 #pragma unroll
             for (int sh = 1; sh < 8; sh <<= 1) {
                 const float ot = __shfl_xor_sync(g.mask, mt, sh);
+                const uint32_t oi = __shfl_xor_sync(g.mask, mi, sh);
                 const uint32_t op = __shfl_xor_sync(g.mask, mp, sh);
-                if (ot < mt || (ot == mt && op < mp)) {
+                if (ot < mt || (ot == mt && (oi < mi || (oi == mi && op < mp)))) {
                     mt = ot;
+                    mi = oi;
                     mp = op;
                 }
             }
             if (mp != kNoHit) {
-                const uint32_t owner = __ffs(__ballot_sync(g.mask, cp == mp && ct == mt)) - 1;
+                const uint32_t owner = __ffs(__ballot_sync(g.mask, cp == mp && ci == mi && ct == mt)) - 1;
                 best.u = __shfl_sync(g.mask, cu, (int)owner);
                 best.v = __shfl_sync(g.mask, cv, (int)owner);
                 best.t = mt;
-                best.inst = inst_id;
+                best.inst = mi;
                 best.prim = mp;
             }
             continue;
