@@ -865,10 +865,20 @@ V3 samplePBRStandard(V3 &wi, V3 wo, float &pdf, const PBR &p, float u0, float u1
     return F;
 }
 // pt/MIS.glsl:5-10
+// With an overflowing square (a light sample grazing the emitter's own
+// plane) the weight is the limit from the ratio of the pdfs instead of
+// inf / inf, as the library computes it; finite squares are unchanged.
 float PowerHeuristic(float fPdf, float gPdf)
 {
     float f = fPdf, g = gPdf;
-    return (f * f) / (f * f + g * g);
+    const float ff = f * f, gg = g * g;
+    if (std::isinf(ff) || std::isinf(gg)) {
+        if (std::isinf(f) || std::isinf(g))
+            return std::isinf(g) ? (std::isinf(f) ? 0.5f : 0.0f) : 1.0f;
+        const float r = g / f;
+        return 1.0f / (1.0f + r * r);
+    }
+    return ff / (ff + gg);
 }
 // phaseFunctions.glsl:1-31
 float HenyeyGreenstein(float cosTheta, float g)

@@ -266,10 +266,21 @@ __device__ __forceinline__ float3 sample_pbr(float3 &wi, const float3 &wo, float
 }
 
 // ---- MIS: shaders/pt/MIS.glsl:5-10
+// When a square overflows (a light sample grazing the emitter's own plane,
+// whose pdf carries d^2 / cos with cos near zero) the quotient would be
+// inf / inf; the weight is then taken from the ratio of the pdfs, its limit.
+// Finite squares give the reference's formula and rounding unchanged.
 __device__ __forceinline__ float power_heuristic(float fpdf, float gpdf)
 {
     float f = fpdf, g = gpdf;
-    return (f * f) / (f * f + g * g);
+    const float ff = f * f, gg = g * g;
+    if (isinf(ff) || isinf(gg)) {
+        if (isinf(f) || isinf(g))
+            return isinf(g) ? (isinf(f) ? 0.5f : 0.0f) : 1.0f;
+        const float r = g / f;
+        return 1.0f / (1.0f + r * r);
+    }
+    return ff / (ff + gg);
 }
 
 // ---- Phase function: shaders/include/phaseFunctions.glsl:1-31
