@@ -679,13 +679,13 @@ def run_converged(args) -> None:
     def bufs(w, h, m2=False):
         return {k: torch.zeros((h, w, 4), device="cuda") for k in keys + (("radiance_m2",) if m2 else ())}
 
-    def render(g, sd, info, spp, w, h, fp64=False, m2=False):
+    def render(g, sd, info, spp, w, h, fp64=False, m2=False, sampler="rtgems"):
         info.samples = spp
         b = bufs(w, h, m2)
         torch.cuda.synchronize()
         t = time.perf_counter()
         g.render(sd, info, outputs={k: v.data_ptr() for k, v in b.items()}, env_is=True, reduce_fp64=fp64,
-                 want_m2=m2)
+                 want_m2=m2, sampler=sampler)
         torch.cuda.synchronize()
         return b, time.perf_counter() - t
 
@@ -724,7 +724,11 @@ def run_converged(args) -> None:
     e, info = scenes.instanced_sky_scene(1, W, H, 16, 8, 4, sky_w=4096, sky_h=2048)
     g = ctx.upload(e.scene.build())
     sd = e.scene.scene_data(W, H)
-    ref, t_ref = render(g, sd, info, ref_spp, W, H, fp64=True, m2=True)
+    # The judge image takes the low-discrepancy sampler: the same estimator
+    # (same expected image) on sample streams independent of the RTGEMS
+    # streams of the images it judges, whose first batches it would
+    # otherwise share (one seed per batch index).
+    ref, t_ref = render(g, sd, info, ref_spp, W, H, fp64=True, m2=True, sampler="pmj")
     nb = ref_spp // info.batch_size
     x = ref["radiance"][..., :3].double()
     var = (nb * ref["radiance_m2"][..., :3].double() - x * x).clamp(min=0) / (nb - 1)
@@ -798,12 +802,14 @@ def run_converged(args) -> None:
             "config": {"workload": "converged_instanced_sky_960x544", "target_rel_rmse": target,
                        "metric": "sqrt(sum((x - ref)^2) / sum(ref^2)) over RGB",
                        "reference": f"{ref_spp} spp, FP64-accumulated batch sums (VVPT_RENDER_REDUCE_FP64), "
-                                    "environment importance sampled",
+                                    "environment importance sampled, PMJ sampler (streams independent of the "
+                                    "judged RTGEMS images)",
                        "requests": M, "request_spp": pick["spp"],
                        "train": f"{args.train_steps} steps of 4 x 256^2 crops from {args.train_crops} seeds x "
                                 f"{len(in_spps)} input spp (4/8/16, FP16), {ref_spp}-spp FP64 targets"},
             "target_met": served_err <= target, "served_rel_rmse": served_err,
             "reference_rel_noise": ref_noise,
+            "reference_rel_noise_from_fit": float(np.sqrt(b)),
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(np.max(lat))},
             "plain": {"images_per_hour": plain_iph,
