@@ -36,9 +36,10 @@ are called "meshes[i]" and "nodes[i]", unnamed materials "materials[i]", the
 default material "DefaultMaterial". One Mesh is kept per glTF primitive and
 shared by every node that uses it (the reference uploads a copy per node; the
 rendered image is the same). Primitives without normals get flat face normals
-(glTF's rule; assimp leaves them zero). Images are PNG (embedded, data URI or
-file); an image that cannot be decoded (JPEG, for one) leaves its slot
-untextured with a warning, as the reference does when stb_image fails.
+(glTF's rule; assimp leaves them zero). Images are PNG or sequential JPEG
+(embedded, data URI or file); an image that cannot be decoded (a progressive
+JPEG, for one) leaves its slot untextured with a warning, as the reference
+does when stb_image fails.
 """
 from __future__ import annotations
 
@@ -260,13 +261,20 @@ class _GltfFile:
 # ---------------------------------------------------------------- PNG images
 
 def _decode_image(data: bytes, what: str):
-    """(H x W x 4 uint8, channels in the file as stb_image counts them) or
-    None with a warning when the image is not a PNG."""
+    """(H x W x 4 uint8, channels in the file as stb_image counts them) of a
+    PNG or sequential JPEG, or None with a warning when the image cannot be
+    decoded (the slot stays untextured, as when stb_image fails)."""
+    from .jpeg import decode_jpeg
     from .scene_io import decode_png
 
+    if data[:2] == b"\xff\xd8":
+        try:
+            return decode_jpeg(data, what)
+        except ValueError as e:
+            warnings.warn(f"{what}: JPEG not decoded ({e}); the slot stays untextured")
+            return None
     if data[:8] != b"\x89PNG\r\n\x1a\n":
-        kind = "JPEG" if data[:2] == b"\xff\xd8" else "unknown format"
-        warnings.warn(f"{what}: {kind} image not decoded; the slot stays untextured")
+        warnings.warn(f"{what}: unknown image format; the slot stays untextured")
         return None
     return decode_png(data, what)
 
