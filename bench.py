@@ -762,12 +762,20 @@ def run_converged(args) -> None:
         t_d = time.perf_counter() - t0
         err = _rel_rmse(den, ref["radiance"])
         spp_eq = plain_spp_for(err)
+        finite = spp_eq != float("inf")
         sweep.append({"spp": spp, "rel_rmse_noisy": _rel_rmse(img["radiance"], ref["radiance"]),
                       "rel_rmse_denoised": err, "render_s": t_r, "denoise_s": t_d,
-                      "plain_spp_same_error": spp_eq if spp_eq != float("inf") else None})
+                      "plain_spp_same_error": spp_eq if finite else None,
+                      # the plain tracer's time for the same error over this render + denoise
+                      "gain_at_equal_error": (W * H * spp_eq / paths_per_s) / (t_r + t_d) if finite else None})
+    # operating point: the fewest spp that meet the target; when none does, the
+    # input spp where the denoiser gains most over the plain tracer at equal error
     met = [r for r in sweep if r["rel_rmse_denoised"] <= target]
-    pick = met[0] if met else min(sweep, key=lambda r: r["rel_rmse_denoised"])
-    err_pick = pick["rel_rmse_denoised"]
+    if met:
+        pick, pick_rule = met[0], "fewest spp meeting the target"
+    else:
+        pick = max(sweep, key=lambda r: r["gain_at_equal_error"] or 0.0)
+        pick_rule = "target not met at any spp: largest gain at equal error"
 
     # batched + served + denoised: M requests together through the job engine
     M = args.requests_converged
@@ -804,7 +812,7 @@ def run_converged(args) -> None:
                        "reference": f"{ref_spp} spp, FP64-accumulated batch sums (VVPT_RENDER_REDUCE_FP64), "
                                     "environment importance sampled, PMJ sampler (streams independent of the "
                                     "judged RTGEMS images)",
-                       "requests": M, "request_spp": pick["spp"],
+                       "requests": M, "request_spp": pick["spp"], "request_spp_rule": pick_rule,
                        "train": f"{args.train_steps} steps of 4 x 256^2 crops from {args.train_crops} seeds x "
                                 f"{len(in_spps)} input spp (4/8/16, FP16), {ref_spp}-spp FP64 targets"},
             "target_met": served_err <= target, "served_rel_rmse": served_err,
