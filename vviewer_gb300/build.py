@@ -46,8 +46,8 @@ def _newest_input() -> float:
     return max(f.stat().st_mtime for f in files if f.is_file())
 
 
-def _compile(src: Path, nvcc: str, extra: list[str], defines: list[str]) -> Path:
-    obj = BUILD_DIR / (src.stem + src.suffix.replace(".", "_") + ".o")
+def _compile(src: Path, nvcc: str, extra: list[str], defines: list[str], build_dir: Path = BUILD_DIR) -> Path:
+    obj = build_dir / (src.stem + src.suffix.replace(".", "_") + ".o")
     dflags = [f"-D{d}" for d in defines]
     if src.suffix == ".cu":
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *dflags, *extra, "-c", str(src), "-o", str(obj)]
@@ -61,27 +61,31 @@ def _compile(src: Path, nvcc: str, extra: list[str], defines: list[str]) -> Path
 
 
 def build(force: bool = False, verbose: bool = False, extra_nvcc: list[str] | None = None,
-          defines: list[str] | None = None) -> Path:
+          defines: list[str] | None = None, out: Path | None = None, build_dir: Path | None = None) -> Path:
     """Compiles and links libvvpt.so if it is missing or stale; returns its path.
-    `defines` (NAME=VALUE) reach both compilers, e.g. VVPT_BLAS_WIDE=0 for the
-    binary BLAS layout; `extra_nvcc` only nvcc."""
-    if LIB.exists() and not force and LIB.stat().st_mtime >= _newest_input():
-        return LIB
+    `defines` (NAME=VALUE) reach both compilers, e.g. VVPT_BLAS_WIDE=1 for the
+    compressed 8-wide BLAS layout; `extra_nvcc` only nvcc. `out` and
+    `build_dir` put a variant build beside the default one (the library path
+    and the object folder)."""
+    lib = Path(out) if out else LIB
+    objdir = Path(build_dir) if build_dir else BUILD_DIR
+    if lib.exists() and not force and lib.stat().st_mtime >= _newest_input():
+        return lib
     nvcc = _nvcc()
-    OUT_DIR.mkdir(exist_ok=True)
-    BUILD_DIR.mkdir(exist_ok=True)
+    lib.parent.mkdir(parents=True, exist_ok=True)
+    objdir.mkdir(parents=True, exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, extra_nvcc or [], defines or []), srcs))
-    tmp = LIB.with_suffix(".so.tmp")
+        objs = list(ex.map(lambda s: _compile(s, nvcc, extra_nvcc or [], defines or [], objdir), srcs))
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":

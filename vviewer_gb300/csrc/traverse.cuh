@@ -376,190 +376,229 @@ __device__ __forceinline__ BVHNode load_node_cached(int idx)
 // push a return marker; pop the marker: back to the world-space ray). Keeping
 // the two levels in one loop keeps a warp's lanes in step: a lane inside an
 // instance never holds lanes that are still in the TLAS, as nested per-level
-// loops would. `err` receives status bits.
+// loops would. The loop's state lives in a TraceState and one step is
+// trace_step, so that a kernel can also run the steps of several rays on one
+// lane, one after the other (trace_after is the one-ray loop). `err` receives
+// status bits.
 constexpr int kTagNode = 0, kTagLeaf = 1, kTagInst = 2, kTagReturn = 3, kTagWide = 4;
 
-__device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
-                                           const Hit &after, uint32_t &err)
-{
+struct TraceState {
+    float3 o, d;        // world-space ray
+    float3 winvd;       // its inverse direction
+    float tmin, slack, box_tmin;
+    // current level: the TLAS (world ray) or one instance's BLAS (object
+    // ray); wr.org is the level's origin (the watertight constants are only
+    // read in a BLAS)
+    WatertightRay wr;
+    float3 cinvd;
     Hit best;
-    best.t = tmax;
-    best.u = best.v = 0.0f;
-    best.inst = kNoHit;
-    best.prim = kNoHit;
-    const float slack = cull_slack(s, o, d);
-    const float box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t), slack);
-    const float3 winvd = safe_inv(d);
-    // current level: the TLAS (world ray) or one instance's BLAS (object ray)
-    float3 co = o, cinvd = winvd;
-    WatertightRay wr = wt_setup(o, d);
-    uint32_t inst_id = kNoHit;
-    uint32_t node_base = s.tlas_root, tri_base = 0;
-    bool in_blas = false;
-    int node = 0;                 // inner node to visit (local index), -1 none
-    int leaf_first = 0, leaf_count = 0; // triangles still to test (local indices)
+    uint32_t inst_id, node_base, tri_base;
+    bool in_blas;
+    int node;                    // inner node to visit (local index), -1 none
+    int leaf_first, leaf_count;  // triangles still to test (local indices)
+    int cached;                  // TLAS nodes below this index come from shared memory
 #if VVPT_BLAS_WIDE
     // BLAS level: the group of wide children still to visit (hits at bit
     // slot ^ oct, imask, first child) and the triangles still to test (mask
     // over t_base + 0..31); oct = sign bits of the object-space direction
-    uint32_t w_base = 0, w_bits = 0, w_imask = 0, t_base = 0, t_bits = 0, oct = 0;
+    uint32_t w_base, w_bits, w_imask, t_base, t_bits, oct;
 #endif
-    int2 stack[kTraversalStack];
-    int sp = 0;
-    // TLAS nodes below this index come from shared memory when the cache
-    // holds this scene's TLAS
-    const int cached = vvpt_tlas_cache_src == s.nodes + s.tlas_root ? vvpt_tlas_cache_count : 0;
-    auto push = [&](int value, int tag, int count) {
-        if (sp < kTraversalStack)
-            stack[sp++] = make_int2(value, (tag << 28) | count);
-        else
-            err |= kErrStackOverflow;
-    };
-    for (;;) {
+    int sp;                      // entries on the traversal stack
+};
+// The traversal stack, kept apart from the scalar state so that the scalars
+// stay in registers.
+typedef int2 TraceStack[kTraversalStack];
+
+__device__ __forceinline__ void trace_begin(TraceState &st, const SceneView &s, const float3 &o, const float3 &d,
+                                            float tmin, float tmax, const Hit &after)
+{
+    st.o = o;
+    st.d = d;
+    st.tmin = tmin;
+    st.best.t = tmax;
+    st.best.u = st.best.v = 0.0f;
+    st.best.inst = kNoHit;
+    st.best.prim = kNoHit;
+    st.slack = cull_slack(s, o, d);
+    st.box_tmin = cull_near(after.inst == kNoHit ? tmin : fmaxf(tmin, after.t), st.slack);
+    st.winvd = safe_inv(d);
+    st.cinvd = st.winvd;
+    st.wr = wt_setup(o, d);
+    st.inst_id = kNoHit;
+    st.node_base = s.tlas_root;
+    st.tri_base = 0;
+    st.in_blas = false;
+    st.node = 0;
+    st.leaf_first = st.leaf_count = 0;
+    st.cached = vvpt_tlas_cache_src == s.nodes + s.tlas_root ? vvpt_tlas_cache_count : 0;
 #if VVPT_BLAS_WIDE
-        if (t_bits) {
-            const int b = __ffs((int)t_bits) - 1;
-            t_bits &= t_bits - 1u;
-            const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + t_base + (uint32_t)b);
-            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-            const uint32_t prim = __float_as_uint(p0.w);
-            const uint32_t tag = __float_as_uint(p1.w);
-            const uint32_t hinst = tag ? tag - 1u : inst_id; // baked triangles name their instance
-            float t, u, v;
-            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, hinst, prim, best) &&
-                is_after(t, hinst, prim, after)) {
-                best.t = t;
-                best.u = u;
-                best.v = v;
-                best.inst = hinst;
-                best.prim = prim;
-            }
-            continue;
-        }
-        if (w_bits) {
-            // nearest remaining child of the group (octant order)
-            const int b = __ffs((int)w_bits) - 1;
-            w_bits &= w_bits - 1u;
-            const uint32_t slot = (uint32_t)b ^ oct;
-            const uint32_t child = w_base + (uint32_t)__popc(w_imask & ((1u << slot) - 1u));
-            if (w_bits)
-                push((int)w_base, kTagWide, (int)((w_bits << 8) | w_imask));
-            float4 wn[5];
-            load_wide(s.wnodes, node_base + child, wn);
-            wide_visit(wn, co, cinvd, oct, box_tmin, cull_far(best.t, slack), w_bits, w_imask, w_base, t_base, t_bits);
-            continue;
-        }
+    st.w_base = st.w_bits = st.w_imask = st.t_base = st.t_bits = st.oct = 0;
 #endif
-        if (leaf_count > 0) {
-            VVPT_TRAVERSAL_STAT(1);
-            const float4 *tp = reinterpret_cast<const float4 *>(s.tris + tri_base + leaf_first);
-            const float4 p0 = ldg_scene(tp), p1 = ldg_scene(tp + 1), p2 = ldg_scene(tp + 2);
-            const uint32_t prim = __float_as_uint(p0.w);
-            const uint32_t tag = __float_as_uint(p1.w);
-            const uint32_t hinst = tag ? tag - 1u : inst_id; // baked triangles name their instance
-            float t, u, v;
-            if (wt_intersect(wr, p0, p1, p2, tmin, best.t, t, u, v) && better(t, hinst, prim, best) &&
-                is_after(t, hinst, prim, after)) {
-                best.t = t;
-                best.u = u;
-                best.v = v;
-                best.inst = hinst;
-                best.prim = prim;
-            }
-            leaf_first++;
-            leaf_count--;
-            continue;
-        }
-        if (node >= 0) {
-            VVPT_TRAVERSAL_STAT(in_blas ? 0 : 3);
-            const BVHNode n = (!in_blas && node < cached) ? load_node_cached(node)
-                                                          : load_node(s.nodes, (int)node_base + node);
-            float tl, tr;
-            const float far_t = cull_far(best.t, slack);
-            box2(n, co, cinvd, box_tmin, far_t, tl, tr);
-            const bool hl = tl <= far_t && n.c.x >= 0;
-            const bool hr = tr <= far_t && n.c.y >= 0;
-            // near child first
-            const bool swap = hl && hr && tr < tl;
-            int next = -1;
-#pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const bool right = (k == 0) == swap;
-                const bool h = right ? hr : hl;
-                if (!h)
-                    continue;
-                const int idx = right ? n.c.y : n.c.x;
-                const int cnt = right ? n.c.w : n.c.z;
-                if (cnt == 0) {
-                    if (next < 0)
-                        next = idx;
-                    else
-                        push(idx, kTagNode, 0);
-                } else if (in_blas) {
-                    if (leaf_count == 0) {
-                        leaf_first = idx;
-                        leaf_count = cnt;
-                    } else {
-                        push(idx, kTagLeaf, cnt);
-                    }
-                } else {
-                    push(idx, kTagInst, cnt);
-                }
-            }
-            node = next;
-            continue;
-        }
-        if (sp == 0)
-            break;
-        const int2 e = stack[--sp];
-        const int tag = (int)((unsigned)e.y >> 28);
-        const int cnt = e.y & 0x0FFFFFFF;
-        if (tag == kTagNode) {
-            node = e.x;
-#if VVPT_BLAS_WIDE
-        } else if (tag == kTagWide) {
-            w_base = (uint32_t)e.x;
-            w_bits = ((uint32_t)cnt >> 8) & 0xffu;
-            w_imask = (uint32_t)cnt & 0xffu;
-#endif
-        } else if (tag == kTagLeaf) {
-            leaf_first = e.x;
-            leaf_count = cnt;
-        } else if (tag == kTagInst) {
-            VVPT_TRAVERSAL_STAT(2);
-            if (cnt > 1)
-                push(e.x + 1, kTagInst, cnt - 1);
-            inst_id = __ldg(s.tlas_order + e.x);
-            const DevInstance &inst = s.instances[inst_id];
-            const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
-            co = wt_xform_point(rows, o);
-            const float3 cd = wt_xform_vector(rows, d);
-            cinvd = safe_inv(cd);
-            wr = wt_setup(co, cd);
-            node_base = inst.node_offset;
-            tri_base = inst.tri_offset;
-            in_blas = true;
-            push(0, kTagReturn, 0);
-#if VVPT_BLAS_WIDE
-            // the BLAS root as a one-child group
-            oct = (__float_as_uint(cd.x) >> 31) | ((__float_as_uint(cd.y) >> 31) << 1) |
-                  ((__float_as_uint(cd.z) >> 31) << 2);
-            w_base = 0;
-            w_imask = 1u;
-            w_bits = 1u << oct;
-#else
-            node = 0;
-#endif
-        } else {
-            // back to the TLAS
-            co = o;
-            cinvd = winvd;
-            node_base = s.tlas_root;
-            in_blas = false;
-            inst_id = kNoHit;
-        }
+    st.sp = 0;
+}
+
+__device__ __forceinline__ void trace_push(TraceState &st, TraceStack &stack, int value, int tag, int count,
+                                           uint32_t &err)
+{
+    if (st.sp < kTraversalStack)
+        stack[st.sp++] = make_int2(value, (tag << 28) | count);
+    else
+        err |= kErrStackOverflow;
+}
+
+// Tests one triangle of the current BLAS against the ray and keeps it when it
+// is the best candidate after `after`.
+__device__ __forceinline__ void trace_triangle(TraceState &st, const SceneView &s, uint32_t local, const Hit &after)
+{
+    const float4 *tp = reinterpret_cast<const float4 *>(s.tris + st.tri_base + local);
+    const float4 p0 = ldg_scene(tp), p1 = ldg_scene(tp + 1), p2 = ldg_scene(tp + 2);
+    const uint32_t prim = __float_as_uint(p0.w);
+    const uint32_t tag = __float_as_uint(p1.w);
+    const uint32_t hinst = tag ? tag - 1u : st.inst_id; // baked triangles name their instance
+    float t, u, v;
+    if (wt_intersect(st.wr, p0, p1, p2, st.tmin, st.best.t, t, u, v) && better(t, hinst, prim, st.best) &&
+        is_after(t, hinst, prim, after)) {
+        st.best.t = t;
+        st.best.u = u;
+        st.best.v = v;
+        st.best.inst = hinst;
+        st.best.prim = prim;
     }
-    return best;
+}
+
+// One loop step; false when the traversal is over (st.best holds the result).
+__device__ __forceinline__ bool trace_step(TraceState &st, TraceStack &stack, const SceneView &s, const Hit &after,
+                                           uint32_t &err)
+{
+#if VVPT_BLAS_WIDE
+    if (st.t_bits) {
+        const int b = __ffs((int)st.t_bits) - 1;
+        st.t_bits &= st.t_bits - 1u;
+        trace_triangle(st, s, st.t_base + (uint32_t)b, after);
+        return true;
+    }
+    if (st.w_bits) {
+        // nearest remaining child of the group (octant order)
+        const int b = __ffs((int)st.w_bits) - 1;
+        st.w_bits &= st.w_bits - 1u;
+        const uint32_t slot = (uint32_t)b ^ st.oct;
+        const uint32_t child = st.w_base + (uint32_t)__popc(st.w_imask & ((1u << slot) - 1u));
+        if (st.w_bits)
+            trace_push(st, stack, (int)st.w_base, kTagWide, (int)((st.w_bits << 8) | st.w_imask), err);
+        float4 wn[5];
+        load_wide(s.wnodes, st.node_base + child, wn);
+        wide_visit(wn, st.wr.org, st.cinvd, st.oct, st.box_tmin, cull_far(st.best.t, st.slack), st.w_bits,
+                   st.w_imask, st.w_base, st.t_base, st.t_bits);
+        return true;
+    }
+#endif
+    if (st.leaf_count > 0) {
+        VVPT_TRAVERSAL_STAT(1);
+        trace_triangle(st, s, (uint32_t)st.leaf_first, after);
+        st.leaf_first++;
+        st.leaf_count--;
+        return true;
+    }
+    if (st.node >= 0) {
+        VVPT_TRAVERSAL_STAT(st.in_blas ? 0 : 3);
+        const BVHNode n = (!st.in_blas && st.node < st.cached) ? load_node_cached(st.node)
+                                                                : load_node(s.nodes, (int)st.node_base + st.node);
+        float tl, tr;
+        const float far_t = cull_far(st.best.t, st.slack);
+        box2(n, st.wr.org, st.cinvd, st.box_tmin, far_t, tl, tr);
+        const bool hl = tl <= far_t && n.c.x >= 0;
+        const bool hr = tr <= far_t && n.c.y >= 0;
+        // near child first
+        const bool swap = hl && hr && tr < tl;
+        int next = -1;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const bool right = (k == 0) == swap;
+            const bool h = right ? hr : hl;
+            if (!h)
+                continue;
+            const int idx = right ? n.c.y : n.c.x;
+            const int cnt = right ? n.c.w : n.c.z;
+            if (cnt == 0) {
+                if (next < 0)
+                    next = idx;
+                else
+                    trace_push(st, stack, idx, kTagNode, 0, err);
+            } else if (st.in_blas) {
+                if (st.leaf_count == 0) {
+                    st.leaf_first = idx;
+                    st.leaf_count = cnt;
+                } else {
+                    trace_push(st, stack, idx, kTagLeaf, cnt, err);
+                }
+            } else {
+                trace_push(st, stack, idx, kTagInst, cnt, err);
+            }
+        }
+        st.node = next;
+        return true;
+    }
+    if (st.sp == 0)
+        return false;
+    const int2 e = stack[--st.sp];
+    const int tag = (int)((unsigned)e.y >> 28);
+    const int cnt = e.y & 0x0FFFFFFF;
+    if (tag == kTagNode) {
+        st.node = e.x;
+#if VVPT_BLAS_WIDE
+    } else if (tag == kTagWide) {
+        st.w_base = (uint32_t)e.x;
+        st.w_bits = ((uint32_t)cnt >> 8) & 0xffu;
+        st.w_imask = (uint32_t)cnt & 0xffu;
+#endif
+    } else if (tag == kTagLeaf) {
+        st.leaf_first = e.x;
+        st.leaf_count = cnt;
+    } else if (tag == kTagInst) {
+        VVPT_TRAVERSAL_STAT(2);
+        if (cnt > 1)
+            trace_push(st, stack, e.x + 1, kTagInst, cnt - 1, err);
+        st.inst_id = __ldg(s.tlas_order + e.x);
+        const DevInstance &inst = s.instances[st.inst_id];
+        const float4 rows[3] = {inst.w2o[0], inst.w2o[1], inst.w2o[2]};
+        const float3 co = wt_xform_point(rows, st.o);
+        const float3 cd = wt_xform_vector(rows, st.d);
+        st.cinvd = safe_inv(cd);
+        st.wr = wt_setup(co, cd);
+        st.node_base = inst.node_offset;
+        st.tri_base = inst.tri_offset;
+        st.in_blas = true;
+        trace_push(st, stack, 0, kTagReturn, 0, err);
+#if VVPT_BLAS_WIDE
+        // the BLAS root as a one-child group
+        st.oct = (__float_as_uint(cd.x) >> 31) | ((__float_as_uint(cd.y) >> 31) << 1) |
+                 ((__float_as_uint(cd.z) >> 31) << 2);
+        st.w_base = 0;
+        st.w_imask = 1u;
+        st.w_bits = 1u << st.oct;
+#else
+        st.node = 0;
+#endif
+    } else {
+        // back to the TLAS
+        st.wr.org = st.o;
+        st.cinvd = st.winvd;
+        st.node_base = s.tlas_root;
+        st.in_blas = false;
+        st.inst_id = kNoHit;
+    }
+    return true;
+}
+
+__device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
+                                           const Hit &after, uint32_t &err)
+{
+    TraceState st;
+    TraceStack stack;
+    trace_begin(st, s, o, d, tmin, tmax, after);
+    while (trace_step(st, stack, s, after, err)) {
+    }
+    return st.best;
 }
 
 #if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL && defined(__CUDACC__)

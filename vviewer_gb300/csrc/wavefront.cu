@@ -450,6 +450,7 @@ __global__ void k_begin(Queues q, int pp)
         q.counters[C_WALK] = 0u;
         q.counters[C_CONN] = 0u;
         q.counters[C_NEEQ] = 0u;
+        q.counters[C_FETCH_EXT] = 0u;
         q.counters[C_EXT0 + (1 - pp)] = 0u;
         q.counters[C_REGEN0 + (1 - pp)] = 0u;
     }
@@ -631,11 +632,94 @@ __device__ __forceinline__ void group_sync()
 #endif
 }
 
+// Shade bin of a closest hit (0 Lambert, 1 PBR, 2 miss; | 4: the fused
+// emitter ray takes the full candidate walk).
+__device__ __forceinline__ uint32_t extend_key(const SceneView &s, const Hit &h, bool fused, uint32_t key)
+{
+    if (h.inst == kNoHit)
+        return key | 2u;
+    const DevMaterial &m = s.materials[s.instances[h.inst].material];
+    key |= (uint32_t)m.uv_tiling.z == 2u ? 0u : 1u;
+    // a transparent first candidate also needs the walk
+    if (fused && h.t <= kExtTmax && m.mrao.w >= 0.99f)
+        key |= 4u;
+    return key;
+}
+
+// Lane refill: a warp traces its rays step by step (trace_step), and when
+// no more than VVPT_REFILL_BELOW of its lanes still hold a ray, the idle
+// lanes take the next rays of the queue (one atomic per warp). Rays of very
+// different lengths then share a warp's steps instead of the warp running
+// until its longest ray ends. Binary BLAS only.
+#ifndef VVPT_EXTEND_REFILL
+#define VVPT_EXTEND_REFILL (!VVPT_BLAS_WIDE)
+#endif
+#ifndef VVPT_REFILL_BELOW
+#define VVPT_REFILL_BELOW 16
+#endif
+
 __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable jt, PathState ps, Queues q, int pp)
 {
     const uint32_t n = q.counters[C_EXT0 + pp];
     const uint32_t *queue = q.ext[pp];
     uint32_t err = 0;
+#if VVPT_EXTEND_REFILL
+    if (n > 0)
+        tlas_cache_fill(jt.jobs[ps.job[queue[min(first_ray(), n - 1u)]]].scene);
+    else
+        tlas_cache_none();
+    const uint32_t lane = threadIdx.x & 31u;
+    TraceState st;
+    TraceStack stack;
+    const SceneView *sv = nullptr;
+    uint32_t i = 0, slot = 0, key = 0;
+    bool active = false, fused = false;
+    bool open = true; // warp-uniform: the queue may still hold rays
+    for (;;) {
+        uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+        if (open && __popc(act) <= VVPT_REFILL_BELOW) {
+            const uint32_t want = ~act;
+            const uint32_t cnt = (uint32_t)__popc(want);
+            uint32_t base = 0;
+            if (lane == 0)
+                base = atomicAdd(&q.counters[C_FETCH_EXT], cnt);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            open = base + cnt < n;
+            if (!active) {
+                const uint32_t idx = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
+                if (idx < n) {
+                    i = idx;
+                    slot = queue[i];
+                    sv = &jt.jobs[ps.job[slot]].scene;
+                    // with an emitter ray riding on this ray, start at its tmin
+                    fused = (ps.flags[slot] & F_NEE_FUSED) != 0;
+                    key = 0;
+                    trace_begin(st, *sv, f3(ps.o[slot]), f3(ps.d[slot]), fused ? kConnTmin : kExtTmin, kExtTmax,
+                                no_hit());
+                    active = true;
+                }
+            }
+            act = __ballot_sync(0xFFFFFFFFu, active);
+        }
+        if (act == 0)
+            break;
+        if (active && !trace_step(st, stack, *sv, no_hit(), err)) {
+            const Hit &h = st.best;
+            if (fused && key == 0 && h.inst != kNoHit && h.t < kExtTmin) {
+                // the emitter ray's first candidate lies below the extension
+                // ray's tmin: the emitter ray takes the full candidate walk,
+                // and this lane goes on with the extension ray from its tmin
+                key = 4;
+                trace_begin(st, *sv, st.o, st.d, kExtTmin, kExtTmax, no_hit());
+            } else {
+                ps.hit[slot] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+                ps.hit_inst[slot] = h.inst;
+                q.ext_key[i] = extend_key(*sv, h, fused, key);
+                active = false;
+            }
+        }
+    }
+#else
     if (first_ray() < n)
         tlas_cache_fill(jt.jobs[ps.job[queue[first_ray()]]].scene);
     else
@@ -672,15 +756,7 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
             h = trace_closest(s, o, d, kExtTmin, kExtTmax, err);
 #endif
         }
-        if (h.inst == kNoHit) {
-            key |= 2;
-        } else {
-            const DevMaterial &m = s.materials[s.instances[h.inst].material];
-            key |= (uint32_t)m.uv_tiling.z == 2u ? 0u : 1u;
-            // a transparent first candidate also needs the walk
-            if (fused && h.t <= kExtTmax && m.mrao.w >= 0.99f)
-                key |= 4;
-        }
+        key = extend_key(s, h, fused, key);
 #if VVPT_BLAS_WIDE && VVPT_GROUP_TRAVERSAL
         if (g.gl == 0)
 #endif
@@ -690,6 +766,7 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
             q.ext_key[i] = key;
         }
     }
+#endif
     if (blockIdx.x == 0 && threadIdx.x == 0)
         atomicAdd(&q.counters[C_SEGMENTS], n);
     if (err)

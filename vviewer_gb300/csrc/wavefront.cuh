@@ -78,7 +78,8 @@ enum CounterIndex {
     C_PATHS = 14,
     C_WALK = 15,
     C_NEEQ = 16,
-    C_COUNT = 17
+    C_FETCH_EXT = 17,    // extension rays handed out so far in this iteration (lane refill)
+    C_COUNT = 18
 };
 
 struct Queues {
