@@ -79,7 +79,8 @@ enum CounterIndex {
     C_WALK = 15,
     C_NEEQ = 16,
     C_FETCH_EXT = 17,    // extension rays handed out so far in this iteration (lane refill)
-    C_COUNT = 18
+    C_FETCH_SHADOW = 18, // shadow and emitter rays handed out so far in this iteration
+    C_COUNT = 19
 };
 
 struct Queues {
