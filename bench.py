@@ -609,15 +609,17 @@ def run_denoise(args) -> None:
     infer_ms = sum(ms) / len(ms)
     flops = denoiser_flops(H, W)
     # training step, 8 x 256^2
-    tb = [torch.rand((8, 256, 256, 4), device="cuda", generator=g) for _ in range(4)]
-    for _ in range(3):
-        dn.train_step(*tb, lr=1e-4)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(5):
-        dn.train_step(*tb, lr=1e-4)
-    torch.cuda.synchronize()
-    train_ms = (time.perf_counter() - t0) / 5 * 1e3
+    train_ms = None
+    if not args.no_train:
+        tb = [torch.rand((8, 256, 256, 4), device="cuda", generator=g) for _ in range(4)]
+        for _ in range(3):
+            dn.train_step(*tb, lr=1e-4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            dn.train_step(*tb, lr=1e-4)
+        torch.cuda.synchronize()
+        train_ms = (time.perf_counter() - t0) / 5 * 1e3
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
     hbm = float(peaks.get("hbm_gbs", 6800.0))
@@ -635,7 +637,8 @@ def run_denoise(args) -> None:
                          "frac": achieved / peak, "traffic": None, "flops_per_frame": flops},
             "layer_roofline": {"bound_ms": bound_ms, "frac_of_bound": bound_ms / infer_ms,
                                "hbm_gbs": hbm, "tensor_tflops": peak, "layers": layers},
-            "train_step_ms": train_ms, "train_tflops": 3 * denoiser_flops(256, 256, 8) / (train_ms / 1e3) / 1e12}
+            "train_step_ms": train_ms,
+            "train_tflops": 3 * denoiser_flops(256, 256, 8) / (train_ms / 1e3) / 1e12 if train_ms else None}
     dn.close()
     ctx.close()
     print(json.dumps(line), flush=True)
@@ -851,6 +854,7 @@ def main():
     ap.add_argument("--train-crops", type=int, default=16, help="converged: training scenes (512^2 crops)")
     ap.add_argument("--requests-converged", type=int, default=16, help="converged: requests served together")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-train", action="store_true", help="denoise: inference only (no training steps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (no vvpt_autotune pass)")
     ap.add_argument("--tuning", default="", help="SLOTS,BLOCKS_PER_SM: a fixed tuning instead of the autotune pass")
     ap.add_argument("--width", type=int, default=0)

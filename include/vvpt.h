@@ -422,11 +422,13 @@ VVPT_API vvpt_status vvpt_autotune(vvpt_ctx *ctx,
                                    double budget_ms,
                                    vvpt_tuning *out_tuning);
 
-/* BLAS builder of vvpt_scene_upload: AUTO builds meshes of at least 65,536
+/* BVH builder of vvpt_scene_upload: AUTO builds meshes of at least 65,536
  * triangles on the GPU (binned SAH, one tree level per round of kernels) and
- * the rest on the host; HOST builds every BLAS on the host (binned SAH with
- * FP64 costs). Both give the same closest hits. */
-enum { VVPT_BVH_BUILDER_AUTO = 0, VVPT_BVH_BUILDER_HOST = 1 };
+ * the rest, the baked small instances and the TLAS on the host; HOST builds
+ * every tree on the host (binned SAH with FP64 costs); GPU builds every BLAS,
+ * the baked small instances' BLAS and the TLAS on the GPU (trees of at most
+ * one leaf stay on the host). All give the same closest hits. */
+enum { VVPT_BVH_BUILDER_AUTO = 0, VVPT_BVH_BUILDER_HOST = 1, VVPT_BVH_BUILDER_GPU = 2 };
 VVPT_API vvpt_status vvpt_set_bvh_builder(vvpt_ctx *ctx, int builder);
 
 /* ---- Jobs: batched and served renders ------------------------------------

@@ -25,7 +25,7 @@ from vviewer_gb300.renderer import RenderInfo
 from vviewer_gb300.scene import EnvironmentType, Engine, MaterialLambert, Transform
 
 pytestmark = pytest.mark.gpu
-N_BVH_AUTO, N_BVH_HOST = 0, 1
+N_BVH_AUTO, N_BVH_HOST, N_BVH_GPU = 0, 1, 2
 
 
 def assert_hits_equal(hg, ho):
@@ -542,17 +542,47 @@ def test_progress_reaches_one(ctx):
 
 def test_gpu_bvh_builder_gives_the_same_hits(ctx):
     """Meshes of 65,536 triangles or more are built on the GPU by default;
-    the host builder (VVPT_BVH_BUILDER_HOST) must give identical closest hits
-    (both are exact), and both must match the oracle."""
+    the host builder (VVPT_BVH_BUILDER_HOST) and the all-GPU builder
+    (VVPT_BVH_BUILDER_GPU: every BLAS, the baked small instances and the
+    TLAS) must give identical closest hits (all are exact), and they must
+    match the oracle."""
     e, _ = scenes.cornell_medium(4, 64, 64, 4, 8, 4, freq=60, spheres=2)  # 2 x 72,000 triangles
     fs = e.scene.build()
     rays = np.concatenate([make_rays(fs, 100_000, 17, -0.2, 1.2), make_near_rays(fs, 20_000, 18)])
     hits = {}
-    for builder in (N_BVH_AUTO, N_BVH_HOST):
-        ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, builder))
-        g = ctx.upload(fs)
-        hits[builder] = g.trace_closest(rays)
-        g.release()
-    ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, N_BVH_AUTO))
+    try:
+        for builder in (N_BVH_AUTO, N_BVH_HOST, N_BVH_GPU):
+            ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, builder))
+            g = ctx.upload(fs)
+            hits[builder] = g.trace_closest(rays)
+            g.release()
+    finally:
+        ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, N_BVH_AUTO))
     assert_hits_equal(hits[N_BVH_AUTO], hits[N_BVH_HOST])
+    assert_hits_equal(hits[N_BVH_GPU], hits[N_BVH_HOST])
     assert_hits_equal(hits[N_BVH_AUTO], oracle.trace_closest(fs, rays))
+    assert ctx.lib.vvpt_set_bvh_builder(ctx.handle, 3) == 1  # VVPT_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("name", ["cornell", "volume_cube", "shared_components"])
+def test_all_gpu_builder_hits_and_renders(ctx, name):
+    """Every tree built on the GPU, including the TLAS over many instances
+    and the baked BLAS of the small instances: closest hits equal to the
+    oracle's, and a render equal bit for bit to the default builder's."""
+    build, (lo, hi) = HIT_SCENES[name]
+    e = build()
+    fs = e.scene.build()
+    rays = np.concatenate([make_rays(fs, 60_000, 23, lo, hi), make_near_rays(fs, 20_000, 24)])
+    info = RenderInfo(samples=8, depth=6, batch_size=4, width=24, height=16, write_files=False)
+    sd = e.scene.scene_data(info.width, info.height)
+    out = {}
+    try:
+        for builder in (N_BVH_AUTO, N_BVH_GPU):
+            ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, builder))
+            g = ctx.upload(fs)
+            out[builder] = (g.trace_closest(rays), g.render(sd, info))
+            g.release()
+    finally:
+        ctx.check(ctx.lib.vvpt_set_bvh_builder(ctx.handle, N_BVH_AUTO))
+    assert_hits_equal(out[N_BVH_GPU][0], oracle.trace_closest(fs, rays))
+    assert np.array_equal(out[N_BVH_GPU][1].radiance, out[N_BVH_AUTO][1].radiance)

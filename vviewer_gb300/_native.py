@@ -22,6 +22,8 @@ STATUS_NAMES = {
     8: "VVPT_ERR_UNSUPPORTED",
 }
 
+BVH_BUILDER_AUTO, BVH_BUILDER_HOST, BVH_BUILDER_GPU = 0, 1, 2
+
 MATERIAL_PBR_STANDARD = 0
 MATERIAL_LAMBERT = 2
 MATERIAL_VOLUME = 3

@@ -285,7 +285,8 @@ VVPT_API vvpt_status vvpt_set_tuning(vvpt_ctx *ctx, const vvpt_tuning *t)
 
 VVPT_API vvpt_status vvpt_set_bvh_builder(vvpt_ctx *ctx, int builder)
 {
-    if (!ctx || (builder != VVPT_BVH_BUILDER_AUTO && builder != VVPT_BVH_BUILDER_HOST))
+    if (!ctx || (builder != VVPT_BVH_BUILDER_AUTO && builder != VVPT_BVH_BUILDER_HOST &&
+                 builder != VVPT_BVH_BUILDER_GPU))
         return VVPT_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->bvh_builder = builder;
@@ -311,12 +312,13 @@ VVPT_API vvpt_status vvpt_scene_upload(vvpt_ctx *ctx, const vvpt_scene_desc *des
     PackedScene pk;
     std::string err;
     BlasBuilder gpu_builder;
-    if (ctx->bvh_builder == VVPT_BVH_BUILDER_AUTO) {
+    if (ctx->bvh_builder != VVPT_BVH_BUILDER_HOST) {
         cudaStream_t bs = vv_stream(ctx);
         gpu_builder = [bs](const std::vector<Box3> &boxes, const BVHBuildOptions &opt, BVHBuildResult &res,
                            std::string &e) { return build_bvh2_gpu(boxes, opt, bs, res, e); };
     }
-    vvpt_status st = pack_scene(desc, pk, err, 0, gpu_builder);
+    const bool all_gpu = ctx->bvh_builder == VVPT_BVH_BUILDER_GPU;
+    vvpt_status st = pack_scene(desc, pk, err, 0, gpu_builder, all_gpu ? 1u : 65536u, all_gpu);
     if (st != VVPT_OK)
         return fail(ctx, st, err);
     auto scene = new vvpt_scene();

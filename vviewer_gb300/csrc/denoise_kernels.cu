@@ -1625,7 +1625,12 @@ bool launch_strip(const ConvArgs &a, cudaStream_t s, uint32_t *err, ConvKernels 
 {
     StripPlan pl;
     CUtensorMap tmap;
-    if (!err || kind == kConvTiles || !plan_strip(a, pl) || (a.cc && pl.per_sm < 2 && !VVPT_STRIP_FUSED_ONE_CTA) || !encode_input_map(a, tmap))
+    // A fused layer (upsample + concat in the kernel) needs two CTAs per SM
+    // to pay: at one (the half-resolution decoder input, whose weights leave
+    // room for one) it took 581 us against 450 us for the separate
+    // upsample-concat and convolution at 3840 x 2160.
+    if (!err || kind == kConvTiles || !plan_strip(a, pl) || (a.cc && pl.per_sm < 2 && !VVPT_STRIP_FUSED_ONE_CTA) ||
+        !encode_input_map(a, tmap))
         return false;
     if (kind == kConvPersistent)
         pl.grid = std::min(pl.grid, 16);

@@ -128,8 +128,24 @@ float build_env_distribution(const float *rgba, uint32_t w, uint32_t h, std::vec
 }
 
 vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads,
-                       const BlasBuilder &large_builder, uint32_t large_min)
+                       const BlasBuilder &large_builder, uint32_t large_min, bool builder_for_all)
 {
+    // a tree for the TLAS or the baked small instances: on the given builder
+    // when it takes every tree, else (or when it declines) on the host
+    auto build_other = [&](const std::vector<Box3> &boxes, const BVHBuildOptions &opt,
+                           BVHBuildResult &res) -> bool {
+        if (builder_for_all && large_builder) {
+            std::string e;
+            if (large_builder(boxes, opt, res, e))
+                return true;
+            if (!e.empty()) {
+                err = e;
+                return false;
+            }
+        }
+        res = build_bvh2(boxes, opt);
+        return true;
+    };
     out = PackedScene();
     // ---- validation (indices the shaders would dereference)
     if ((desc->num_meshes && !desc->meshes) || (desc->num_instances && !desc->instances) ||
@@ -515,7 +531,9 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
                 fb.push_back(b);
             }
         }
-        BVHBuildResult fbvh = build_bvh2(fb, BVHBuildOptions());
+        BVHBuildResult fbvh;
+        if (!build_other(fb, BVHBuildOptions(), fbvh))
+            return VVPT_ERR_DEVICE;
         DevInstance syn;
         std::memset(&syn, 0, sizeof(syn));
         const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -599,7 +617,9 @@ vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::strin
 #endif
     BVHBuildOptions tlas_opt;
     tlas_opt.max_leaf = VVPT_TLAS_MAX_LEAF;
-    BVHBuildResult tlas = build_bvh2(tlas_boxes, tlas_opt);
+    BVHBuildResult tlas;
+    if (!build_other(tlas_boxes, tlas_opt, tlas))
+        return VVPT_ERR_DEVICE;
     out.tlas_root = (uint32_t)nodes.size();
     nodes.insert(nodes.end(), tlas.nodes.begin(), tlas.nodes.end());
     std::vector<uint32_t> &tlas_order = out.tlas_order;

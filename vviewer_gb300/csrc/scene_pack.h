@@ -51,9 +51,11 @@ using BlasBuilder = std::function<bool(const std::vector<Box3> &, const BVHBuild
 
 // Returns VVPT_OK or an error status with `err` set. `threads` = 0 uses every
 // hardware thread for the BLAS builds. Meshes of at least `large_min`
-// triangles go to `large_builder` when one is given (one at a time).
+// triangles go to `large_builder` when one is given (one at a time); with
+// `builder_for_all` the baked small instances' BLAS and the TLAS go to it too.
 vvpt_status pack_scene(const vvpt_scene_desc *desc, PackedScene &out, std::string &err, unsigned threads = 0,
-                       const BlasBuilder &large_builder = BlasBuilder(), uint32_t large_min = 65536);
+                       const BlasBuilder &large_builder = BlasBuilder(), uint32_t large_min = 65536,
+                       bool builder_for_all = false);
 
 // Piecewise-constant sampling tables of an RGBA32F equirect environment
 // (PackedScene::env_dist layout): function = luminance dilated over the 3x3

@@ -274,11 +274,13 @@ struct LightSample {
 // uniform pick (importance sampled by sample_env); `allow_env` = false makes
 // that pick contribute nothing (the last event of a path, whose environment
 // contribution the reference's estimator never adds either).
-// Out of line by default (VVPT_SHADE_OUTLINE): the shading kernel samples a
-// light at a medium scatter point and at a surface, and one copy of this
-// code instead of two shortens that kernel's instruction stream.
+// Out of line with VVPT_SHADE_OUTLINE = 1 (a build option, measured, not
+// kept): the shading kernel samples a light at a medium scatter point and at
+// a surface, and one copy instead of two shortens its instruction stream,
+// but the call's register saves cost more (1920 x 1080 x 64 medium scene:
+// 158.0 against 160.0 M paths/s).
 #ifndef VVPT_SHADE_OUTLINE
-#define VVPT_SHADE_OUTLINE 1
+#define VVPT_SHADE_OUTLINE 0
 #endif
 #if VVPT_SHADE_OUTLINE
 #define VVPT_SHADE_FN __noinline__
