@@ -313,6 +313,16 @@ __device__ __forceinline__ float srgb_to_linear(float c)
 {
     return c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
 }
+// srgb_to_linear(k / 255) for the 256 values of an 8-bit channel, written by
+// k_init_slots at the start of every render (the same expression, so the
+// same bits as evaluating it per texel). A table read instead of three powf
+// per texel keeps the shading kernels' code short: every texture lookup is
+// inlined and fetches up to five texels.
+// (VVPT_SRGB_LUT = 0 evaluates it per texel, for comparison.)
+#ifndef VVPT_SRGB_LUT
+#define VVPT_SRGB_LUT 1
+#endif
+__device__ float vvpt_srgb_lut[256];
 __device__ __forceinline__ float4 texel(const SceneView &s, const DevTexture &t, int x, int y)
 {
     size_t i = (size_t)y * t.width + (size_t)x;
@@ -320,6 +330,11 @@ __device__ __forceinline__ float4 texel(const SceneView &s, const DevTexture &t,
         return __ldg(reinterpret_cast<const float4 *>(s.texels + t.offset) + i);
     }
     uchar4 c = __ldg(reinterpret_cast<const uchar4 *>(s.texels + t.offset) + i);
+#if VVPT_SRGB_LUT
+    if (t.format == 1)
+        return make_float4(vvpt_srgb_lut[c.x], vvpt_srgb_lut[c.y], vvpt_srgb_lut[c.z], c.w / 255.0f);
+    return make_float4(c.x / 255.0f, c.y / 255.0f, c.z / 255.0f, c.w / 255.0f);
+#else
     float4 v = make_float4(c.x / 255.0f, c.y / 255.0f, c.z / 255.0f, c.w / 255.0f);
     if (t.format == 1) {
         v.x = srgb_to_linear(v.x);
@@ -327,6 +342,7 @@ __device__ __forceinline__ float4 texel(const SceneView &s, const DevTexture &t,
         v.z = srgb_to_linear(v.z);
     }
     return v;
+#endif
 }
 __device__ __forceinline__ int wrap_repeat(int i, int n)
 {

@@ -417,6 +417,8 @@ __global__ void k_init_slots(Queues q, PathState ps, JobTable jt, uint32_t slots
         ps.item[i] = 0xFFFFFFFFu;
         ps.job[i] = 0u;
     }
+    if (blockIdx.x == 0)
+        vvpt_srgb_lut[threadIdx.x & 255u] = srgb_to_linear((float)(threadIdx.x & 255u) / 255.0f);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int c = 0; c < C_COUNT; c++)
             q.counters[c] = 0u;
