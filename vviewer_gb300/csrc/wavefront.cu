@@ -1042,34 +1042,18 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
             float vtend = is_hit ? hv.x : fminf(p.zfar_trunc, kExtTmax);
             sampled_medium = medium_event(s, p, vol, kExtTmin, vtend, origin, dir, beta, rng, scatter_pos, g);
         }
+        // The event's own part first; an event that samples a light (a
+        // scatter point in a medium, or a surface the path continues from)
+        // then samples it at one call site, so that the light-sampling code
+        // (mesh lights, environment) is inlined once; the evaluation after it
+        // follows per event. The random numbers are drawn in the same order.
+        SurfaceHit h;
+        bool lambert = false, surface_light = false;
+        float3 albedo = f3(0.0f);
+        PBR pbr;
         if (sampled_medium) {
             // light sample at the scatter point with the HG phase function
-            // (process_volume_hit.glsl:42-79)
-            float3 wo = -normalize3(dir);
-            // in background mode 2 an escape before any surface event sees
-            // the solid colour, so the environment is not a light there
-            LightSample ls = sample_light(s, p, scatter_pos, rng, !last && !((int)p.env_type == 2 && sdepth == 0));
-            if (!is_black(ls.radiance)) {
-                float ph = henyey_greenstein(dot3(wo, ls.dir), g);
-                float3 F = f3(ph);
-                if (!is_black(F)) {
-                    float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, ph);
-                    has_shadow = true;
-                    sh_dir = ls.dir;
-                    sh_tmax = ls.tmax;
-                    sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
-                }
-            }
-            float3 wi;
-            const float2 uu = rnd2(p, rng);
-            const float u0 = uu.x, u1 = uu.y;
-            float spdf = hg_sample(wo, wi, u0, u1, g);
-            origin = scatter_pos;
-            dir = wi;
-            has_nee = true;
-            sampled = true;
-            nee_beta = beta;
-            nee_pdf = spdf;
+            // (process_volume_hit.glsl:42-79), below
         } else if (!is_hit) {
             // miss: background (rayPrimary.rmiss.glsl:53-103)
             stop = true;
@@ -1108,10 +1092,10 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
         } else {
             // surface event
             const uint32_t prim = __float_as_uint(hv.w);
-            SurfaceHit h = make_surface_hit(s, inst_id, prim, hv.y, hv.z, dir);
+            h = make_surface_hit(s, inst_id, prim, hv.y, hv.z, dir);
             const DevMaterial &m = s.materials[h.material];
             const float2 tuv = make_float2(h.uv.x * m.uv_tiling.x, h.uv.y * m.uv_tiling.y);
-            const bool lambert = KIND == 3 ? (uint32_t)m.uv_tiling.z == 2u : KIND == 0;
+            lambert = KIND == 3 ? (uint32_t)m.uv_tiling.z == 2u : KIND == 0;
             bool passthrough = false;
             if (m.mrao.w > 0.0f) {
                 float alpha = material_alpha(s, m, tuv);
@@ -1136,9 +1120,8 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
             } else {
                 float4 nm = tex2d(s, m.tex2[1], tuv.x, tuv.y);
                 apply_normal_to_frame(h.frame, normal_from_normal_map(f3(nm)));
-                float3 albedo = f3(m.albedo) * f3(tex2d(s, m.tex1[0], tuv.x, tuv.y));
+                albedo = f3(m.albedo) * f3(tex2d(s, m.tex1[0], tuv.x, tuv.y));
                 float3 emissive = material_emissive(s, m, tuv);
-                PBR pbr;
                 if (!lambert) {
                     pbr.albedo = albedo;
                     pbr.metallic = m.mrao.x * tex2d(s, m.tex1[1], tuv.x, tuv.y).x;
@@ -1157,61 +1140,93 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
                     terminal_no_rr = true;
                 } else {
                     sdepth = min(sdepth + 1u, 255u);
-                    const float3 wo = world_to_local(h.frame, -dir);
-                    LightSample ls = sample_light(s, p, h.wpos, rng, !last);
-                    if (!is_black(ls.radiance)) {
-                        float3 wi = world_to_local(h.frame, ls.dir);
-                        float3 F;
-                        float bpdf;
-                        if (lambert) {
-                            float ct = fminf(fmaxf(wi.y, 0.0f), 1.0f);
-                            F = albedo * kInvPi * ct;
-                            bpdf = cosine_hemisphere_pdf(ct);
-                        } else {
-                            F = eval_pbr(pbr, wi, wo, normalize3(wo + wi));
-                            bpdf = ls.delta ? 0.0f : pdf_pbr(wi, wo, pbr);
-                        }
-                        if (!is_black(F)) {
-                            float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, bpdf);
-                            has_shadow = true;
-                            sh_dir = ls.dir;
-                            sh_tmax = ls.tmax;
-                            sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
-                        }
-                    }
-                    // BSDF sampling
-                    float spdf;
-                    float3 sdir_local;
-                    bool black_f = false;
-                    float3 Fs;
-                    if (lambert) {
-                        const float2 uu = rnd2(p, rng);
-                        const float u0 = uu.x, u1 = uu.y;
-                        sdir_local = cosine_sample_hemisphere(u0, u1, spdf);
-                    } else {
-                        const float2 uu = rnd2(p, rng);
-                        const float u0 = uu.x, u1 = uu.y;
-                        float r = rnd1(p, rng);
-                        Fs = sample_pbr(sdir_local, wo, spdf, pbr, u0, u1, r);
-                        black_f = is_black(Fs);
-                    }
-                    float3 sdir = local_to_world(h.frame, sdir_local);
-                    origin = h.wpos;
-                    dir = sdir;
-                    if (lambert) {
-                        beta *= albedo;
-                        has_nee = true;
-                    } else if (black_f) {
-                        stop = true;
-                        terminal_no_rr = true;
-                    } else {
-                        beta *= clamp3(Fs / spdf, 0.0f, 1.0f);
-                        has_nee = true;
-                    }
-                    sampled = has_nee;
-                    nee_beta = beta;
-                    nee_pdf = spdf;
+                    surface_light = true;
                 }
+            }
+        }
+        if (sampled_medium || surface_light) {
+            // in background mode 2 an escape before any surface event sees
+            // the solid colour, so the environment is not a light there
+            const LightSample ls =
+                sample_light(s, p, sampled_medium ? scatter_pos : h.wpos, rng,
+                             sampled_medium ? !last && !((int)p.env_type == 2 && sdepth == 0) : !last);
+            if (sampled_medium) {
+                float3 wo = -normalize3(dir);
+                if (!is_black(ls.radiance)) {
+                    float ph = henyey_greenstein(dot3(wo, ls.dir), g);
+                    float3 F = f3(ph);
+                    if (!is_black(F)) {
+                        float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, ph);
+                        has_shadow = true;
+                        sh_dir = ls.dir;
+                        sh_tmax = ls.tmax;
+                        sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
+                    }
+                }
+                float3 wi;
+                const float2 uu = rnd2(p, rng);
+                const float u0 = uu.x, u1 = uu.y;
+                float spdf = hg_sample(wo, wi, u0, u1, g);
+                origin = scatter_pos;
+                dir = wi;
+                has_nee = true;
+                sampled = true;
+                nee_beta = beta;
+                nee_pdf = spdf;
+            } else {
+                const float3 wo = world_to_local(h.frame, -dir);
+                if (!is_black(ls.radiance)) {
+                    float3 wi = world_to_local(h.frame, ls.dir);
+                    float3 F;
+                    float bpdf;
+                    if (lambert) {
+                        float ct = fminf(fmaxf(wi.y, 0.0f), 1.0f);
+                        F = albedo * kInvPi * ct;
+                        bpdf = cosine_hemisphere_pdf(ct);
+                    } else {
+                        F = eval_pbr(pbr, wi, wo, normalize3(wo + wi));
+                        bpdf = ls.delta ? 0.0f : pdf_pbr(wi, wo, pbr);
+                    }
+                    if (!is_black(F)) {
+                        float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, bpdf);
+                        has_shadow = true;
+                        sh_dir = ls.dir;
+                        sh_tmax = ls.tmax;
+                        sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * F * beta / ls.pdf;
+                    }
+                }
+                // BSDF sampling
+                float spdf;
+                float3 sdir_local;
+                bool black_f = false;
+                float3 Fs;
+                if (lambert) {
+                    const float2 uu = rnd2(p, rng);
+                    const float u0 = uu.x, u1 = uu.y;
+                    sdir_local = cosine_sample_hemisphere(u0, u1, spdf);
+                } else {
+                    const float2 uu = rnd2(p, rng);
+                    const float u0 = uu.x, u1 = uu.y;
+                    float r = rnd1(p, rng);
+                    Fs = sample_pbr(sdir_local, wo, spdf, pbr, u0, u1, r);
+                    black_f = is_black(Fs);
+                }
+                float3 sdir = local_to_world(h.frame, sdir_local);
+                origin = h.wpos;
+                dir = sdir;
+                if (lambert) {
+                    beta *= albedo;
+                    has_nee = true;
+                } else if (black_f) {
+                    stop = true;
+                    terminal_no_rr = true;
+                } else {
+                    beta *= clamp3(Fs / spdf, 0.0f, 1.0f);
+                    has_nee = true;
+                }
+                sampled = has_nee;
+                nee_beta = beta;
+                nee_pdf = spdf;
             }
         }
         // Russian roulette (russian_roulette.glsl:1-11) for events that reach it
