@@ -1064,6 +1064,9 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
             float wenv = 1.0f;
             if (p.env_light && (flags & F_SAMPLED))
                 wenv = power_heuristic(ps.nee_b[slot].w, env_pdf(s, dir) / (float)(p.num_lights + 1u));
+            // one environment lookup for modes 1 and 2 (one inlined copy)
+            const bool env_seen = mode == 1 || (mode == 2 && sdepth != 0);
+            const float3 envc = env_seen ? env_lookup(s, dir) : f3(0.0f);
             if (mode == 0) {
                 if (sdepth == 0) {
                     write_alb = true;
@@ -1072,7 +1075,7 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
                 }
                 rad += p.background * beta;
             } else if (mode == 1) {
-                float3 bg = p.env_intensity * env_lookup(s, dir);
+                float3 bg = p.env_intensity * envc;
                 if (sdepth == 0) {
                     write_alb = true;
                     new_alb = bg;
@@ -1086,7 +1089,7 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
                     new_nrm = f3(0.0f);
                     rad += p.background * beta;
                 } else {
-                    rad += env_lookup(s, dir) * beta * wenv;
+                    rad += envc * beta * wenv;
                 }
             }
         } else {
