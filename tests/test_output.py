@@ -1,4 +1,4 @@
-"""The output step (SURVEY row a20 / f4): exposure, sRGB 8-bit PNG, RGBE HDR
+"""The output step: exposure, sRGB 8-bit PNG, RGBE HDR
 and the AOV file set, against the reference's own rules restated here in
 float32 arithmetic:
   * applyExposure / tonemap (src/lib/vengine/core/ImageUtils.cpp:34-49):
