@@ -169,7 +169,8 @@ void refresh_weights(vvpt_denoiser *dn, cudaStream_t s)
     dn->weights_dirty = false;
 }
 
-void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, bool out_f32, cudaStream_t s)
+void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, bool out_f32, cudaStream_t s,
+              float4 *rgba = nullptr)
 {
     const Layer &L = dn->layers[li];
     vvdn::ConvArgs a{};
@@ -185,6 +186,7 @@ void conv_fwd(vvpt_denoiser *dn, int li, const bf16 *in, void *out, int level, b
     a.n = dn->n;
     a.h = dn->h >> level;
     a.wd = dn->w >> level;
+    a.rgba = rgba;
     vvdn::conv3x3(a, s, dn->mma_sync ? nullptr : dn->err.as<uint32_t>(), dn->conv_kind);
 }
 
@@ -244,8 +246,10 @@ void conv_wgrad(vvpt_denoiser *dn, int li, const bf16 *dout, const bf16 *in, int
 // concat(upsample(coarse), skip) straight from both tensors where the strip
 // kernel takes it; training keeps the concatenated tensor for the weight
 // gradient
+// rgba (inference, tcgen05 kernels): the output layer writes the final RGBA
+// frame there instead of out_f32
 void forward(vvpt_denoiser *dn, const float *rad, const float *alb, const float *nrm, cudaStream_t s,
-             bool fuse_concat = false)
+             bool fuse_concat = false, float *rgba = nullptr)
 {
     refresh_weights(dn, s);
     const int n = dn->n;
@@ -268,7 +272,8 @@ void forward(vvpt_denoiser *dn, const float *rad, const float *alb, const float 
         }
         conv_fwd(dn, li + 1, act(dn, dn->b[l]), act(dn, dn->d[l]), l, false, s);
     }
-    conv_fwd(dn, kLayers - 1, act(dn, dn->d[0]), dn->out_f32.as<float>(), 0, true, s);
+    conv_fwd(dn, kLayers - 1, act(dn, dn->d[0]), dn->out_f32.as<float>(), 0, true, s,
+             dn->mma_sync ? nullptr : reinterpret_cast<float4 *>(rgba));
 }
 
 void backward(vvpt_denoiser *dn, cudaStream_t s)
@@ -510,8 +515,10 @@ VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *dn, const float *radianc
     if ((st = ensure_shape(dn, 1, (int)height, (int)width, false)) != VVPT_OK)
         return st;
     cudaStream_t s = vv_stream(ctx);
-    forward(dn, radiance, albedo, normal, s, true);
-    vvdn::unpack_output(dn->out_f32.as<float>(), kOutCh, out, (int)(width * height), s);
+    const bool fused_out = !dn->mma_sync && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    forward(dn, radiance, albedo, normal, s, true, fused_out ? out : nullptr);
+    if (!fused_out)
+        vvdn::unpack_output(dn->out_f32.as<float>(), kOutCh, out, (int)(width * height), s);
     VV_CUDA(cudaGetLastError(), "denoiser kernels");
     return check_device_status(dn, s);
 }

@@ -647,6 +647,13 @@ __device__ __forceinline__ void store_row16(const ConvArgs &a, long p, int c, co
         if (a.relu)
             v[k] = fmaxf(v[k], 0.0f);
     }
+    if (a.rgba) {
+        // the output unpacking of the frame, in the epilogue (k_unpack_output)
+        if (c == 0)
+            a.rgba[p] = make_float4(expm1f(fmaxf(v[0], 0.0f)), expm1f(fmaxf(v[1], 0.0f)), expm1f(fmaxf(v[2], 0.0f)),
+                                    1.0f);
+        return;
+    }
     const long o = p * a.cout + c;
     if (a.mask) {
         __align__(16) bf16 m[16];

@@ -29,6 +29,9 @@ struct ConvArgs {
     // [cc, cin) from `in` ([P][cin - cc]). cc = 0: `in` holds all cin.
     const bf16 *coarse;
     int cc;
+    // Output layer at inference (tcgen05 kernels): the frame written as RGBA
+    // f32, expm1(max(y, 0)) of channels 0-2 and alpha 1, instead of `out`.
+    float4 *rgba;
 };
 
 enum ConvKernels {

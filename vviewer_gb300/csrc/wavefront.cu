@@ -1716,6 +1716,9 @@ __device__ __forceinline__ bool shadow_walk_next(ShadowWalk &w, Hit &after, Trac
 #ifndef VVPT_SHADOW_REFILL
 #define VVPT_SHADOW_REFILL 0
 #endif
+#ifndef VVPT_SHADOW_REFILL_BELOW
+#define VVPT_SHADOW_REFILL_BELOW VVPT_REFILL_BELOW
+#endif
 
 __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable jt, PathState ps, Queues q)
 {
@@ -1744,7 +1747,7 @@ __global__ void __launch_bounds__(256, VVPT_TRACE_MIN_BLOCKS) k_shadow(JobTable 
     bool open = true; // warp-uniform: the queues may still hold rays
     for (;;) {
         uint32_t tr = __ballot_sync(0xFFFFFFFFu, state == kLaneTracing);
-        if (__popc(tr) <= VVPT_REFILL_BELOW) {
+        if (__popc(tr) <= VVPT_SHADOW_REFILL_BELOW) {
             if (state == kLaneDone) {
                 const JobView &J = jt.jobs[job];
                 const float4 ct = cold_t[threadIdx.x];
