@@ -709,6 +709,15 @@ __device__ __forceinline__ uint32_t extend_key(const SceneView &s, const Hit &h,
 #define VVPT_REFILL_BELOW 16
 #endif
 constexpr uint32_t kLaneFree = 0, kLaneTracing = 1, kLaneDone = 2;
+// Step turns (k_extend): triangle tests and the other kinds of step in
+// separate warp steps, triangle tests when at least VVPT_TRI_TURN_PCT % of
+// the tracing lanes have one pending.
+#ifndef VVPT_STEP_TURNS
+#define VVPT_STEP_TURNS 1
+#endif
+#ifndef VVPT_TRI_TURN_PCT
+#define VVPT_TRI_TURN_PCT 33
+#endif
 
 // Hands the next queue entries to the free lanes of the warp: returns the
 // entry index of this lane (meaningful when `mine`), and clears `open` when
@@ -789,8 +798,21 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
                 continue;
             }
         }
+#if VVPT_STEP_TURNS
+        // triangle tests and node visits in separate warp steps: triangle
+        // tests run when enough of the tracing lanes have one pending, the
+        // other kinds of step otherwise (a lane whose kind is not this
+        // step's waits; every lane's kind gets its turn, since the lanes
+        // that step move on to a leaf, finish, or leave the tracing set)
+        const bool tri = state == kLaneTracing && st.leaf_count > 0;
+        const bool tri_turn =
+            100 * __popc(__ballot_sync(0xFFFFFFFFu, tri)) >= VVPT_TRI_TURN_PCT * __popc(tr);
+        if (state == kLaneTracing && tri == tri_turn && !trace_step(st, stack, jt.jobs[job].scene, no_hit(), err))
+            state = kLaneDone;
+#else
         if (state == kLaneTracing && !trace_step(st, stack, jt.jobs[job].scene, no_hit(), err))
             state = kLaneDone;
+#endif
     }
 #else
     if (first_ray() < n)
