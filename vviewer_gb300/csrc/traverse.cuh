@@ -590,14 +590,34 @@ __device__ __forceinline__ bool trace_step(TraceState &st, TraceStack &stack, co
     return true;
 }
 
+// VVPT_TRACE_TURNS: the lanes that run this loop together take triangle
+// tests and the other kinds of step in separate steps (as the extension
+// kernel's refill loop does), triangle tests when at least
+// VVPT_TRACE_TURN_PCT % of them have one pending.
+#ifndef VVPT_TRACE_TURNS
+#define VVPT_TRACE_TURNS 0
+#endif
+#ifndef VVPT_TRACE_TURN_PCT
+#define VVPT_TRACE_TURN_PCT 33
+#endif
 __device__ __forceinline__ Hit trace_after(const SceneView &s, const float3 &o, const float3 &d, float tmin, float tmax,
                                            const Hit &after, uint32_t &err)
 {
     TraceState st;
     TraceStack stack;
     trace_begin(st, s, o, d, tmin, tmax, after);
+#if VVPT_TRACE_TURNS && defined(__CUDA_ARCH__)
+    for (;;) {
+        const uint32_t act = __activemask();
+        const bool tri = st.leaf_count > 0;
+        const bool turn = 100 * __popc(__ballot_sync(act, tri)) >= VVPT_TRACE_TURN_PCT * __popc(act);
+        if (tri == turn && !trace_step(st, stack, s, after, err))
+            break;
+    }
+#else
     while (trace_step(st, stack, s, after, err)) {
     }
+#endif
     return st.best;
 }
 
