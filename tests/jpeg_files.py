@@ -109,12 +109,14 @@ class _Writer:
             self.put((1 << (8 - self.n)) - 1, 8 - self.n)
 
 
-def encode_jpeg(rgb: np.ndarray, quality: float = 1.0, subsample: bool = True, restart: int = 0,
+def encode_jpeg(rgb: np.ndarray, quality: float = 1.0, subsample: bool | tuple = True, restart: int = 0,
                 return_coefficients: bool = False):
     """rgb: H x W x 3 (or H x W for grey) uint8. quality scales a flat-ish
-    quantisation table (1.0: steps of 1-3). With return_coefficients also the
-    quantised coefficients per component ([block row, block column, 64],
-    zigzag order) and the quantisation table (8 x 8)."""
+    quantisation table (1.0: steps of 1-3). subsample: True for 4:2:0, False
+    for 4:4:4, or the luma sampling factors (h, v), e.g. (2, 1) for 4:2:2.
+    With return_coefficients also the quantised coefficients per component
+    ([block row, block column, 64], zigzag order) and the quantisation table
+    (8 x 8)."""
     img = np.asarray(rgb, dtype=np.float64)
     grey = img.ndim == 2
     h, w = img.shape[:2]
@@ -128,12 +130,14 @@ def encode_jpeg(rgb: np.ndarray, quality: float = 1.0, subsample: bool = True, r
         cb = -0.168736 * r - 0.331264 * g + 0.5 * b + 128.0
         cr = 0.5 * r - 0.418688 * g - 0.081312 * b + 128.0
         if subsample:
+            sh, sv = (2, 2) if subsample is True else subsample
+
             def half(p):
-                hh, ww = (h + 1) // 2, (w + 1) // 2
-                pp = np.pad(p, ((0, 2 * hh - h), (0, 2 * ww - w)), mode="edge")
-                return pp.reshape(hh, 2, ww, 2).mean(axis=(1, 3))
+                hh, ww = (h + sv - 1) // sv, (w + sh - 1) // sh
+                pp = np.pad(p, ((0, sv * hh - h), (0, sh * ww - w)), mode="edge")
+                return pp.reshape(hh, sv, ww, sh).mean(axis=(1, 3))
             planes = [y, half(cb), half(cr)]
-            samp = [(2, 2), (1, 1), (1, 1)]
+            samp = [(sh, sv), (1, 1), (1, 1)]
         else:
             planes = [y, cb, cr]
             samp = [(1, 1)] * 3

@@ -25,7 +25,7 @@ def _psnr(a, b):
 
 
 @pytest.mark.parametrize("h,w", [(8, 8), (37, 53), (16, 33), (1, 1)])
-@pytest.mark.parametrize("subsample", [False, True])
+@pytest.mark.parametrize("subsample", [False, True, (2, 1), (1, 2)])
 def test_coefficients_match_the_encoder(h, w, subsample):
     data, coefs, q = encode_jpeg(_image(h, w), subsample=subsample, return_coefficients=True)
     frame, qt = decode_jpeg_coefficients(data, "t.jpg")
@@ -55,7 +55,7 @@ def test_inverse_dct_follows_the_formula():
                 assert abs(int(out[by * 8 + y, bx * 8 + x, 0]) - ref) <= (0 if abs(s % 1 - 0.5) > 1e-9 else 1)
 
 
-@pytest.mark.parametrize("subsample,min_psnr", [(False, 45.0), (True, 37.0)])
+@pytest.mark.parametrize("subsample,min_psnr", [(False, 45.0), (True, 37.0), ((2, 1), 39.0), ((1, 2), 39.0)])
 def test_round_trip_quality(subsample, min_psnr):
     img = _image(37, 53)
     out, channels = decode_jpeg(encode_jpeg(img, subsample=subsample), "t.jpg")
