@@ -588,6 +588,25 @@ VVPT_API vvpt_status vvpt_denoiser_apply(vvpt_denoiser *denoiser,
                                          uint32_t width,
                                          uint32_t height);
 
+/* ---- Model textures -------------------------------------------------------
+ *
+ * Replaces stb_image's JPEG path in assimpLoadTextureData
+ * (src/lib/vengine/core/io/AssimpLoadModel.cpp): sequential Huffman JPEG
+ * (ITU-T T.81 baseline and extended, 8-bit, grey or YCbCr with sampling
+ * factors 1 and 2, restart intervals) decoded on the host to RGBA8 (grey
+ * replicated to RGB; alpha 255). With rgba = NULL only width, height and
+ * channels (1 or 3) are returned; otherwise rgba must hold width * height * 4
+ * bytes. Progressive, lossless, arithmetic-coded and 12-bit files return
+ * VVPT_ERR_UNSUPPORTED; malformed files VVPT_ERR_INVALID_ARG. No context or
+ * GPU is needed. */
+VVPT_API vvpt_status vvpt_jpeg_decode(const uint8_t *data,
+                                      uint64_t size,
+                                      uint32_t *width,
+                                      uint32_t *height,
+                                      uint32_t *channels,
+                                      uint8_t *rgba,
+                                      uint64_t rgba_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,16 +1,20 @@
 """JPEG texture decoding (vengine reads model textures through stb_image,
 AssimpLoadModel.cpp:assimpLoadTextureData, which decodes JPEG as well as PNG).
 The files come from the small baseline encoder in jpeg_files.py, which also
-returns the quantised coefficients it wrote, so the entropy decoder is checked
-coefficient for coefficient and the reconstruction against a direct
-evaluation of the T.81 inverse DCT formula."""
+returns the quantised coefficients it wrote. The Python restatement
+(jpeg_reference.py) is checked coefficient for coefficient against the
+encoder and its reconstruction against a direct evaluation of the T.81 inverse
+DCT formula; libvvpt's host decoder (vvpt_jpeg_decode, what model import
+uses) is checked against the restatement. No GPU is needed."""
 import math
 
 import numpy as np
 import pytest
 
 from jpeg_files import ZIGZAG, encode_jpeg
-from vviewer_gb300.jpeg import decode_jpeg, decode_jpeg_coefficients
+from jpeg_reference import decode_jpeg as decode_jpeg_py
+from jpeg_reference import decode_jpeg_coefficients
+from vviewer_gb300.jpeg import decode_jpeg
 
 
 def _image(h, w, seed=1):
@@ -151,3 +155,40 @@ def test_gltf_embedded_jpeg_is_decoded(tmp_path):
     import_model(e, b.save(tmp_path / "photo.glb"), name="photo")
     p = e.material("photo:Photo")
     assert np.array_equal(e.textures[p.albedo_texture][1], decode_jpeg(data)[0]) and not p.transparent
+
+
+@pytest.mark.parametrize("subsample", [False, True, (2, 1), (1, 2)])
+@pytest.mark.parametrize("h,w,restart", [(37, 53, 0), (64, 48, 3), (9, 130, 1)])
+def test_native_decoder_matches_the_restatement(subsample, h, w, restart):
+    """libvvpt's decoder against the Python restatement of the same steps:
+    the same texels (an IDCT summed in another order may round a .5 tie the
+    other way: at most one unit, on few texels)."""
+    data = encode_jpeg(_image(h, w, seed=h + w), quality=2.0, subsample=subsample, restart=restart)
+    a, ca = decode_jpeg(data, "n.jpg")
+    b, cb = decode_jpeg_py(data, "p.jpg")
+    assert ca == cb == 3 and a.shape == b.shape == (h, w, 4)
+    diff = np.abs(a.astype(int) - b.astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() < 1e-3
+
+
+def test_native_decoder_survives_corrupt_files():
+    """Truncated and byte-flipped files give an error status or an image,
+    never a crash or an out-of-range read."""
+    rng = np.random.default_rng(0)
+    bases = [encode_jpeg(_image(24, 40, seed=2), restart=2, subsample=s) for s in (False, True)]
+    bases.append(encode_jpeg(_image(16, 16, seed=3)[..., 0]))
+    decoded = failed = 0
+    for k in range(3000):
+        d = bytearray(bases[k % 3])
+        if k % 2:
+            d = d[:rng.integers(2, len(d))]
+        else:
+            for _ in range(rng.integers(1, 6)):
+                d[rng.integers(2, len(d))] = rng.integers(0, 256)
+        try:
+            img, _ = decode_jpeg(bytes(d), "f.jpg")
+            assert img.dtype == np.uint8 and img.ndim == 3
+            decoded += 1
+        except ValueError:
+            failed += 1
+    assert decoded + failed == 3000 and failed > 0

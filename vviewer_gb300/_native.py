@@ -202,6 +202,8 @@ _SIGNATURES = {
     "vvpt_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.POINTER(SceneData),
                                     C.POINTER(RenderInfo), C.POINTER(Outputs)]),
     "vvpt_sampler_tables": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vvpt_jpeg_decode": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_uint32), C.c_void_p, C.c_uint64]),
 }
 
 _lib = None
