@@ -576,8 +576,8 @@ VVPT_API vvpt_status vvpt_render(vvpt_ctx *ctx, vvpt_scene *scene, const vvpt_sc
                     VV_CUDA(cudaEventSynchronize(kb), "profile kernel");
                     float ms = 0.0f;
                     cudaEventElapsedTime(&ms, ka, kb);
-                    prof.kernels[k].launches += 1;
-                    prof.kernels[k].units += units;
+                    prof.kernels[k].launches += (uint64_t)launches_of(k);
+                    prof.kernels[k].units += launches_of(k) ? units : 0;
                     prof.kernels[k].total_ms += ms;
                     stats.kernel_launches += launches_of(k);
                 }

@@ -702,9 +702,6 @@ __device__ __forceinline__ uint32_t extend_key(const SceneView &s, const Hit &h,
 // ray ends, and the code between traversals runs for many lanes at once.
 // Per-lane values that only that code reads stay in shared memory (one entry
 // per thread), so the traversal state keeps the registers. Binary BLAS only.
-#ifndef VVPT_EXTEND_REFILL
-#define VVPT_EXTEND_REFILL (!VVPT_BLAS_WIDE)
-#endif
 #ifndef VVPT_REFILL_BELOW
 #define VVPT_REFILL_BELOW 16
 #endif
@@ -756,6 +753,9 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
     for (;;) {
         uint32_t tr = __ballot_sync(0xFFFFFFFFu, state == kLaneTracing);
         if (__popc(tr) <= VVPT_REFILL_BELOW) {
+            // finished rays go straight to the shade queues (material
+            // bins) and the emitter-walk queue: warp-uniform appends
+            uint32_t fin_slot = 0, fin_key = 0xFFu, fin_i = 0;
             if (state == kLaneDone) {
                 const uint4 c = cold[threadIdx.x];
                 const SceneView &s = jt.jobs[job].scene;
@@ -773,10 +773,31 @@ __global__ void __launch_bounds__(256, VVPT_EXTEND_MIN_BLOCKS) k_extend(JobTable
                 } else {
                     ps.hit[c.y] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
                     ps.hit_inst[c.y] = h.inst;
-                    q.ext_key[c.x] = extend_key(s, h, fused, key);
+                    fin_slot = c.y;
+                    fin_i = c.x;
+                    fin_key = extend_key(s, h, fused, key);
                     state = kLaneFree;
                 }
             }
+#if VVPT_EXTEND_PARTITION
+            const uint32_t bin = fin_key & 3u;
+            uint32_t pos = warp_append_all(bin == 0, &q.counters[C_SHADE_L]);
+            if (bin == 0)
+                q.shade_l[pos] = fin_slot;
+            pos = warp_append_all(bin == 1, &q.counters[C_SHADE_P]);
+            if (bin == 1)
+                q.shade_p[pos] = fin_slot;
+            pos = warp_append_all(bin == 2, &q.counters[C_SHADE_M]);
+            if (bin == 2)
+                q.shade_m[pos] = fin_slot;
+            const bool walk = fin_key != 0xFFu && (fin_key & 4u);
+            pos = warp_append_all(walk, &q.counters[C_WALK]);
+            if (walk)
+                q.walk[pos] = fin_slot;
+#else
+            if (fin_key != 0xFFu)
+                q.ext_key[fin_i] = fin_key;
+#endif
             if (open) {
                 bool mine;
                 const uint32_t i = refill_take(state == kLaneFree, &q.counters[C_FETCH_EXT], n, open, mine);
@@ -2006,7 +2027,8 @@ void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Qu
         k_extend<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q, pp);
         break;
     case K_PARTITION:
-        k_partition<<<shape.grid, shape.block, 0, stream>>>(ps, q, pp);
+        if (kPartitionLaunches)
+            k_partition<<<shape.grid, shape.block, 0, stream>>>(ps, q, pp);
         break;
     case K_WALK:
         k_walk<<<shape.grid, shape.block, kTlasCacheBytes, stream>>>(jt, ps, q);

@@ -171,9 +171,25 @@ enum KernelId {
 #ifndef VVPT_SHADE_SPLIT
 #define VVPT_SHADE_SPLIT 0
 #endif
+// Lane refill in the extension kernel (binary BLAS). With
+// VVPT_EXTEND_PARTITION = 1 (a build option, measured, not kept) the refill
+// kernel also appends its hits to the material-sorted shade queues and the
+// emitter-walk queue itself and k_partition is not launched: the extension
+// kernel grew by what the partition launch took (1920 x 1080 x 64 medium
+// scene: 174.3 against 174.5 M paths/s).
+#ifndef VVPT_EXTEND_REFILL
+#define VVPT_EXTEND_REFILL (!VVPT_BLAS_WIDE)
+#endif
+#ifndef VVPT_EXTEND_PARTITION
+#define VVPT_EXTEND_PARTITION 0
+#endif
 constexpr int kShadeLaunches = VVPT_SHADE_SPLIT ? 3 : 1;
-constexpr int launches_of(int k) { return k == K_SHADE ? kShadeLaunches : 1; }
-constexpr int kKernelsPerIteration = K_NUM + kShadeLaunches - 1;
+constexpr int kPartitionLaunches = (VVPT_EXTEND_REFILL && VVPT_EXTEND_PARTITION) ? 0 : 1;
+constexpr int launches_of(int k)
+{
+    return k == K_SHADE ? kShadeLaunches : (k == K_PARTITION ? kPartitionLaunches : 1);
+}
+constexpr int kKernelsPerIteration = K_NUM + kShadeLaunches - 1 + kPartitionLaunches - 1;
 void launch_kernel(KernelId k, const JobTable &jt, const PathState &ps, const Queues &q, int pingpong,
                    const LaunchShape &shape, cudaStream_t stream);
 
