@@ -728,7 +728,8 @@ __device__ __forceinline__ uint32_t refill_take(bool free, uint32_t *counter, ui
     if (lane == 0 && cnt)
         base = atomicAdd(counter, cnt);
     base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    open = base + cnt < n;
+    if (cnt)
+        open = base + cnt < n;
     const uint32_t idx = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
     mine = free && idx < n;
     return idx;
