@@ -723,14 +723,14 @@ def run_converged(args) -> None:
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t_train
 
-    # ---- the judged view
+    # ---- the view the served images are measured on
     e, info = scenes.instanced_sky_scene(1, W, H, 16, 8, 4, sky_w=4096, sky_h=2048)
     g = ctx.upload(e.scene.build())
     sd = e.scene.scene_data(W, H)
-    # The judge image takes the low-discrepancy sampler: the same estimator
-    # (same expected image) on sample streams independent of the RTGEMS
-    # streams of the images it judges, whose first batches it would
-    # otherwise share (one seed per batch index).
+    # The reference image takes the low-discrepancy sampler: the same
+    # estimator (same expected image) on sample streams independent of the
+    # RTGEMS streams of the images measured against it, whose first batches
+    # it would otherwise share (one seed per batch index).
     ref, t_ref = render(g, sd, info, ref_spp, W, H, fp64=True, m2=True, sampler="pmj")
     nb = ref_spp // info.batch_size
     x = ref["radiance"][..., :3].double()

@@ -1,6 +1,6 @@
 """Generates tests/golden/medium_converged.npz: the CPU oracle's converged,
-FP64-accumulated render of a small view of the headline scene, the judge of
-the GPU's converged-image test.
+FP64-accumulated render of a small view of the headline scene, the reference
+of the GPU's converged-image test.
 
 Scene: scenes.cornell_medium(seed 4) at its full geometry (the Cornell room
 filled with the homogeneous medium, eight displaced icospheres at frequency
