@@ -814,7 +814,7 @@ def run_converged(args) -> None:
                        "metric": "sqrt(sum((x - ref)^2) / sum(ref^2)) over RGB",
                        "reference": f"{ref_spp} spp, FP64-accumulated batch sums (VVPT_RENDER_REDUCE_FP64), "
                                     "environment importance sampled, PMJ sampler (streams independent of the "
-                                    "judged RTGEMS images)",
+                                    "measured RTGEMS images)",
                        "requests": M, "request_spp": pick["spp"], "request_spp_rule": pick_rule,
                        "train": f"{args.train_steps} steps of 4 x 256^2 crops from {args.train_crops} seeds x "
                                 f"{len(in_spps)} input spp (4/8/16, FP16), {ref_spp}-spp FP64 targets"},
