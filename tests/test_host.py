@@ -81,6 +81,8 @@ def test_null_arguments_are_rejected(native_lib):
     assert native_lib.vvpt_scene_upload(None, None, None) == 1
     assert native_lib.vvpt_render(None, None, None, None, None) == 1
     assert native_lib.vvpt_progress(None, None) == 1
+    assert native_lib.vvpt_set_bvh_builder(None, 2) == 1
+    assert native_lib.vvpt_jpeg_decode(None, 0, None, None, None, None, 0) == 1
     assert native_lib.vvpt_version().startswith(b"vvpt")
 
 
