@@ -1,7 +1,7 @@
 """The compressed 8-wide BLAS layout (build option VVPT_BLAS_WIDE=1,
 csrc/bvh_wide.cpp) on the GPU. The library is built a second time with the
-option into a scratch folder and driven from a child process (one process
-loads one libvvpt.so). Closest hits must be bit-identical to the oracle's, and
+option, in-tree beside the default build, and driven from a child process
+(one process loads one libvvpt.so). Closest hits must be bit-identical to the oracle's, and
 renders bit-identical to the default (binary BLAS) build's: the hit and
 any-hit candidate orders are fixed by (t, instance, primitive), not by the
 BVH, so the node layout cannot change an image."""
@@ -61,8 +61,9 @@ CHILD = textwrap.dedent("""
 def test_wide_blas_build_matches_oracle_and_binary_build(ctx, tmp_path):
     from vviewer_gb300 import build as B
 
-    lib = B.build(force=True, defines=["VVPT_BLAS_WIDE=1"], out=tmp_path / "libvvpt_wide.so",
-                  build_dir=tmp_path / "obj")
+    # in-tree, beside the default build (vviewer_gb300/_lib, _build: not committed)
+    lib = B.build(force=True, defines=["VVPT_BLAS_WIDE=1"], out=B.OUT_DIR / "variants" / "libvvpt_wide.so",
+                  build_dir=B.BUILD_DIR / "wide")
     res_file = tmp_path / "wide.npz"
     script = tmp_path / "child.py"
     script.write_text(CHILD)
