@@ -644,6 +644,18 @@ def run_denoise(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def pick_operating_point(sweep: list, target: float) -> tuple[dict, str]:
+    """The served input spp of the converged workload: the fewest spp whose
+    denoised error meets the target; when none does, the spp where the
+    denoiser gains most over the plain tracer at equal error. Entries are in
+    increasing spp order."""
+    met = [r for r in sweep if r["rel_rmse_denoised"] <= target]
+    if met:
+        return met[0], "fewest spp meeting the target"
+    return (max(sweep, key=lambda r: r["gain_at_equal_error"] or 0.0),
+            "target not met at any spp: largest gain at equal error")
+
+
 def _rel_rmse(img, ref) -> float:
     """Relative RMSE of an image against a reference: the root of
     sum((img - ref)^2) / sum(ref^2) over the pixels and the three radiance
@@ -771,14 +783,7 @@ def run_converged(args) -> None:
                       "plain_spp_same_error": spp_eq if finite else None,
                       # the plain tracer's time for the same error over this render + denoise
                       "gain_at_equal_error": (W * H * spp_eq / paths_per_s) / (t_r + t_d) if finite else None})
-    # operating point: the fewest spp that meet the target; when none does, the
-    # input spp where the denoiser gains most over the plain tracer at equal error
-    met = [r for r in sweep if r["rel_rmse_denoised"] <= target]
-    if met:
-        pick, pick_rule = met[0], "fewest spp meeting the target"
-    else:
-        pick = max(sweep, key=lambda r: r["gain_at_equal_error"] or 0.0)
-        pick_rule = "target not met at any spp: largest gain at equal error"
+    pick, pick_rule = pick_operating_point(sweep, target)
 
     # batched + served + denoised: M requests together through the job engine
     M = args.requests_converged
