@@ -230,28 +230,37 @@ __device__ __forceinline__ float pdf_pbr(const float3 &wi, const float3 &wo, con
     return pd * r + pm * (1.0f - r);
 }
 // samplePBRStandard (pbrStandard.glsl:188-214): draws u0,u1 then rnd
+// The specular lobe's direction: a GGX half vector, mirrored.
+__device__ __forceinline__ float3 ggx_sample_reflect(const float3 &wo, const PBR &p, float u0, float u1)
+{
+    float phi = (2.0f * kPi) * u1;
+    float alpha = p.roughness * p.roughness;
+    float tan2 = alpha * alpha * u0 / (1.0f - u0);
+    float cos_theta = 1.0f / sqrtf(1.0f + tan2);
+    float sin_theta = sqrtf(fmaxf(kEps, 1.0f - cos_theta * cos_theta));
+    float3 wh = f3(sin_theta * cosf(phi), cos_theta, sin_theta * sinf(phi));
+    if (!(wh.y > 0.0f))
+        wh = wh * -1.0f;
+    // reflect(-wo, wh) = -wo - 2 dot(wh, -wo) wh
+    float3 I = -wo;
+    return I - 2.0f * dot3(wh, I) * wh;
+}
+
+// The reference's sampling of the metallic/roughness BSDF: the diffuse lobe
+// with probability diffuse_sampling_ratio, else the specular lobe; the
+// returned pdf is the two-lobe pdf and F the BSDF (zero when the pdf is
+// below kEps). The shading kernel draws the same numbers and makes the same
+// choice with its surface code shared between Lambert and PBR surfaces.
 __device__ __forceinline__ float3 sample_pbr(float3 &wi, const float3 &wo, float &pdf, const PBR &p, float u0, float u1,
                                              float rnd)
 {
     pdf = 0.0f;
     wi = f3(0.0f);
     float r = diffuse_sampling_ratio(p);
-    if (rnd <= r) {
+    if (rnd <= r)
         wi = cosine_sample_hemisphere(u0, u1, pdf);
-    } else {
-        float phi = (2.0f * kPi) * u1;
-        float alpha = p.roughness * p.roughness;
-        float tan2 = alpha * alpha * u0 / (1.0f - u0);
-        float cos_theta = 1.0f / sqrtf(1.0f + tan2);
-        float sin_theta = sqrtf(fmaxf(kEps, 1.0f - cos_theta * cos_theta));
-        float3 wh = f3(sin_theta * cosf(phi), cos_theta, sin_theta * sinf(phi));
-        if (!(wh.y > 0.0f))
-            wh = wh * -1.0f;
-        // reflect(-wo, wh) = -wo - 2 dot(wh, -wo) wh
-        float3 I = -wo;
-        wi = I - 2.0f * dot3(wh, I) * wh;
-        pdf = pdf_disney_microfacet(wi, wo, p);
-    }
+    else
+        wi = ggx_sample_reflect(wo, p, u0, u1);
     float3 F = eval_pbr(p, wi, wo, normalize3(wi + wo));
     pdf = pdf_pbr(wi, wo, p);
     if (pdf < kEps)

@@ -1010,6 +1010,11 @@ __device__ __noinline__ float3 fused_nee(const SceneView &s, const RenderParams 
 // for its own case only (the other surface models are dead code there), so
 // the Lambert and miss kernels fit more resident blocks than the
 // metallic/roughness one.
+// VVPT_SHADE_SHARED_BSDF: one call site for the cosine-weighted warp and one
+// copy of the metallic/roughness evaluation in the surface event.
+#ifndef VVPT_SHADE_SHARED_BSDF
+#define VVPT_SHADE_SHARED_BSDF 1
+#endif
 template <int KIND>
 __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MIN_BLOCKS : VVPT_SHADE_MIN_BLOCKS)
     k_shade(JobTable jt, PathState ps, Queues q, int pp)
@@ -1222,6 +1227,58 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
                 nee_pdf = spdf;
             } else {
                 const float3 wo = world_to_local(h.frame, -dir);
+#if VVPT_SHADE_SHARED_BSDF
+                // The BSDF sample's numbers follow the light sample's, as
+                // always; the cosine-weighted warp serves Lambert surfaces
+                // and the metallic/roughness diffuse lobe from one call site,
+                // and one copy of the metallic/roughness evaluation (a loop
+                // that is not unrolled) takes the light's direction and the
+                // sampled one. Same arithmetic as sample_pbr.
+                const float2 uu = rnd2(p, rng);
+                const float rl = lambert ? 0.0f : rnd1(p, rng);
+                float spdf = 0.0f;
+                float3 sdir_local;
+                if (lambert || rl <= diffuse_sampling_ratio(pbr))
+                    sdir_local = cosine_sample_hemisphere(uu.x, uu.y, spdf);
+                else
+                    sdir_local = ggx_sample_reflect(wo, pbr, uu.x, uu.y);
+                const float3 wil = world_to_local(h.frame, ls.dir);
+                float3 Fl = f3(0.0f), Fsm = f3(0.0f);
+                float pl = 0.0f, psm = 0.0f;
+                if (lambert) {
+                    const float ct = fminf(fmaxf(wil.y, 0.0f), 1.0f);
+                    Fl = albedo * kInvPi * ct;
+                    pl = cosine_hemisphere_pdf(ct);
+                } else {
+#pragma unroll 1
+                    for (int k = 0; k < 2; k++) {
+                        const float3 wi = k == 0 ? wil : sdir_local;
+                        const float3 F = eval_pbr(pbr, wi, wo, normalize3(wo + wi));
+                        const float pd = pdf_pbr(wi, wo, pbr);
+                        if (k == 0) {
+                            Fl = F;
+                            pl = ls.delta ? 0.0f : pd;
+                        } else {
+                            Fsm = F;
+                            psm = pd;
+                        }
+                    }
+                }
+                if (!is_black(ls.radiance) && !is_black(Fl)) {
+                    float w = ls.delta ? 1.0f : power_heuristic(ls.pdf, pl);
+                    has_shadow = true;
+                    sh_dir = ls.dir;
+                    sh_tmax = ls.tmax;
+                    sh_c = (ls.delta ? ls.radiance : w * ls.radiance) * Fl * beta / ls.pdf;
+                }
+                bool black_f = false;
+                float3 Fs = f3(0.0f);
+                if (!lambert) {
+                    spdf = psm;
+                    Fs = psm < kEps ? f3(0.0f) : Fsm;
+                    black_f = is_black(Fs);
+                }
+#else
                 if (!is_black(ls.radiance)) {
                     float3 wi = world_to_local(h.frame, ls.dir);
                     float3 F;
@@ -1258,6 +1315,7 @@ __global__ void __launch_bounds__(256, KIND == 0 || KIND == 2 ? VVPT_SHADE_LM_MI
                     Fs = sample_pbr(sdir_local, wo, spdf, pbr, u0, u1, r);
                     black_f = is_black(Fs);
                 }
+#endif
                 float3 sdir = local_to_world(h.frame, sdir_local);
                 origin = h.wpos;
                 dir = sdir;
