@@ -100,6 +100,21 @@ def profiled_traffic(kernel: str, units_per_launch: float):
     return None, None
 
 
+def profiled_limiter(kernel: str):
+    """The committed ncu summary's issue figures of `kernel` (lines
+    `issue_active[k] = f` and `threads_per_warp_instruction[k] = n`): what
+    bounds a kernel whose HBM roofline fraction is small by construction."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        text = f.read_text()
+        a = re.search(rf"issue_active\[{re.escape(kernel)}\]\s*=\s*([0-9.eE+]+)", text)
+        t = re.search(rf"threads_per_warp_instruction\[{re.escape(kernel)}\]\s*=\s*([0-9.eE+]+)", text)
+        if a and t:
+            return {"kind": "instruction issue under SIMT divergence, then memory latency",
+                    "issue_active": float(a.group(1)), "threads_per_warp_instruction": float(t.group(1)),
+                    "source": f.name}
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -341,7 +356,7 @@ def run_ours(args) -> None:
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": dom["name"], "peak_source": f"{peak_kind} hbm_gbs (copy)",
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
-                "traffic_source": traffic_src,
+                "traffic_source": traffic_src, "limiter": profiled_limiter(dom["name"]),
                 "kernels": [{**k, "share": k["total_ms"] / total_prof} for k in ctx.kernel_profile()]}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
